@@ -1,0 +1,142 @@
+"""ctypes binding of libgpucell_gb300.so (the C ABI in include/gpucell_gb300.h).
+
+The library is the only compute path: if it is missing, importing the
+binding raises instead of falling back to anything else.  Build it with
+``python -c "import __graft_entry__ as g; g.build()"`` (or
+``python -m gpucell_gb300.build``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from .build import LIB_PATH
+
+GC_OK = 0
+GC_FLAG_NONFINITE = 1
+GC_FLAG_BAD_INDEX = 2
+GC_FLAG_CELL_OVERFLOW = 4
+GC_FLAG_STRETCH = 8
+
+
+class Structconst(C.Structure):
+    """ctypes mirror of Structconst (src/TypesDef.cuh:49-78), 96 bytes."""
+
+    _fields_ = [
+        ("nFluidStart", C.c_uint),
+        ("nBound2Start", C.c_uint),
+        ("nCellStart", C.c_uint),
+        ("nTotalPar", C.c_uint),
+        ("nCellPar", C.c_uint),
+        ("iSeed", C.c_long),
+        ("CutRadius", C.c_float),
+        ("Mass", C.c_float),
+        ("SoundSpeed1", C.c_float),
+        ("SoundSpeed2", C.c_float),
+        ("DenInit", C.c_float),
+        ("VVsigma", C.c_float),
+        ("ShearVis", C.c_float),
+        ("BulkVis", C.c_float),
+        ("ConstExtForce", C.c_float),
+        ("TimeStep", C.c_float),
+        ("surEnergy", C.c_float),
+        ("MaxCut", C.c_float),
+        ("zeroLen", C.c_float),
+        ("scaFac", C.c_float),
+        ("Temp", C.c_float),
+    ]
+
+
+assert C.sizeof(Structconst) == 96
+
+_P = C.c_void_p
+_I = C.c_int
+_U = C.c_uint
+_L = C.c_long
+
+# name -> argument types (all return int status unless listed in _RESTYPES)
+_SIGS = {
+    "gc_last_error": [],
+    "gc_version": [],
+    "gc_set_periodic": [_I],
+    "gc_get_periodic": [],
+    "gc_set_noise": [_I],
+    "gc_set_step": [C.c_longlong],
+    "gc_get_step": [],
+    "gc_set_stream": [_P],
+    "gc_device_status": [_P],
+    "gc_shutdown": [],
+    "gc_launch_count": [],
+    "gc_cupar_ConstsDataUp": [_P],
+    "gc_cupar_UpdateFluidCoor": [_I, _P, _P, _P, _P],
+    "gc_cupar_AppFluidPeriodicBC": [_I, _P, _P, _P, _P],
+    "gc_cupar_CalFluidDen": [_I, _P, _P, _P, _P, _P, _P, _P],
+    "gc_cupar_PredictFluidVel": [_I, _P, _P, _P, _P],
+    "gc_cupar_CalBound2Vel": [_I, _P, _P, _P, _P, _P, _P, _P],
+    "gc_cupar_EOS": [_I, _P, _P, _P],
+    "gc_cupar_CalFluidSDPDForce": [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "gc_cupar_CalFluidRepForce": [_I, _P, _P, _P, _P, _P, _P, _P],
+    "gc_cupar_SetFluidExtForce": [_I, _I, _P, _P],
+    "gc_cupar_CorrectFliudVel": [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "gc_cupar_CalGeoPara": [_L, _I, _I] + [_P] * 17,
+    "gc_cupar_SetMechPara": [_I, _I] + [_P] * 14,
+    "gc_cupar_CalCellDefForce": [_I, _U, _U, _U, _U] + [_P] * 27,
+    "gc_cupar_CalCellAggForce": [_U, _U, _U] + [_P] * 10,
+    "gc_cudiv_PreConList": [_I, _I] + [_P] * 8,
+    "gc_cudiv_Sort": [_I, _P, _P],
+    "gc_cudiv_CalBeginEndCube": [_I, _I, _P, _P],
+    "gc_cudiv_SortBasicArrays": [_I] + [_P] * 8,
+    "gc_cudiv_SortArraysWithCells": [_I] + [_P] * 10,
+    "gc_cudiv_Printf": [_I, _P, _P, _P],
+    "gc_debug_neighbor_stats": [_I, _P, _P, _P, _P, _P],
+}
+_RESTYPES = {"gc_last_error": C.c_char_p, "gc_get_step": C.c_longlong, "gc_launch_count": C.c_ulonglong}
+
+_lib = None
+
+
+class GcError(RuntimeError):
+    """A gc_* call returned a non-zero status."""
+
+
+def load(path: str | None = None):
+    """Loads the library (once) and declares every exported signature."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: the CUDA library has not been built "
+                           "(run `python -m gpucell_gb300.build`)")
+    lib = C.CDLL(path)
+    for name, args in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _RESTYPES.get(name, C.c_int)
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+def call(name: str, *args) -> int:
+    """Calls gc_<name> and raises GcError on a non-zero status."""
+    lib = load()
+    rc = getattr(lib, name)(*args)
+    if rc != GC_OK:
+        msg = lib.gc_last_error().decode(errors="replace")
+        raise GcError(f"{name} failed with status {rc}: {msg}")
+    return rc
+
+
+def launch_count() -> int:
+    return int(load().gc_launch_count())
+
+
+def device_status() -> int:
+    lib = load()
+    flags = C.c_uint(0)
+    call("gc_device_status", C.byref(flags))
+    return flags.value

@@ -1,0 +1,301 @@
+// gc_internal.cuh -- shared internals of libgpucell_gb300: the parameter block
+// every kernel receives by value, device helpers (minimum image, cube
+// coordinates, Wendland C2 kernel, Philox pair noise) and the host-side
+// library state.
+//
+// The method these helpers implement is pinned in oracle/oracle.c (the FP64
+// CPU restatement); both follow the same formulas, cited there against the
+// literature, because GPUCell's own kernel bodies are not available.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include "gpucell_gb300.h"
+
+// Block sizes named by src/ParticleGPU.cuh:6 and src/ConfigDomain.cuh:7.
+#ifndef SDPDSIZE
+#define SDPDSIZE 128
+#endif
+#ifndef DIVSIZE
+#define DIVSIZE 128
+#endif
+
+// ---------------------------------------------------------------------------
+// Grid and parameters
+// ---------------------------------------------------------------------------
+
+// Neighbour grid.  Per axis: a periodic axis is cut into floor(L/rc') cubes
+// covering [lo, hi); a wall axis is padded by rc on each side and cut into
+// floor((L + 2 rc)/rc') cubes, as GPUCell's host does for y and z
+// (src/Particle.cu:551-559).  rc' = rc (1 + 1e-4) keeps every cube at least
+// rc wide after FP32 rounding of the cube coordinate.  The cube count never
+// exceeds the reference's SizeCube for the same box.
+struct GcGrid {
+    float lo[3], hi[3];     // bounding box
+    float L[3], halfL[3];   // box lengths
+    float origin[3];        // lower corner of cube 0
+    float invw[3];          // cubes per unit length
+    int   n[3];             // cubes per axis
+    int   ncells;           // n[0]*n[1]*n[2]
+    int   pmask;            // periodic axes (1 = x, 2 = y, 4 = z)
+};
+
+// Everything a kernel needs, passed by value (kernel parameters live in the
+// constant bank, so this costs nothing per thread).
+struct GcParams {
+    // counts and type boundaries (Structconst, src/TypesDef.cuh:49-78)
+    unsigned nB2, nF, nC, nT, nCP;   // nBound2Start, nFluidStart, nCellStart, nTotalPar, nCellPar
+    float rc, inv_rc, rc2;
+    float mass, inv_mass;
+    float c1sq, c2sq;                // SoundSpeed1^2, SoundSpeed2^2
+    float rho0;                      // DenInit
+    float lambda;                    // VVsigma
+    float dt;
+    float gx;                        // ConstExtForce (already times Mass)
+    float kT;
+    // Wendland C2, support rc: W = wnorm (1-s)^4 (1+4s), F = -W'/r = fnorm (1-s)^3
+    float wnorm, fnorm, w0;
+    // SDPD dissipative/random coefficients (Espanol & Revenga 2003)
+    float visA;                      // 5 eta/3 - zeta
+    float visB;                      // 5 (zeta + eta/3)
+    float sqrtA, sqrtAB;             // sqrt(visA), sqrt(visA + visB)
+    float noise_pref;                // 2 kT / dt (0 when the noise is off)
+    // Bound1 repulsion (Monaghan 1994, exponents 12 and 4)
+    float rep_r0, rep_r0sq, rep_D;
+    // Morse aggregation
+    float De, beta, r0m, maxcut, maxcut2;
+    // pair-noise key
+    uint32_t seed_lo, seed_hi;
+    uint32_t step_lo, step_hi;
+    GcGrid g;
+};
+
+// ---------------------------------------------------------------------------
+// Small vector helpers
+// ---------------------------------------------------------------------------
+
+__host__ __device__ inline float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__host__ __device__ inline float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ inline float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ inline float3 operator*(float s, float3 a) { return f3(s * a.x, s * a.y, s * a.z); }
+__host__ __device__ inline float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
+__host__ __device__ inline void operator+=(float3& a, float3 b) { a.x += b.x; a.y += b.y; a.z += b.z; }
+__host__ __device__ inline void operator-=(float3& a, float3 b) { a.x -= b.x; a.y -= b.y; a.z -= b.z; }
+__host__ __device__ inline float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ inline float3 cross3(float3 a, float3 b) {
+    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+// Particle type from the original id (src/Particle.cu:432-435).
+enum { PT_B1 = 0, PT_B2 = 1, PT_FLUID = 2, PT_MEMB = 3 };
+__device__ __forceinline__ int ptype(unsigned id, const GcParams& p) {
+    return id < p.nB2 ? PT_B1 : (id < p.nF ? PT_B2 : (id < p.nC ? PT_FLUID : PT_MEMB));
+}
+__device__ __forceinline__ bool is_mobile(unsigned id, const GcParams& p) { return id >= p.nF; }
+// Members of the SDPD set (Bound2, fluid, membrane); Bound1 only repels.
+__device__ __forceinline__ bool is_sdpd(unsigned id, const GcParams& p) { return id >= p.nB2; }
+
+// ---------------------------------------------------------------------------
+// Distances.  The neighbour predicate is r^2 < rc^2 with r^2 evaluated in
+// FP32 exactly as written here (explicit round-to-nearest, no contraction);
+// oracle/oracle.c evaluates the same expression with -ffp-contract=off, so
+// both sides select bit-identical neighbour sets.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float min_image_1(float d, int axis, const GcGrid& g) {
+    if (g.pmask & (1 << axis)) {
+        if (d > g.halfL[axis]) d = __fsub_rn(d, g.L[axis]);
+        else if (d < -g.halfL[axis]) d = __fadd_rn(d, g.L[axis]);
+    }
+    return d;
+}
+
+__device__ __forceinline__ float3 min_image(float3 a, float3 b, const GcGrid& g) {
+    return f3(min_image_1(__fsub_rn(a.x, b.x), 0, g),
+              min_image_1(__fsub_rn(a.y, b.y), 1, g),
+              min_image_1(__fsub_rn(a.z, b.z), 2, g));
+}
+
+__device__ __forceinline__ float norm2_rn(float3 d) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z));
+}
+
+// Cube coordinate along one axis: periodic axes wrap, wall axes clamp (a
+// clamped particle is only ever farther from its true neighbours, so the
+// 27-cube search stays complete).
+__device__ __forceinline__ int cube_coord(float x, int axis, const GcGrid& g) {
+    int c = (int)floorf(__fmul_rn(__fsub_rn(x, g.origin[axis]), g.invw[axis]));
+    int n = g.n[axis];
+    if (g.pmask & (1 << axis)) {
+        c %= n;
+        if (c < 0) c += n;
+    } else {
+        c = c < 0 ? 0 : (c >= n ? n - 1 : c);
+    }
+    return c;
+}
+
+__device__ __forceinline__ int cube_key(int cx, int cy, int cz, const GcGrid& g) {
+    return cx + g.n[0] * (cy + g.n[1] * cz);
+}
+
+// Neighbouring cube index along an axis, or -1 when it falls off a wall axis.
+__device__ __forceinline__ int cube_step(int c, int d, int axis, const GcGrid& g) {
+    c += d;
+    int n = g.n[axis];
+    if (c < 0) return (g.pmask & (1 << axis)) ? c + n : -1;
+    if (c >= n) return (g.pmask & (1 << axis)) ? c - n : -1;
+    return c;
+}
+
+// ---------------------------------------------------------------------------
+// Wendland C2 kernel in 3-D with support rc (h = rc/2):
+//   W(r)     = 21/(2 pi rc^3) (1 - s)^4 (1 + 4 s),   s = r/rc
+//   F(r)     = -W'(r)/r = 210/(pi rc^5) (1 - s)^3
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float wendland_w(float r, const GcParams& p) {
+    float s = r * p.inv_rc;
+    float t = 1.f - s;
+    float t2 = t * t;
+    return p.wnorm * t2 * t2 * (1.f + 4.f * s);
+}
+
+__device__ __forceinline__ float wendland_f(float r, const GcParams& p) {
+    float t = 1.f - r * p.inv_rc;
+    return p.fnorm * t * t * t;
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror & Shaw, SC'11), the counter-based
+// generator behind the pair noise.  Counter = (min id, max id, step lo,
+// step hi), key = the 64-bit seed; the same four words on both sides of a
+// pair give an antisymmetric pair noise that does not depend on the particle
+// order.
+// ---------------------------------------------------------------------------
+
+__host__ __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                       uint32_t k0, uint32_t k1, uint32_t out[4]) {
+#ifdef __CUDA_ARCH__
+#pragma unroll
+#endif
+    for (int r = 0; r < 10; ++r) {
+#ifdef __CUDA_ARCH__
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+#else
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// A uniform variate with zero mean and unit variance from the top 24 bits
+// of a Philox word: sqrt(12) ((w >> 8) + 1/2) / 2^24 - sqrt(3).  Groot &
+// Warren (1997) drive the same integrator with uniform noise; only the first
+// two moments enter the fluctuation-dissipation balance.
+__device__ __forceinline__ float unit_uniform(uint32_t w) {
+    return fmaf((float)(w >> 8) + 0.5f, 3.4641016151377544f / 16777216.f, -1.7320508075688772f);
+}
+
+// The three noise components xi_ij for the pair (i, j); xi_ji = -xi_ij.
+__device__ __forceinline__ float3 pair_noise(unsigned id_i, unsigned id_j, const GcParams& p) {
+    unsigned a = id_i < id_j ? id_i : id_j;
+    unsigned b = id_i < id_j ? id_j : id_i;
+    uint32_t w[4];
+    philox4x32_10(a, b, p.step_lo, p.step_hi, p.seed_lo, p.seed_hi, w);
+    float s = id_i < id_j ? 1.f : -1.f;
+    return f3(s * unit_uniform(w[0]), s * unit_uniform(w[1]), s * unit_uniform(w[2]));
+}
+
+// ---------------------------------------------------------------------------
+// Device status flags (GC_FLAG_*), one word per device.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void raise_flag(unsigned* flags, unsigned f) {
+    if (flags) atomicOr(flags, f);
+}
+
+// ---------------------------------------------------------------------------
+// Host-side state
+// ---------------------------------------------------------------------------
+
+enum GcScratchSlot {
+    SCR_FLAGS = 0,
+    SCR_SORT_COUNT,      // cube counts / starts (uint32, ncells + 1)
+    SCR_SORT_RANK,       // rank of each element within its cube
+    SCR_SORT_KEY,        // scattered keys
+    SCR_SORT_VAL,        // scattered values
+    SCR_SORT_SRC,        // input position of each scattered element
+    SCR_SCAN_BLOCKS,     // block sums of the device-wide scan
+    SCR_MAXKEY,          // max key when the caller gave no grid
+    SCR_GATHER,          // K7 gather buffer (80 bytes per particle)
+    SCR_CELLSUM,         // per-cell area / volume sums
+    SCR_COUNT_
+};
+
+struct GcState {
+    Structconst c;
+    bool consts_set = false;
+    int periodic_mask = 1;
+    int noise_on = 1;
+    long long step = -1;           // last step index seen by UpdateFluidCoor
+    cudaStream_t stream = 0;
+    float* velhalf_ptr = nullptr;  // caller's VelHalf, for the wall velocity
+    // grid cache
+    bool grid_set = false;
+    const float* grid_bbox_ptr = nullptr;
+    int grid_mask = -1;
+    float grid_rc = 0.f;
+    GcGrid grid{};
+    // scratch
+    void* scratch[SCR_COUNT_] = {};
+    size_t scratch_bytes[SCR_COUNT_] = {};
+};
+
+GcState& gc_state();
+// Sets the thread's last-error text and returns `code`.
+int gc_fail(int code, const char* fmt, ...);
+// Maps a CUDA error to GC_ECUDA with a message naming `what`.
+int gc_cuda_fail(cudaError_t e, const char* what);
+// Grows scratch slot `slot` to at least `bytes`; returns nullptr on failure
+// (with the error text set).
+void* gc_scratch(int slot, size_t bytes);
+unsigned* gc_flags_ptr();
+// Parameter block for the current constants, grid and step.
+int gc_make_params(GcParams* out, bool need_grid);
+// (Re)builds the grid from the caller's device bbox pointer.
+int gc_ensure_grid(const float* d_bbox);
+// Step index that keys the noise of the next force evaluation.
+long long gc_noise_step();
+
+// Counts one kernel launch of this library and returns GC_ECUDA if the
+// launch failed.  Written after every <<<...>>> so that
+// gc_launch_count() is exact.
+void gc_count_launch();
+#define GC_CHECK_LAUNCH(what)                                   \
+    do {                                                        \
+        gc_count_launch();                                      \
+        cudaError_t e_ = cudaGetLastError();                    \
+        if (e_ != cudaSuccess) return gc_cuda_fail(e_, what);   \
+    } while (0)
+
+#define GC_TRY(call)                                            \
+    do {                                                        \
+        int rc_ = (call);                                       \
+        if (rc_ != GC_OK) return rc_;                           \
+    } while (0)
+
+#define GC_CUDA(call, what)                                     \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return gc_cuda_fail(e_, what);   \
+    } while (0)
+
+inline int gc_blocks(long long n, int bs) { return (int)((n + bs - 1) / bs); }

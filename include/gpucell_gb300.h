@@ -1,0 +1,152 @@
+/*
+ * gpucell_gb300.h -- C ABI of libgpucell_gb300.so.
+ *
+ * One extern "C" function per entry point of GPUCell's GPU boundary, with
+ * the reference's argument order and meaning, plain pointers only:
+ *   float3 / tfloat3 arrays  -> float*, 3 floats per element
+ *   float4 arrays            -> float*, 4 floats per element
+ *   int2 / int3 / int6       -> int*,   2 / 3 / 6 ints per element
+ * Every function returns GC_OK (0) or a negative GC_E* status; the text of
+ * the last error is available from gc_last_error().  Pointers named d_*
+ * are device pointers owned by the caller; h_* are host pointers that the
+ * reference passes but never reads back (accepted and ignored).  Work is
+ * enqueued on the library's stream (gc_set_stream; the legacy default
+ * stream unless changed), and no function synchronises the host except
+ * where stated.
+ *
+ * The C++ symbols cupar::* / cudiv::* (include/gpucell/cupar.h) forward to
+ * these and turn a failure into the reference's print-and-exit(1).
+ *
+ * Particle arrays are in "slot" order: the order of the latest neighbour
+ * sort.  d_sortpart[slot] is the original id of the particle in that slot
+ * and d_curpos[id] its slot (src/Particle.cu:734, :1322).  Original ids are
+ * grouped by type as described in include/gpucell/TypesDef.h.
+ */
+#ifndef GPUCELL_GB300_H
+#define GPUCELL_GB300_H
+
+#include "gpucell/TypesDef.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GC_OK           0
+#define GC_EINVAL      -1   /* bad argument (size, pointer, state) */
+#define GC_ECUDA       -2   /* a CUDA runtime call or launch failed */
+#define GC_ESTATE      -3   /* call out of order (e.g. before ConstsDataUp) */
+#define GC_ENOMEM      -4   /* scratch allocation failed */
+#define GC_EDEVICE     -5   /* a device-side check raised its flag */
+
+/* device status flags reported by gc_device_status() */
+#define GC_FLAG_NONFINITE     1u   /* a NaN/Inf position or force was seen */
+#define GC_FLAG_BAD_INDEX     2u   /* a topology index pointed outside its array */
+#define GC_FLAG_CELL_OVERFLOW 4u   /* a grid cell held more particles than a sweep stages */
+#define GC_FLAG_STRETCH       8u   /* a membrane edge reached its maximum length */
+
+/* ---- library controls (no counterpart in the reference) ---------------- */
+
+/* Text of the most recent error of this thread ("" if none). */
+const char* gc_last_error(void);
+/* Library version as 10000*major + 100*minor + patch. */
+int gc_version(void);
+/* Periodic axes as a bit mask (1 = x, 2 = y, 4 = z).  The reference grid
+ * pads y and z by one cube and leaves x unpadded (src/Particle.cu:551-556),
+ * i.e. x periodic with walls in y and z: that is the default (mask 1).
+ * The environment variable GPUCELL_PERIODIC (e.g. "xz") sets the initial
+ * value.  Takes effect at the next gc_cudiv_PreConList. */
+int gc_set_periodic(int mask);
+int gc_get_periodic(void);
+/* Thermal pair noise on (1, default) or off (0). GPUCELL_NOISE=0 turns it
+ * off at load time. */
+int gc_set_noise(int on);
+/* Step index that keys the pair noise.  The cupar:: path counts steps
+ * itself (one per gc_cupar_UpdateFluidCoor, starting at 0); this sets the
+ * counter to `step` for the next force evaluation. */
+int gc_set_step(long long step);
+long long gc_get_step(void);
+/* Stream used by every gc_* launch (a cudaStream_t; NULL = legacy default). */
+int gc_set_stream(void* stream);
+/* Reads and clears the device-side status flags (GC_FLAG_*).  Synchronises
+ * the library's stream. */
+int gc_device_status(unsigned* flags);
+/* Number of kernels this library has launched since it was loaded. */
+unsigned long long gc_launch_count(void);
+/* Frees every scratch buffer the library allocated.  Safe to call twice;
+ * also registered with atexit(). */
+int gc_shutdown(void);
+
+/* ---- cupar: particle physics (src/ParticleGPU.cuh:10-35) ---------------- */
+
+/* src/ParticleGPU.cuh:10, called at src/Particle.cu:662 */
+int gc_cupar_ConstsDataUp(const Structconst* consts);
+/* src/ParticleGPU.cuh:11, src/Particle.cu:1333 */
+int gc_cupar_UpdateFluidCoor(int n, int* d_sortpart, float* d_totalforce, float* d_totalcoor, float* d_velrhop);
+/* src/ParticleGPU.cuh:12, src/Particle.cu:1338 */
+int gc_cupar_AppFluidPeriodicBC(int n, int* d_sortpart, float* d_totalcoor, int* d_nthrobound, float* d_bboxsdpd);
+/* src/ParticleGPU.cuh:13, src/Particle.cu:1343 */
+int gc_cupar_CalFluidDen(int n, float* d_totalcoor, float* d_velrhop, int* d_cc, int* d_ncube, float* d_outerregion, int* d_sortpart, int* d_beginendcube);
+/* src/ParticleGPU.cuh:14, src/Particle.cu:1348 */
+int gc_cupar_PredictFluidVel(int n, int* d_sortpart, float* d_velrhop, float* d_velhalf, float* d_totalforce);
+/* src/ParticleGPU.cuh:15, src/Particle.cu:1353 */
+int gc_cupar_CalBound2Vel(int n, float* d_totalcoor, float* d_velrhop, int* d_cc, int* d_ncube, float* d_outerregion, int* d_sortpart, int* d_beginendcube);
+/* src/ParticleGPU.cuh:16, src/Particle.cu:1358 */
+int gc_cupar_EOS(int n, int* d_sortpart, float* d_velrhop, float* d_press);
+/* src/ParticleGPU.cuh:17, src/Particle.cu:1363 */
+int gc_cupar_CalFluidSDPDForce(int n, float* h_sdpdforce, float* d_totalcoor, float* d_velrhop, int* d_cc, int* d_ncube, int* d_sortpart, float* d_outerregion, int* d_beginendcube, float* d_totalforce, float* d_press);
+/* src/ParticleGPU.cuh:18, src/Particle.cu:1368 */
+int gc_cupar_CalFluidRepForce(int n, float* d_totalcoor, int* d_cc, int* d_ncube, int* d_sortpart, float* d_outerregion, int* d_beginendcube, float* d_totalforce);
+/* src/ParticleGPU.cuh:19, src/Particle.cu:1373 */
+int gc_cupar_SetFluidExtForce(int driveon, int n, int* d_sortpart, float* d_totalforce);
+/* src/ParticleGPU.cuh:21, src/Particle.cu:1379 */
+int gc_cupar_CorrectFliudVel(int n, int* d_sortpart, float* d_totalforce, float* d_velhalf, float* d_velrhop, float* d_totalcoor, int* d_cc, int* d_ncube, float* d_outerregion, int* d_beginendcube);
+/* src/ParticleGPU.cuh:25-26, src/Particle.cu:476 (stepcount -1: records the
+ * reference geometry) and :1322 (every step) */
+int gc_cupar_CalGeoPara(long stepcount, int ntri, int ncell, float* d_bbox, int* d_curpos, int* d_tri, int* d_beginendtri, int* d_nthrobound, float* d_totalcoor, float* d_trinordir, float* d_triarea,
+    float* d_reftriarea, float* d_tricenter, float* d_refarea_para, float* d_refvol_para, float* d_area_para, float* d_vol_para, float* d_area, float* d_vol, float* d_pararea);
+/* src/ParticleGPU.cuh:28-29, src/Particle.cu:479 */
+int gc_cupar_SetMechPara(int ncell, int nedge, int* d_edge, int* d_curpos, float* d_refedgelen, float* d_maxrefedgelen, float* d_bendmodpara, float* d_shearmodpara, float* d_hbending,
+    float* d_powerindex, float* d_perlenWLC, float* d_hpow, float* d_reftriangle, float* d_trinordir, float* d_tricenter, float* d_coor);
+/* src/ParticleGPU.cuh:30-33, src/Particle.cu:1385 */
+int gc_cupar_CalCellDefForce(int ncell, unsigned nedge, unsigned ntri, unsigned ntotalpar, unsigned ncellpar, float* d_bbox, int* d_edge, int* d_tri, float* d_coor, float* h_defforce, float* d_defforce, int* d_nthrobound,
+    float* d_maxrefedgelen, float* d_powerindex, float* d_perlenWLC, float* d_hpow, float* d_trinordir, float* d_tricenter,
+    float* d_reftriangle, float* d_hbending, float* d_triarea, float* d_reftriarea, float* d_hlarea_para, float* d_hgarea_para, float* d_area_para,
+    float* d_refarea_para, float* d_hvol_para, float* d_vol_para, float* d_refvol_para, float* d_totalforce, int* d_sortpart, int* d_curpos);
+/* src/ParticleGPU.cuh:34-35, src/Particle.cu:1390 */
+int gc_cupar_CalCellAggForce(unsigned ncell, unsigned n, unsigned ncellpar, float* d_totalcoor, float* d_aggforce, int* d_cc, int* d_ncube, int* d_sortpart,
+    int* d_celltab, float* d_outerregion, int* d_beginendcube, float* d_totalforce, float* d_pararea);
+
+/* ---- cudiv: neighbour grid (src/ConfigDomain.cuh:11-17) ----------------- */
+
+/* src/ConfigDomain.cuh:11, src/Particle.cu:668.  Reads d_bboxsph to the
+ * host (one synchronous 24-byte copy) the first time it sees that pointer. */
+int gc_cudiv_PreConList(int n, int cutradius, float* d_totalcoor, float* d_bboxsph, float* d_invwid, int* d_ncube, int* d_cc, int* d_cubepart, int* d_sortpart, int* d_oldpos);
+/* src/ConfigDomain.cuh:12, src/Particle.cu:669.  Stable sort of n (key,
+ * value) pairs by key.  Keys must lie in [0, K) where K is the cube count of
+ * the latest PreConList; without one, K is found on the device (one
+ * synchronous 4-byte copy). */
+int gc_cudiv_Sort(int n, int* keys, int* values);
+/* src/ConfigDomain.cuh:13, src/Particle.cu:672 */
+int gc_cudiv_CalBeginEndCube(int n, int sizecube, int* d_cubepart, int* d_beginendcube);
+/* src/ConfigDomain.cuh:14, src/Particle.cu:677 */
+int gc_cudiv_SortBasicArrays(int n, int* d_sortpart, int* d_oldpos, float* d_totalcoor, int* d_cc, float* d_velrhop, float* d_velhalf, float* d_totalforce, float* d_press);
+/* src/ConfigDomain.cuh:15, src/Particle.cu:675 */
+int gc_cudiv_SortArraysWithCells(int n, int* d_sortpart, int* d_oldpos, int* d_curpos, float* d_totalcoor, int* d_cc, float* d_velrhop, float* d_velhalf, float* d_totalforce, float* d_press, int* d_nthrobound);
+/* src/ConfigDomain.cuh:17 (never called by the reference): prints the
+ * first min(n, 16) slots to stdout.  Synchronises. */
+int gc_cudiv_Printf(int n, int* d_curpos, int* d_sortpart, float* d_totalcoor);
+
+/* ---- test hooks (no counterpart in the reference) ----------------------- */
+
+/* Runs the production neighbour traversal of CalFluidDen over the current
+ * sort and, for every slot, writes the number of neighbours within
+ * CutRadius (d_count) and an order-independent checksum of their original
+ * ids (d_hash: the sum over neighbours of a 64-bit mix of the id).  Used to
+ * prove the neighbour sets equal the oracle's. */
+int gc_debug_neighbor_stats(int n, float* d_totalcoor, int* d_sortpart, int* d_beginendcube, int* d_count, unsigned long long* d_hash);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPUCELL_GB300_H */

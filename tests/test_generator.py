@@ -1,0 +1,56 @@
+"""Synthetic inputs: mesh topology and GPUCell's input-file format (no GPU)."""
+import numpy as np
+
+from gpucell_gb300 import generator as gen
+
+
+def test_icosphere_counts_and_edges():
+    for s, nv in ((2, 162), (3, 642), (4, 2562)):
+        v, f = gen.icosphere(s)
+        assert v.shape == (nv, 3) and f.shape == (2 * nv - 4, 3)
+        e = gen.edge_records(f)
+        assert e.shape[0] == f.shape[0] * 3 // 2          # src/Particle.cu:217
+        # p1 -> p2 runs forward in t1 and backward in t2; p3/p4 are the third vertices
+        for p1, p2, p3, p4, t1, t2 in e[:200]:
+            a, b = list(f[t1]), list(f[t2])
+            assert set(a) == {p1, p2, p3} and set(b) == {p1, p2, p4}
+            i = a.index(p1)
+            assert a[(i + 1) % 3] == p2
+            j = b.index(p2)
+            assert b[(j + 1) % 3] == p1
+
+
+def test_channel_counts_match_configuration():
+    cfg = gen.channel()
+    assert (cfg.n_fluid, cfg.n_b2, cfg.ncp, cfg.ntri, cfg.nedge) == (65536, 12288, 642, 1280, 1920)
+    c = cfg.consts()
+    assert c["nCellStart"] + c["nCellPar"] == c["nTotalPar"] == cfg.n
+
+
+def test_reference_file_round_trip(tmp_path):
+    cfg = gen.small_channel()
+    gen.write_reference_inputs(cfg, str(tmp_path))
+    got = gen.read_reference_inputs(str(tmp_path))
+    assert (got["n_b1"], got["n_b2"], got["n_fluid"]) == (cfg.n_b1, cfg.n_b2, cfg.n_fluid)
+    np.testing.assert_allclose(got["sdpd_coor"], cfg.coor[:cfg.n_cell_start], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(got["cell_coor"], cfg.coor[cfg.n_cell_start:], rtol=1e-6, atol=1e-6)
+    np.testing.assert_array_equal(got["tri"], cfg.tri)
+    np.testing.assert_array_equal(got["edge"], cfg.edge)
+    np.testing.assert_array_equal(got["betri"], cfg.betri)
+    np.testing.assert_array_equal(got["celltab"], cfg.celltab)
+    assert abs(got["den_init"] - cfg.den_init) < 1e-6 * cfg.den_init
+    # every line fits the reference's 200-character line buffer (src/Particle.cu:50)
+    for name in ("SDPDParCoor.txt", "SDPDPhyPara.txt", "CELLParStruct.txt", "CELLPhyPara.txt"):
+        assert max(len(ln) for ln in open(tmp_path / name)) < 200
+
+
+def test_suspension_small_has_no_overlap_and_exact_count():
+    cfg = gen.suspension(nx=48, ny=32, nz=32, ncells=3, subdiv=2, hematocrit=0.1)
+    assert cfg.n == 48 * 32 * 32
+    assert cfg.ncp == 3 * 162 and cfg.pmask == 7
+
+
+def test_reference_grid_formula():
+    from gpucell_gb300.host import reference_grid
+    ncube, outer, invwid, size = reference_grid([0, 20, -10, 10, -10, 10])   # src/main.cuh:12
+    assert ncube == [20, 22, 22] and outer == [20.0, 22.0, 22.0] and size == 9680
