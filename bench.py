@@ -3,14 +3,15 @@
 suspension (256x128x128 particles, 200 cells of 2562 vertices, hematocrit
 20 %, periodic, thermal noise on).
 
-Prints one JSON line.  `value` is particle-steps/s with the state resident in
-HBM; `e2e` is the same metric with the state copied host->device before and
-device->host after every step (pinned buffers, the reference's
-ParticlesDataReturn set); `roofline` describes the dominant kernel, timed
+Prints one JSON line.  `value` is particle-steps/s of the fused step with the
+state resident in HBM; `plain_fp32` is the reference-structured FP32 step
+(one kernel per boundary entry point) on the same workload; `e2e` is the
+fused step with the state copied host->device before and device->host after
+every step (pinned buffers); `roofline` describes the dominant kernel, timed
 live with CUDA events; `cpu_baseline` is the FP64 CPU restatement of the
 method timed on this machine's cores on a bounded sample.
 
-    python bench.py [--steps K] [--warmup W] [--variant plain]
+    python bench.py [--steps K] [--warmup W] [--skin S] [--block B] [--no-plain]
     python bench.py --impl reference      # the CPU restatement alone
     torchrun --nproc-per-node N bench.py --gpus N   # independent replicas
 """
@@ -39,7 +40,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--variant", choices=["plain"], default="plain")
+    ap.add_argument("--skin", type=float, default=0.1)
+    ap.add_argument("--block", type=int, default=128)
+    ap.add_argument("--no-plain", dest="plain", action="store_false", help="skip the FP32 boundary-path timing")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--small", action="store_true", help="a 1/8-size suspension (for quick checks)")
@@ -122,10 +125,37 @@ def plain_bytes_per_step(cfg):
     return 352 * cfg.n + 16 * cfg.ntri + 32 * cfg.nedge + 28 * cfg.ncp
 
 
-# Dominant kernel: the SDPD pair force.  Algorithmic bytes per particle:
-# position 12 + velocity/density 16 + pressure 4 + id 4 + cube 12 read,
-# force 12 written.
-SDPD_BYTES_PER_PARTICLE = 60
+# Dominant kernel of the fused step: fk_force.  Algorithmic bytes per
+# particle: its own position, predicted velocity, VelHalf (16 B each) and
+# (1/d, P/d^2) (8 B) read, force and velocity (16 B each) written, the list
+# length (4 B) and its neighbour-list entries (4 B each) read.
+FORCE_STATE_BYTES = 16 * 3 + 8 + 16 * 2 + 4
+
+
+def measure_plain(cfg, dev, steps, warmup):
+    """The reference-structured FP32 step (one kernel per boundary entry
+    point), timed with CUDA events: the FP32 denominator."""
+    import torch
+    from gpucell_gb300 import _lib
+    from gpucell_gb300.host import ParticleSystem
+    ps = ParticleSystem(cfg, device=dev, noise=True)
+    for _ in range(warmup):
+        ps.update()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    l0 = _lib.launch_count()
+    e0.record()
+    for _ in range(steps):
+        ps.update()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    out = {"ms_per_step": ms, "value": cfg.n / (ms / 1e3), "steps": steps,
+           "gpu_launches_per_step": (_lib.launch_count() - l0) / steps, "dtype": "fp32",
+           "path": "boundary entry points (gc_cupar_*/gc_cudiv_*), one kernel each"}
+    del ps
+    torch.cuda.synchronize()
+    return out
 
 
 def run_ours(args):
@@ -135,7 +165,7 @@ def run_ours(args):
 
     from gpucell_gb300 import _lib
     from gpucell_gb300.build import build_library
-    from gpucell_gb300.host import ParticleSystem
+    from gpucell_gb300.fused import FusedSystem, _ptr
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -149,146 +179,147 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
 
-    cfg, wdesc = workload(args, rank)
-    ps = ParticleSystem(cfg, device=dev, noise=True)
-
     def barrier():
         if world > 1:
             dist.barrier()
 
-    for _ in range(max(args.warmup, 3)):
-        ps.update()
-    torch.cuda.synchronize()
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
 
+    cfg, wdesc = workload(args, rank)
+    W = max(args.warmup, 3)
+    K = args.steps
+    plain = measure_plain(cfg, dev, steps=min(K, 10), warmup=3) if args.plain else None
+
+    fs = FusedSystem(cfg, noise=True, skin=args.skin, block=args.block)
+    fs.step(W, 1)
+    torch.cuda.synchronize()
     sampler = ClockSampler()
     if rank == 0:
         sampler.start()
-    K = args.steps
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    kstart = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-    kend = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    fs.profile(True)
     barrier()
     torch.cuda.synchronize()
     l0 = _lib.launch_count()
+    st0 = fs.stats()
     ev0.record()
-    for k in range(K):
-        ps.update_coor()
-        ps.periodic()
-        ps.con_cube_list()
-        ps.density()
-        ps.predict()
-        ps.bound2_vel()
-        ps.eos()
-        kstart[k].record()
-        ps.sdpd_force()
-        kend[k].record()
-        ps.rep_force()
-        ps.ext_force(1)
-        ps.cal_geo_para()
-        ps.def_force()
-        ps.agg_force()
-        ps.correct()
-        ps.bound2_vel()
-        ps.step_count += 1
+    fs.step(K, 1)
     ev1.record()
     torch.cuda.synchronize()
     barrier()
     launches = _lib.launch_count() - l0
-    t_ms = ev0.elapsed_time(ev1)
+    t_ms = max_over_ranks(ev0.elapsed_time(ev1))
     clocks = sampler.stop(local) if rank == 0 else None
-    sdpd_ms = sum(a.elapsed_time(b) for a, b in zip(kstart, kend)) / K
-    if world > 1:
-        t = torch.tensor([t_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_ms = float(t.item())
-    flags = _lib.device_status()
+    prof = fs.profile_read()
+    fs.profile(False)
+    st1 = fs.stats()
+    flags = fs.flags()
 
     # ---- end to end: host state -> device, one step, results -> host ----
-    dyn = ["TotalCoor", "Velrhop", "VelHalf", "TotalForce", "nThroBound", "SortPart"] + \
-          (["CurPos"] if ps.has_cells else [])
-    outs = ["Press"] + (["Area", "Vol", "DefForce", "AggForce", "TriNorDir", "TriCenter"] if ps.has_cells else [])
-    host = {k: torch.empty_like(ps.d[k], device="cpu").pin_memory() for k in dyn + outs}
-    for k in dyn:
-        host[k].copy_(ps.d[k])
-    bi = sum(host[k].numel() * host[k].element_size() for k in dyn)
-    bo = sum(host[k].numel() * host[k].element_size() for k in dyn + outs)
+    n = cfg.n
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt).pin_memory()
+    h = {k: pin((n, 3), torch.float32) for k in ("pos", "vel", "velhalf", "force")}
+    h["nthro"] = pin((n, 3), torch.int32)
+    h["rho"], h["press"] = pin((n,), torch.float32), pin((n,), torch.float32)
+    hc = {}
+    if cfg.ncell:
+        hc = {"area": pin((cfg.ncell,), torch.float32), "vol": pin((cfg.ncell,), torch.float32),
+              "defforce": pin((cfg.ncp, 3), torch.float32), "aggforce": pin((cfg.ncp, 3), torch.float32),
+              "trinordir": pin((cfg.ntri, 3), torch.float32), "tricenter": pin((cfg.ntri, 3), torch.float32)}
+
+    def store():
+        _lib.call("gc_fused_store", fs.h, *[_ptr(h[k]) for k in ("pos", "vel", "rho", "press", "force", "velhalf",
+                                                                 "nthro")], 0)
+        if hc:
+            _lib.call("gc_fused_store_cells", fs.h, *[_ptr(hc[k]) for k in ("area", "vol", "defforce", "aggforce",
+                                                                           "trinordir", "tricenter")],
+                      _ptr(None), 0)
+
+    store()
+    bi = sum(h[k].numel() * h[k].element_size() for k in ("pos", "vel", "velhalf", "force", "nthro"))
+    bo = sum(t.numel() * t.element_size() for t in list(h.values()) + list(hc.values()))
     KE = max(1, args.e2e_steps)
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
     for _ in range(KE):
-        for k in dyn:
-            ps.d[k].copy_(host[k], non_blocking=True)
-        ps.update(1)
-        for k in dyn + outs:
-            host[k].copy_(ps.d[k], non_blocking=True)
-        torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    barrier()
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        _lib.call("gc_fused_load", fs.h, *[_ptr(h[k]) for k in ("pos", "vel", "velhalf", "force", "nthro")], 0)
+        fs.step(1, 1)
+        store()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
 
-    n_all = cfg.n * world
+    n_all = n * world
     value = n_all * K / (t_ms / 1e3)
     e2e_value = n_all * KE / e2e_s
     peaks, peak_kind = measured_peaks()
     hbm = float(peaks["hbm_gbs"])
-    sdpd_bytes = SDPD_BYTES_PER_PARTICLE * cfg.n
-    achieved = sdpd_bytes / (sdpd_ms / 1e3) / 1e9
-    step_bytes = plain_bytes_per_step(cfg)
-    step_gbs = step_bytes / (t_ms / K / 1e3) / 1e9
+    mean_nb = st1["mean_neighbors"]
+    force_ms = prof["force_ms"] / max(prof["steps"], 1)
+    dens_ms = prof["density_ms"] / max(prof["steps"], 1)
+    force_bytes = n * (FORCE_STATE_BYTES + 4 * mean_nb)
+    achieved = force_bytes / (force_ms / 1e3) / 1e9
 
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return
 
-    cpu = cpu_baseline(cfg, args.cpu_steps) if world == 1 else None
+    cpu = cpu_baseline(cfg, args.cpu_steps) if (world == 1 and args.cpu_steps > 0) else None
     line = {
         "metric": METRIC,
         "value": value,
         "unit": "particle-steps/s",
         "n_gpus": world,
         "steps": K,
-        "warmup": max(args.warmup, 3),
+        "warmup": W,
         "ms_per_step": t_ms / K,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "fp32",
+        "dtype": "fp32 (fp64 membrane area/volume sums)",
         "data": "synthetic (seeded generator, no dataset)",
-        "variant": "plain FP32, reference-structured (one kernel per boundary entry point)",
-        "config": dict(wdesc, particles=cfg.n, membrane_vertices=cfg.ncp, triangles=cfg.ntri, edges=cfg.nedge,
+        "variant": "fused step: Verlet lists with skin, fused passes (gc_fused_*)",
+        "config": dict(wdesc, particles=n, membrane_vertices=cfg.ncp, triangles=cfg.ntri, edges=cfg.nedge,
                        parallelism=f"replicas x{world}" if world > 1 else "single GPU",
-                       l2="working set (~0.45 GB of particle state) is larger than L2; no flush",
-                       noise="on"),
+                       l2="working set (>1 GB: state + neighbour lists) is larger than L2; no flush",
+                       noise="on", skin=args.skin, block=args.block),
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": bi,
                 "d2h_bytes_per_step": bo, "steps": KE,
-                "path": "reference-facing C ABI (gc_cupar_*/gc_cudiv_*), pinned host buffers"},
+                "path": "C ABI gc_fused_load -> gc_fused_step -> gc_fused_store(_cells), pinned host buffers"},
         "gpu_launches": launches,
         "roofline": {
-            "kernel": "k_sdpd (CalFluidSDPDForce)",
+            "kernel": "fk_force (SDPD + repulsion + body force + membrane add + corrector)",
             "bound": "hbm",
             "achieved": achieved,
             "peak": hbm,
             "unit": "GB/s",
             "frac": achieved / hbm,
-            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
             "traffic": None,
-            "bytes_per_launch": sdpd_bytes,
-            "launch_ms": sdpd_ms,
-            "note": "the pair sweep is FP32-issue bound; bytes are 60 per particle",
+            "bytes_per_launch": force_bytes,
+            "launch_ms": force_ms,
+            "note": f"bytes = {FORCE_STATE_BYTES} per particle + 4 per list entry (mean list {mean_nb:.1f}); "
+                    "the pair physics is FP32-issue bound",
         },
-        "step_roofline": {"bytes_per_step": step_bytes, "achieved_gbs": step_gbs, "frac": step_gbs / hbm,
-                          "rule": "352 N + 16 N_tri + 32 N_edge + 28 N_vert"},
+        "kernels_ms_per_step": {"fk_force": force_ms, "fk_density": dens_ms},
+        "lists": {"rebuilds_in_timed_steps": st1["rebuilds"] - st0["rebuilds"], "mean_length": mean_nb,
+                  "max_length": st1["max_neighbors"], "capacity": st1["capacity"]},
         "device_flags": flags,
     }
+    if plain:
+        plain["speedup_of_fused"] = plain["ms_per_step"] / (t_ms / K)
+        line["plain_fp32"] = plain
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
+    fs.close()
     if world > 1:
         dist.destroy_process_group()
 

@@ -49,6 +49,12 @@ class Structconst(C.Structure):
 
 assert C.sizeof(Structconst) == 96
 
+
+class GcFusedOptions(C.Structure):
+    """ctypes mirror of GcFusedOptions (include/gpucell_gb300.h)."""
+
+    _fields_ = [("skin", C.c_float), ("block", C.c_int), ("list_capacity", C.c_int), ("reserved", C.c_int * 5)]
+
 _P = C.c_void_p
 _I = C.c_int
 _U = C.c_uint
@@ -89,6 +95,19 @@ _SIGS = {
     "gc_cudiv_SortArraysWithCells": [_I] + [_P] * 10,
     "gc_cudiv_Printf": [_I, _P, _P, _P],
     "gc_debug_neighbor_stats": [_I, _P, _P, _P, _P, _P],
+    "gc_fused_create": [_P, _P, _I, _I, _P, _P],
+    "gc_fused_set_cells": [_P, _I, _I, _I] + [_P] * 9,
+    "gc_fused_load": [_P] * 6 + [_I],
+    "gc_fused_setup": [_P],
+    "gc_fused_step": [_P, _I, _I],
+    "gc_fused_store": [_P] * 8 + [_I],
+    "gc_fused_store_cells": [_P] * 8 + [_I],
+    "gc_fused_cell_sums": [_P, _P, _P],
+    "gc_fused_stats": [_P] * 6,
+    "gc_fused_flags": [_P, _P],
+    "gc_fused_profile": [_P, _I],
+    "gc_fused_profile_read": [_P, _P, _P, _P],
+    "gc_fused_destroy": [_P],
 }
 _RESTYPES = {"gc_last_error": C.c_char_p, "gc_get_step": C.c_longlong, "gc_launch_count": C.c_ulonglong}
 

@@ -268,8 +268,16 @@ int gc_cuda_fail(cudaError_t e, const char* what);
 // (with the error text set).
 void* gc_scratch(int slot, size_t bytes);
 unsigned* gc_flags_ptr();
+// Parameter block for the given constants (no grid, step 0).
+int gc_params_from(const Structconst& c, int noise_on, GcParams* p);
 // Parameter block for the current constants, grid and step.
 int gc_make_params(GcParams* out, bool need_grid);
+// Grid of cubes at least `cut` wide over the host bbox `bb` (6 floats).
+int gc_build_grid(const float* bb, float cut, int mask, GcGrid* g);
+// Stable sort of (keys, vals) by key in [0, K), in place (neighbor.cu).
+int gc_counting_sort(int n, int K, int* keys, int* vals, cudaStream_t st);
+// Start of every key's range (K + 1 entries) after the latest counting sort.
+const unsigned* gc_sort_starts();
 // (Re)builds the grid from the caller's device bbox pointer.
 int gc_ensure_grid(const float* d_bbox);
 // Step index that keys the noise of the next force evaluation.

@@ -257,6 +257,10 @@ int scan_exclusive(unsigned* buf, int n, cudaStream_t st) {
 
 }  // namespace
 
+// Start of every key's range after the latest gc_counting_sort: K + 1
+// entries, valid until the next sort.
+const unsigned* gc_sort_starts() { return (const unsigned*)gc_state().scratch[SCR_SORT_COUNT]; }
+
 // Stable sort of (keys, values) by key in [0, K); shared by K5 and the fused
 // step.  `keys` and `vals` are sorted in place.
 int gc_counting_sort(int n, int K, int* keys, int* vals, cudaStream_t st) {

@@ -95,7 +95,7 @@ long long gc_noise_step() {
 
 // Builds the grid for the bbox (lo_x, hi_x, lo_y, hi_y, lo_z, hi_z), cube
 // size rc and periodic mask.  Layout of bbox follows BBox in src/main.cuh:12.
-static int build_grid(const float* bb, float rc, int mask, GcGrid* g) {
+int gc_build_grid(const float* bb, float rc, int mask, GcGrid* g) {
     memset(g, 0, sizeof(*g));
     g->pmask = mask;
     long long total = 1;
@@ -132,7 +132,7 @@ int gc_ensure_grid(const float* d_bbox) {
     float bb[6];
     GC_CUDA(cudaMemcpyAsync(bb, d_bbox, sizeof(bb), cudaMemcpyDeviceToHost, s.stream), "read bbox");
     GC_CUDA(cudaStreamSynchronize(s.stream), "read bbox");
-    GC_TRY(build_grid(bb, s.c.CutRadius, s.periodic_mask, &s.grid));
+    GC_TRY(gc_build_grid(bb, s.c.CutRadius, s.periodic_mask, &s.grid));
     s.grid_set = true;
     s.grid_bbox_ptr = d_bbox;
     s.grid_mask = s.periodic_mask;
@@ -140,11 +140,9 @@ int gc_ensure_grid(const float* d_bbox) {
     return GC_OK;
 }
 
-int gc_make_params(GcParams* p, bool need_grid) {
-    GcState& s = gc_state();
-    if (!s.consts_set) return gc_fail(GC_ESTATE, "called before ConstsDataUp");
-    if (need_grid && !s.grid_set) return gc_fail(GC_ESTATE, "neighbour sweep before PreConList built the grid");
-    const Structconst& c = s.c;
+int gc_params_from(const Structconst& c, int noise_on, GcParams* p) {
+    if (!(c.CutRadius > 0.f) || !(c.Mass > 0.f) || !(c.TimeStep > 0.f))
+        return gc_fail(GC_EINVAL, "CutRadius, Mass and TimeStep must be positive");
     memset(p, 0, sizeof(*p));
     p->nB2 = c.nBound2Start;
     p->nF = c.nFluidStart;
@@ -173,7 +171,7 @@ int gc_make_params(GcParams* p, bool need_grid) {
     p->visB = (float)B;
     p->sqrtA = (float)sqrt(A > 0 ? A : 0.0);
     p->sqrtAB = (float)sqrt(A + B > 0 ? A + B : 0.0);
-    p->noise_pref = (s.noise_on && c.Temp > 0.f) ? (float)(2.0 * c.Temp / c.TimeStep) : 0.f;
+    p->noise_pref = (noise_on && c.Temp > 0.f) ? (float)(2.0 * c.Temp / c.TimeStep) : 0.f;
     p->rep_r0 = (float)(rc / 3.0);
     p->rep_r0sq = p->rep_r0 * p->rep_r0;
     p->rep_D = p->c1sq;
@@ -185,6 +183,14 @@ int gc_make_params(GcParams* p, bool need_grid) {
     uint64_t seed = (uint64_t)c.iSeed;
     p->seed_lo = (uint32_t)seed;
     p->seed_hi = (uint32_t)(seed >> 32);
+    return GC_OK;
+}
+
+int gc_make_params(GcParams* p, bool need_grid) {
+    GcState& s = gc_state();
+    if (!s.consts_set) return gc_fail(GC_ESTATE, "called before ConstsDataUp");
+    if (need_grid && !s.grid_set) return gc_fail(GC_ESTATE, "neighbour sweep before PreConList built the grid");
+    GC_TRY(gc_params_from(s.c, s.noise_on, p));
     uint64_t st = (uint64_t)gc_noise_step();
     p->step_lo = (uint32_t)st;
     p->step_hi = (uint32_t)(st >> 32);

@@ -136,6 +136,66 @@ int gc_cudiv_SortArraysWithCells(int n, int* d_sortpart, int* d_oldpos, int* d_c
  * first min(n, 16) slots to stdout.  Synchronises. */
 int gc_cudiv_Printf(int n, int* d_curpos, int* d_sortpart, float* d_totalcoor);
 
+/* ---- fused timestep (no counterpart in the reference) -------------------
+ *
+ * The same method and step order as one Particle::UpdatePar sequence
+ * (src/Particle.cu:1310-1329), on state the library owns: Verlet neighbour
+ * lists with a skin (re-sorted and rebuilt only when a particle has moved
+ * more than skin/2), fused passes, FP64 per-cell area/volume sums.  The
+ * caller loads the state of GPUCell's host frame once (original particle
+ * order, reference layouts), steps, and stores it back whenever it wants to
+ * output; pointers are host pointers unless the *_device flag is set.
+ * Noise steps are numbered from 0 after gc_fused_setup, as the boundary
+ * entry points number them after ConstsDataUp. */
+typedef struct GcFused GcFused;
+typedef struct {
+    float skin;           /* Verlet skin in units of CutRadius (0: 0.1) */
+    int block;            /* threads per block of the particle kernels: 64, 128, 256 or 512 (0: 128) */
+    int list_capacity;    /* initial neighbour-list capacity per particle (0: from the density) */
+    int reserved[5];
+} GcFusedOptions;
+/* bbox6 (host) as src/main.cuh:12; periodic_mask as gc_set_periodic. */
+int gc_fused_create(const Structconst* consts, const float* bbox6, int periodic_mask, int noise_on,
+                    const GcFusedOptions* opt, GcFused** out);
+/* Membrane topology and per-edge / per-triangle moduli (host arrays, the
+ * reference's 1-based conventions, src/Particle.cu:174-303, :405-425). */
+int gc_fused_set_cells(GcFused* f, int ncell, int ntri, int nedge, const int* tri, const int* edge,
+                       const int* betri, const int* celltab, const float* shearmod, const float* bendmod,
+                       const float* hlarea, const float* hgarea, const float* hvol);
+/* State in original order: positions, velocities, VelHalf (prescribed wall
+ * velocity of Bound2 particles), forces, crossing counts (NULL = zero).
+ * Before gc_fused_setup this is the initial state; afterwards it replaces
+ * the state in place (NULL = keep) and the neighbour lists are kept unless
+ * the displacement check of the next step asks for a rebuild. */
+int gc_fused_load(GcFused* f, const float* pos, const float* vel, const float* velhalf, const float* force,
+                  const int* nthro, int from_device);
+/* Reference geometry and membrane mechanics (CalGeoPara with StepCount -1
+ * and SetMechPara, src/Particle.cu:476-480) and the first neighbour lists. */
+int gc_fused_setup(GcFused* f);
+/* nsteps timesteps; drive_on as Particle::DrivePar (src/Particle.cu:1302). */
+int gc_fused_step(GcFused* f, int nsteps, int drive_on);
+/* State in original order (NULL pointers are skipped). */
+int gc_fused_store(GcFused* f, float* pos, float* vel, float* rho, float* press, float* force, float* velhalf,
+                   int* nthro, int to_device);
+/* Membrane outputs of the latest step, in the reference's orders. */
+int gc_fused_store_cells(GcFused* f, float* area, float* vol, float* defforce, float* aggforce, float* trinordir,
+                         float* tricenter, float* pararea, int to_device);
+/* Per-cell area and volume as summed (FP64), host pointers. */
+int gc_fused_cell_sums(GcFused* f, double* area, double* vol);
+/* List rebuilds, steps taken, list capacity, mean and max list length. */
+int gc_fused_stats(GcFused* f, long long* rebuilds, long long* steps, int* list_capacity, double* mean_neighbors,
+                   int* max_neighbors);
+/* Reads and clears the handle's device status flags (GC_FLAG_*). */
+int gc_fused_flags(GcFused* f, unsigned* flags);
+/* Times the density and force kernels of every following step with CUDA
+ * events on the library's stream (1) or stops doing so (0). */
+int gc_fused_profile(GcFused* f, int enable);
+/* Total milliseconds of the density and force kernels and the number of
+ * steps timed since gc_fused_profile(f, 1) or the previous read.
+ * Synchronises. */
+int gc_fused_profile_read(GcFused* f, double* density_ms, double* force_ms, long long* steps);
+int gc_fused_destroy(GcFused* f);
+
 /* ---- test hooks (no counterpart in the reference) ----------------------- */
 
 /* Runs the production neighbour traversal of CalFluidDen over the current

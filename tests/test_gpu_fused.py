@@ -1,0 +1,126 @@
+"""The fused timestep (gc_fused_*) against the FP64 oracle and against the
+boundary entry points.
+
+Tolerances, stated per test:
+  * a few steps from rest, noise off: positions within 1e-5, velocities
+    within 1e-4 of their largest magnitude, cell area and volume (FP64 sums)
+    within 1e-5 relative of the oracle;
+  * noise on, against the boundary entry points (same Philox pair noise):
+    positions within 1e-5, forces within 1e-4 of their largest magnitude.
+"""
+import numpy as np
+import pytest
+
+from gpucell_gb300 import generator as gen
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle(cfg, noise):
+    from oracle.binding import Oracle
+    o = Oracle(cfg, noise=noise)
+    o.setup()
+    return o
+
+
+def _close_rel(got, want, tol):
+    scale = max(np.abs(want).max(), 1e-30)
+    err = np.abs(got - want).max()
+    assert err <= tol * scale, f"max err {err:g} vs scale {scale:g}"
+
+
+def test_fused_tracks_oracle_noise_off(cuda_device):
+    from gpucell_gb300.fused import FusedSystem
+    cfg = gen.small_channel()
+    fs = FusedSystem(cfg, noise=False)
+    o = _oracle(cfg, False)
+    for _ in range(3):
+        fs.step(1, 1)
+        o.step()
+    g = fs.fetch()
+    np.testing.assert_allclose(g["pos"], o.pos, atol=1e-5)
+    _close_rel(g["vel"], o.vel, 1e-4)
+    np.testing.assert_allclose(g["Area64"], o.area, rtol=1e-5)
+    np.testing.assert_allclose(g["Vol64"], o.vol, rtol=1e-5)
+    np.testing.assert_allclose(g["rho"][cfg.n_b1 + cfg.n_b2:], o.rho[cfg.n_b1 + cfg.n_b2:], rtol=1e-5)
+    assert fs.flags() == 0
+
+
+def test_fused_matches_boundary_path_with_noise(cuda_device):
+    from gpucell_gb300.fused import FusedSystem
+    from gpucell_gb300.host import ParticleSystem
+    cfg = gen.small_channel()
+    ps = ParticleSystem(cfg, noise=True)
+    fs = FusedSystem(cfg, noise=True)
+    for _ in range(2):
+        ps.update()
+        fs.step(1, 1)
+    a, b = ps.fetch(), fs.fetch()
+    np.testing.assert_allclose(b["pos"], a["pos"], atol=1e-5)
+    _close_rel(b["force"], a["force"], 1e-4)
+    _close_rel(b["vel"], a["vel"], 1e-4)
+
+
+def test_fused_rebuilds_keep_parity(cuda_device):
+    """A tiny skin forces frequent list rebuilds; the trajectory still
+    follows the oracle (noise off)."""
+    from gpucell_gb300.fused import FusedSystem
+    cfg = gen.small_channel()
+    fs = FusedSystem(cfg, noise=False, skin=0.002)
+    o = _oracle(cfg, False)
+    for _ in range(8):
+        fs.step(1, 1)
+        o.step()
+    st = fs.stats()
+    assert st["rebuilds"] >= 3, st
+    g = fs.fetch()
+    np.testing.assert_allclose(g["pos"], o.pos, atol=5e-5)
+    _close_rel(g["vel"], o.vel, 1e-3)
+
+
+def test_fused_periodic_suspension(cuda_device):
+    """Fully periodic box with cells that cross the faces."""
+    from gpucell_gb300.fused import FusedSystem
+    cfg = gen.suspension(nx=36, ny=24, nz=24, ncells=3, subdiv=2, hematocrit=0.15, seed=3)
+    fs = FusedSystem(cfg, noise=False)
+    o = _oracle(cfg, False)
+    for _ in range(3):
+        fs.step(1, 1)
+        o.step()
+    g = fs.fetch()
+    assert np.array_equal(g["nthro"], o.nthro)
+    np.testing.assert_allclose(g["pos"], o.pos, atol=1e-5)
+    _close_rel(g["vel"], o.vel, 1e-4)
+    np.testing.assert_allclose(g["Area64"], o.area, rtol=1e-5)
+    np.testing.assert_allclose(g["Vol64"], o.vol, rtol=1e-5)
+
+
+def test_fused_aggregation(cuda_device):
+    from gpucell_gb300.fused import FusedSystem
+    phys = gen.Physics(sur_energy=5.0, max_cut=1.2, zero_len=0.3, sca_fac=4.0)
+    cfg = gen.channel(nx=24, ny=12, nz=18, wall_layers=3, b1_layers=1, cell_subdiv=2, cell_diameter=3.0,
+                      phys=phys, cell_centers=[(0.0, -0.55, 0.0), (0.0, 0.55, 0.0)], seed=11, name="two_cells")
+    fs = FusedSystem(cfg, noise=False)
+    o = _oracle(cfg, False)
+    for _ in range(2):
+        fs.step(1, 1)
+        o.step()
+    g = fs.fetch()
+    assert np.abs(o.aggforce).max() > 0
+    _close_rel(g["AggForce"], o.aggforce, 2e-5)
+    _close_rel(g["DefForce"], o.defforce, 2e-5)
+    np.testing.assert_allclose(g["pos"], o.pos, atol=1e-5)
+
+
+def test_fused_store_load_round_trip(cuda_device):
+    from gpucell_gb300.fused import FusedSystem
+    cfg = gen.small_channel()
+    fs = FusedSystem(cfg, noise=True)
+    fs.step(2, 1)
+    a = fs.fetch()
+    fs.load(a["pos"], a["vel"], a["velhalf"], a["force"], a["nthro"])
+    b = fs.fetch()
+    for k in ("pos", "vel", "velhalf", "force", "nthro"):
+        assert np.array_equal(a[k], b[k]), k
+    fs.step(1, 1)      # continues from the reloaded state
+    assert np.isfinite(fs.fetch()["pos"]).all()
