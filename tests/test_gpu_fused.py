@@ -108,7 +108,11 @@ def test_fused_aggregation(cuda_device):
     g = fs.fetch()
     assert np.abs(o.aggforce).max() > 0
     _close_rel(g["AggForce"], o.aggforce, 2e-5)
-    _close_rel(g["DefForce"], o.defforce, 2e-5)
+    # Near rest the deformation force is a small net of large area/volume
+    # terms (k (A - A0)/A0 dA/dx with k = 5000): compare on the scale of one
+    # term, k times a mean edge length, not on the scale of the net.
+    edge = float(np.mean(o.refedgelen))
+    np.testing.assert_allclose(g["DefForce"], o.defforce, atol=1e-5 * phys.hgarea * edge)
     np.testing.assert_allclose(g["pos"], o.pos, atol=1e-5)
 
 
