@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--small", action="store_true", help="a 1/8-size suspension (for quick checks)")
+    ap.add_argument("--no-noise", dest="noise", action="store_false",
+                    help="thermal noise off (for cost breakdowns; the reported workload has it on)")
     return ap.parse_args()
 
 
@@ -195,7 +197,7 @@ def run_ours(args):
     K = args.steps
     plain = measure_plain(cfg, dev, steps=min(K, 10), warmup=3) if args.plain else None
 
-    fs = FusedSystem(cfg, noise=True, skin=args.skin, block=args.block)
+    fs = FusedSystem(cfg, noise=args.noise, skin=args.skin, block=args.block)
     fs.step(W, 1)
     torch.cuda.synchronize()
     sampler = ClockSampler()
@@ -288,7 +290,7 @@ def run_ours(args):
         "config": dict(wdesc, particles=n, membrane_vertices=cfg.ncp, triangles=cfg.ntri, edges=cfg.nedge,
                        parallelism=f"replicas x{world}" if world > 1 else "single GPU",
                        l2="working set (>1 GB: state + neighbour lists) is larger than L2; no flush",
-                       noise="on", skin=args.skin, block=args.block),
+                       noise="on" if args.noise else "off", skin=args.skin, block=args.block),
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": bi,
                 "d2h_bytes_per_step": bo, "steps": KE,

@@ -40,6 +40,24 @@ __device__ __forceinline__ size_t sell(int i, int k, int cap) {
     return ((size_t)(i >> 5) * cap + k) * 32 + (i & 31);
 }
 
+// Box constants of the per-step kernels.
+struct Box {
+    float L[3], invL[3];
+    int pmask;
+};
+
+// Minimum image of a list pair.  A listed pair is either far closer than
+// L/2 or close to L apart along a periodic axis, so d - L rint(d/L) makes
+// the same shift as the conditional form of the boundary kernels and
+// rounds the same way (one subtraction of L), i.e. the same FP32 value.
+__device__ __forceinline__ float3 pair_image(float3 a, float3 b, const Box& B) {
+    float3 d = f3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+    if (B.pmask & 1) d.x = fmaf(-B.L[0], rintf(d.x * B.invL[0]), d.x);
+    if (B.pmask & 2) d.y = fmaf(-B.L[1], rintf(d.y * B.invL[1]), d.y);
+    if (B.pmask & 4) d.z = fmaf(-B.L[2], rintf(d.z * B.invL[2]), d.z);
+    return d;
+}
+
 // ---------------------------------------------------------------------------
 // K2 + K3 + K9 for fluid and membrane slots
 // ---------------------------------------------------------------------------
@@ -107,28 +125,52 @@ struct SlotArrays {
     int4* nthro;
 };
 
-__global__ void fk_permute(int n, const int* __restrict__ perm, SlotArrays src, SlotArrays dst,
+// Gathers the slot arrays into the new order and wraps every position into
+// the box on periodic axes (counting the crossings), so that the list build
+// can use one image shift per row of cubes.
+__global__ void fk_permute(int n, GcGrid g, const int* __restrict__ perm, SlotArrays src, SlotArrays dst,
                            float4* __restrict__ refpos, int* __restrict__ slot_of) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     int o = perm[q];
     float4 x = src.pos[o];
+    int4 t = src.nthro[o];
+    float* xs[3] = {&x.x, &x.y, &x.z};
+    int* ts[3] = {&t.x, &t.y, &t.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (!(g.pmask & (1 << a))) continue;
+        float c = *xs[a];
+        if (!isfinite(c)) continue;
+        int w = (int)floorf((c - g.lo[a]) / g.L[a]);
+        if (w != 0) {
+            c -= (float)w * g.L[a];
+            if (c >= g.hi[a]) { c -= g.L[a]; ++w; }
+            else if (c < g.lo[a]) { c += g.L[a]; --w; }
+            *xs[a] = c;
+            *ts[a] += w;
+        }
+    }
     dst.pos[q] = x;
     dst.vel[q] = src.vel[o];
     dst.vpred[q] = src.vpred[o];
     dst.vh[q] = src.vh[o];
     dst.force[q] = src.force[o];
-    dst.nthro[q] = src.nthro[o];
+    dst.nthro[q] = t;
     refpos[q] = x;
     slot_of[fid(x)] = q;
 }
 
-// One thread per slot scans the 27 cubes of the list grid.  Fluid and
-// membrane slots list every particle within rc + skin; Bound2 slots list the
-// moving particles (for their wall velocity); Bound1 slots list nothing.
-__global__ void fk_build_list(int n, GcParams p, const float4* __restrict__ pos, const unsigned* __restrict__ start,
-                              int* __restrict__ nbr, int* __restrict__ cnt, int cap, float cut2,
-                              unsigned* flags) {
+// One thread per slot scans the cubes of the list grid around its own.
+// Fluid and membrane slots list every particle within rc + skin; Bound2
+// slots list the moving particles (for their wall velocity); Bound1 slots
+// list nothing.  Positions are inside the box on periodic axes (the
+// permutation wraps them), so each neighbouring row of cubes has one image
+// shift, and the three cubes of a row that do not wrap are one contiguous
+// range of slots.
+__global__ void __launch_bounds__(kBS) fk_build_list(int n, GcParams p, const float4* __restrict__ pos,
+                                                     const unsigned* __restrict__ start, int* __restrict__ nbr,
+                                                     int* __restrict__ cnt, int cap, float cut2, unsigned* flags) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 xi4 = pos[i];
@@ -136,26 +178,40 @@ __global__ void fk_build_list(int n, GcParams p, const float4* __restrict__ pos,
     unsigned id = fid(xi4);
     int t = ptype(id, p);
     int k = 0;
+    const GcGrid& g = p.g;
+    auto scan = [&](unsigned b, unsigned e, float sx, float sy, float sz) {
+        for (unsigned j = b; j < e; ++j) {
+            float4 xj = pos[j];
+            float dx = (xi.x - xj.x) + sx, dy = (xi.y - xj.y) + sy, dz = (xi.z - xj.z) + sz;
+            float r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 >= cut2 || (int)j == i) continue;
+            if (t == PT_B2 && !is_mobile(fid(xj), p)) continue;
+            if (k < cap) nbr[sell(i, k, cap)] = (int)j;
+            ++k;
+        }
+    };
     if (t != PT_B1) {
-        bool only_mobile = (t == PT_B2);
-        int cx = cube_coord(xi.x, 0, p.g), cy = cube_coord(xi.y, 1, p.g), cz = cube_coord(xi.z, 2, p.g);
+        int cx = cube_coord(xi.x, 0, g), cy = cube_coord(xi.y, 1, g), cz = cube_coord(xi.z, 2, g);
         for (int dz = -1; dz <= 1; ++dz) {
-            int z = cube_step(cz, dz, 2, p.g);
-            if (z < 0) continue;
+            int z = cz + dz;
+            float sz = 0.f;
+            if (z < 0) { if (!(g.pmask & 4)) continue; z += g.n[2]; sz = g.L[2]; }
+            else if (z >= g.n[2]) { if (!(g.pmask & 4)) continue; z -= g.n[2]; sz = -g.L[2]; }
             for (int dy = -1; dy <= 1; ++dy) {
-                int y = cube_step(cy, dy, 1, p.g);
-                if (y < 0) continue;
-                for (int dx = -1; dx <= 1; ++dx) {
-                    int x = cube_step(cx, dx, 0, p.g);
-                    if (x < 0) continue;
-                    int c = cube_key(x, y, z, p.g);
-                    for (unsigned j = start[c]; j < start[c + 1]; ++j) {
-                        if ((int)j == i) continue;
-                        float4 xj = pos[j];
-                        if (only_mobile && !is_mobile(fid(xj), p)) continue;
-                        if (norm2_rn(min_image(xi, xyz(xj), p.g)) >= cut2) continue;
-                        if (k < cap) nbr[sell(i, k, cap)] = (int)j;
-                        ++k;
+                int y = cy + dy;
+                float sy = 0.f;
+                if (y < 0) { if (!(g.pmask & 2)) continue; y += g.n[1]; sy = g.L[1]; }
+                else if (y >= g.n[1]) { if (!(g.pmask & 2)) continue; y -= g.n[1]; sy = -g.L[1]; }
+                int row = g.n[0] * (y + g.n[1] * z);
+                if (cx >= 1 && cx + 1 < g.n[0]) {
+                    scan(start[row + cx - 1], start[row + cx + 2], 0.f, sy, sz);
+                } else {
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        int x = cx + dx;
+                        float sx = 0.f;
+                        if (x < 0) { if (!(g.pmask & 1)) continue; x += g.n[0]; sx = g.L[0]; }
+                        else if (x >= g.n[0]) { if (!(g.pmask & 1)) continue; x -= g.n[0]; sx = -g.L[0]; }
+                        scan(start[row + x], start[row + x + 1], sx, sy, sz);
                     }
                 }
             }
@@ -171,9 +227,10 @@ __global__ void fk_build_list(int n, GcParams p, const float4* __restrict__ pos,
 // ---------------------------------------------------------------------------
 // K8 + K11 (+ K10 for Bound2 slots)
 // ---------------------------------------------------------------------------
-__global__ void fk_density(int n, GcParams p, const float4* __restrict__ pos, float4* __restrict__ vpred,
-                           const float4* __restrict__ vh, float2* __restrict__ dp, const int* __restrict__ nbr,
-                           const int* __restrict__ cnt, int cap) {
+__global__ void __launch_bounds__(kBS) fk_density(int n, GcParams p, Box B, const float4* __restrict__ pos,
+                                                  float4* __restrict__ vpred, const float4* __restrict__ vh,
+                                                  float2* __restrict__ dp, const int* __restrict__ nbr,
+                                                  const int* __restrict__ cnt, int cap) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 xi4 = pos[i];
@@ -181,18 +238,25 @@ __global__ void fk_density(int n, GcParams p, const float4* __restrict__ pos, fl
     unsigned id = fid(xi4);
     int t = ptype(id, p);
     int c = cnt[i];
+    const int* lp = nbr + sell(i, 0, cap);
     if (t == PT_FLUID || t == PT_MEMB) {
         float sum = p.w0;
+        int jn = c > 0 ? __ldg(lp) : 0;
+        float4 xn = pos[jn];
         for (int k = 0; k < c; ++k) {
-            int j = nbr[sell(i, k, cap)];
-            float4 xj = pos[j];
-            float r2 = norm2_rn(min_image(xi, xyz(xj), p.g));
+            float4 xj = xn;
+            if (k + 1 < c) {
+                jn = __ldg(lp + (size_t)(k + 1) * 32);
+                xn = pos[jn];
+            }
+            float r2 = norm2_rn(pair_image(xi, xyz(xj), B));
             if (r2 >= p.rc2 || !is_sdpd(fid(xj), p)) continue;
-            sum += wendland_w(sqrtf(r2), p);
+            float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+            sum += wendland_w(r, p);
         }
         float rho = p.mass * sum;
         float c2 = (t == PT_MEMB) ? p.c2sq : p.c1sq;
-        float inv_d = 1.f / sum;
+        float inv_d = __frcp_rn(sum);
         dp[i] = make_float2(inv_d, c2 * (rho - p.rho0) * inv_d * inv_d);
         return;
     }
@@ -201,10 +265,11 @@ __global__ void fk_density(int n, GcParams p, const float4* __restrict__ pos, fl
     float3 num = f3(0.f, 0.f, 0.f);
     float den = 0.f;
     for (int k = 0; k < c; ++k) {
-        int j = nbr[sell(i, k, cap)];
-        float r2 = norm2_rn(min_image(xi, xyz(pos[j]), p.g));
+        int j = __ldg(lp + (size_t)k * 32);
+        float r2 = norm2_rn(pair_image(xi, xyz(pos[j]), B));
         if (r2 >= p.rc2) continue;
-        float w = wendland_w(sqrtf(r2), p);
+        float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+        float w = wendland_w(r, p);
         float4 vj = vpred[j];
         num += w * f3(vj.x, vj.y, vj.z);
         den += w;
@@ -218,12 +283,12 @@ __global__ void fk_density(int n, GcParams p, const float4* __restrict__ pos, fl
 // ---------------------------------------------------------------------------
 // K12 + K13 + K14 + membrane forces + K19
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBS) fk_force(int n, GcParams p, const float4* __restrict__ pos,
+__global__ void __launch_bounds__(kBS) fk_force(int n, GcParams p, Box B, const float4* __restrict__ pos,
                                                 const float4* __restrict__ vpred, const float4* __restrict__ vh,
                                                 const float2* __restrict__ dp, float4* __restrict__ force,
                                                 float4* __restrict__ vel, const int* __restrict__ nbr,
                                                 const int* __restrict__ cnt, int cap,
-                                                const float4* __restrict__ mforce, int drive, unsigned* flags) {
+                                                const float4* __restrict__ mforce, int drive) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 xi4 = pos[i];
@@ -238,34 +303,42 @@ __global__ void __launch_bounds__(kBS) fk_force(int n, GcParams p, const float4*
     bool noise = p.noise_pref > 0.f;
     float3 f = f3(0.f, 0.f, 0.f);
     int c = cnt[i];
+    const int* lp = nbr + sell(i, 0, cap);
+    int jn = c > 0 ? __ldg(lp) : 0;
+    float4 xn = pos[jn];
     for (int k = 0; k < c; ++k) {
-        int j = nbr[sell(i, k, cap)];
-        float4 xj4 = pos[j];
-        float3 d = min_image(xi, xyz(xj4), p.g);
+        int j = jn;
+        float4 xj4 = xn;
+        if (k + 1 < c) {   // prefetch the next entry while this one is computed
+            jn = __ldg(lp + (size_t)(k + 1) * 32);
+            xn = pos[jn];
+        }
+        float3 d = pair_image(xi, xyz(xj4), B);
         float r2 = norm2_rn(d);
-        if (r2 >= p.rc2) continue;
+        if (r2 >= p.rc2 || r2 <= 0.f) continue;   // coincident pairs exert no force
         unsigned idj = fid(xj4);
+        float inv_r = rsqrtf(r2);
         if (!is_sdpd(idj, p)) {   // Bound1: repulsion only
-            if (r2 < p.rep_r0sq && r2 > 0.f) {
-                float q2 = p.rep_r0sq / r2, q4 = q2 * q2, q12 = q4 * q4 * q4;
-                f += (p.rep_D * (q12 - q4) / r2) * d;
+            if (r2 < p.rep_r0sq) {
+                float ir2 = inv_r * inv_r;
+                float q2 = p.rep_r0sq * ir2, q4 = q2 * q2, q12 = q4 * q4 * q4;
+                f += (p.rep_D * (q12 - q4) * ir2) * d;
             }
             continue;
         }
-        float r = sqrtf(r2);
-        float F = wendland_f(r, p);
         float2 dpj = dp[j];
-        f += ((dpi.y + dpj.y) * F) * d;
-        if (r2 <= 0.f) continue;
         float4 vj = vpred[j];
-        float inv_r = 1.f / r;
+        float r = r2 * inv_r;
+        float F = wendland_f(r, p);
+        f += ((dpi.y + dpj.y) * F) * d;
         float3 e = inv_r * d;
         float3 vij = f3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z);
         float ev = dot3(e, vij);
         float fdd = F * dpi.x * dpj.x;
         f -= fdd * (p.visA * vij + (p.visB * ev) * e);
         if (noise) {
-            float q = sqrtf(p.noise_pref * fdd);
+            float qq = p.noise_pref * fdd;
+            float q = qq > 0.f ? qq * rsqrtf(qq) : 0.f;
             float3 xi_ = pair_noise(id, idj, p);
             float exi = dot3(e, xi_);
             f += q * (p.sqrtA * xi_ + ((p.sqrtAB - p.sqrtA) * exi) * e);
@@ -276,7 +349,8 @@ __global__ void __launch_bounds__(kBS) fk_force(int n, GcParams p, const float4*
         float4 mf = mforce[id - p.nC];
         f += f3(mf.x, mf.y, mf.z);
     }
-    if (!(isfinite(f.x) && isfinite(f.y) && isfinite(f.z))) raise_flag(flags, GC_FLAG_NONFINITE);
+    // a non-finite force shows up as a non-finite position in the next
+    // fk_integrate, which raises GC_FLAG_NONFINITE
     force[i] = make_float4(f.x, f.y, f.z, 0.f);
     float4 h = vh[i];
     float s = 0.5f * p.dt * p.inv_mass;
@@ -284,7 +358,7 @@ __global__ void __launch_bounds__(kBS) fk_force(int n, GcParams p, const float4*
 }
 
 // second K10: wall velocity from the corrected velocities
-__global__ void fk_wallvel(int n, GcParams p, const float4* __restrict__ pos, float4* __restrict__ vel,
+__global__ void fk_wallvel(int n, GcParams p, Box B, const float4* __restrict__ pos, float4* __restrict__ vel,
                            const float4* __restrict__ vh, const int* __restrict__ nbr, const int* __restrict__ cnt,
                            int cap) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -296,10 +370,10 @@ __global__ void fk_wallvel(int n, GcParams p, const float4* __restrict__ pos, fl
     float den = 0.f;
     int c = cnt[i];
     for (int k = 0; k < c; ++k) {
-        int j = nbr[sell(i, k, cap)];
-        float r2 = norm2_rn(min_image(xi, xyz(pos[j]), p.g));
+        int j = __ldg(nbr + sell(i, k, cap));
+        float r2 = norm2_rn(pair_image(xi, xyz(pos[j]), B));
         if (r2 >= p.rc2) continue;
-        float w = wendland_w(sqrtf(r2), p);
+        float w = wendland_w(r2 > 0.f ? r2 * rsqrtf(r2) : 0.f, p);
         float4 vj = vel[j];
         num += w * f3(vj.x, vj.y, vj.z);
         den += w;
@@ -807,7 +881,7 @@ int rebuild_lists(GcFused* f) {
     fk_cellkey<<<nb, f->block, 0, st>>>(n, f->lgrid, f->a.pos, f->keys, f->vals);
     GC_CHECK_LAUNCH("fused: cube keys");
     GC_TRY(gc_counting_sort(n, f->lgrid.ncells, f->keys, f->vals, st));
-    fk_permute<<<nb, f->block, 0, st>>>(n, f->vals, f->a, f->b, f->refpos, f->slot_of);
+    fk_permute<<<nb, f->block, 0, st>>>(n, f->lgrid, f->vals, f->a, f->b, f->refpos, f->slot_of);
     GC_CHECK_LAUNCH("fused: permute");
     std::swap(f->a, f->b);
     GcParams lp = f->p;
@@ -846,8 +920,19 @@ void prof_mark(GcFused* f) {
     if (e) cudaEventRecord(e, f->st);
 }
 
+Box make_box(const GcGrid& g) {
+    Box b;
+    for (int a = 0; a < 3; ++a) {
+        b.L[a] = g.L[a];
+        b.invL[a] = 1.f / g.L[a];
+    }
+    b.pmask = g.pmask;
+    return b;
+}
+
 int one_step(GcFused* f, int drive) {
     const int n = f->n;
+    const Box B = make_box(f->lgrid);
     const int nb = gc_blocks(n, f->block);
     cudaStream_t st = f->st;
     f->step += 1;
@@ -865,7 +950,7 @@ int one_step(GcFused* f, int drive) {
     GC_CUDA(cudaStreamSynchronize(st), "fused: flag");
     if (*f->h_rebuild) GC_TRY(rebuild_lists(f));
     prof_mark(f);
-    fk_density<<<nb, f->block, 0, st>>>(n, p, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->nbr, f->cnt, f->cap);
+    fk_density<<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->nbr, f->cnt, f->cap);
     GC_CHECK_LAUNCH("fused: density");
     prof_mark(f);
     if (f->ncell > 0) {
@@ -894,12 +979,12 @@ int one_step(GcFused* f, int drive) {
         }
     }
     prof_mark(f);
-    fk_force<<<nb, f->block, 0, st>>>(n, p, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel, f->nbr,
-                                     f->cnt, f->cap, f->ncell > 0 ? f->mforce : nullptr, drive, f->flags);
+    fk_force<<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel, f->nbr,
+                                     f->cnt, f->cap, f->ncell > 0 ? f->mforce : nullptr, drive);
     GC_CHECK_LAUNCH("fused: force");
     prof_mark(f);
     if (p.nF > p.nB2) {
-        fk_wallvel<<<nb, f->block, 0, st>>>(n, p, f->a.pos, f->a.vel, f->a.vh, f->nbr, f->cnt, f->cap);
+        fk_wallvel<<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vel, f->a.vh, f->nbr, f->cnt, f->cap);
         GC_CHECK_LAUNCH("fused: wall velocity");
     }
     f->steps++;
@@ -1111,8 +1196,8 @@ int gc_fused_setup(GcFused* f) {
     GC_TRY(rebuild_lists(f));
     // density and pressure of the loaded state (the reference has them from
     // DenInit until the first step recomputes them)
-    fk_density<<<gc_blocks(f->n, f->block), f->block, 0, st>>>(f->n, p, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->nbr,
-                                                               f->cnt, f->cap);
+    fk_density<<<gc_blocks(f->n, f->block), f->block, 0, st>>>(f->n, p, make_box(f->lgrid), f->a.pos, f->a.vpred,
+                                                               f->a.vh, f->dp, f->nbr, f->cnt, f->cap);
     GC_CHECK_LAUNCH("fused: set-up density");
     f->setup_done = true;
     f->step = -1;

@@ -175,8 +175,12 @@ __device__ __forceinline__ float wendland_f(float r, const GcParams& p) {
 // order.
 // ---------------------------------------------------------------------------
 
-__host__ __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
-                                                       uint32_t k0, uint32_t k1, uint32_t out[4]) {
+struct PhiloxOut {
+    uint32_t w0, w1, w2, w3;
+};
+
+__host__ __device__ __forceinline__ PhiloxOut philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                            uint32_t k0, uint32_t k1) {
 #ifdef __CUDA_ARCH__
 #pragma unroll
 #endif
@@ -193,7 +197,7 @@ __host__ __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1,
         c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
         k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
     }
-    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+    return PhiloxOut{c0, c1, c2, c3};
 }
 
 // A uniform variate with zero mean and unit variance from the top 24 bits
@@ -208,10 +212,9 @@ __device__ __forceinline__ float unit_uniform(uint32_t w) {
 __device__ __forceinline__ float3 pair_noise(unsigned id_i, unsigned id_j, const GcParams& p) {
     unsigned a = id_i < id_j ? id_i : id_j;
     unsigned b = id_i < id_j ? id_j : id_i;
-    uint32_t w[4];
-    philox4x32_10(a, b, p.step_lo, p.step_hi, p.seed_lo, p.seed_hi, w);
+    PhiloxOut w = philox4x32_10(a, b, p.step_lo, p.step_hi, p.seed_lo, p.seed_hi);
     float s = id_i < id_j ? 1.f : -1.f;
-    return f3(s * unit_uniform(w[0]), s * unit_uniform(w[1]), s * unit_uniform(w[2]));
+    return f3(s * unit_uniform(w.w0), s * unit_uniform(w.w1), s * unit_uniform(w.w2));
 }
 
 // ---------------------------------------------------------------------------
