@@ -936,9 +936,7 @@ int one_step(GcFused* f, int drive) {
     const int nb = gc_blocks(n, f->block);
     cudaStream_t st = f->st;
     f->step += 1;
-    uint64_t s = (uint64_t)f->step;
-    f->p.step_lo = (uint32_t)s;
-    f->p.step_hi = (uint32_t)(s >> 32);
+    f->p.noise_key = noise_key(f->p.seed, (uint64_t)f->step);
     GcParams p = f->p;
     p.g = f->lgrid;
     float hs = 0.5f * f->skin * 0.99f;

@@ -65,9 +65,9 @@ struct GcParams {
     float rep_r0, rep_r0sq, rep_D;
     // Morse aggregation
     float De, beta, r0m, maxcut, maxcut2;
-    // pair-noise key
-    uint32_t seed_lo, seed_hi;
-    uint32_t step_lo, step_hi;
+    // pair-noise key of the current step (noise_key(seed, step))
+    uint64_t seed;
+    uint32_t noise_key;
     GcGrid g;
 };
 
@@ -168,53 +168,66 @@ __device__ __forceinline__ float wendland_f(float r, const GcParams& p) {
 }
 
 // ---------------------------------------------------------------------------
-// Philox4x32-10 (Salmon, Moraes, Dror & Shaw, SC'11), the counter-based
-// generator behind the pair noise.  Counter = (min id, max id, step lo,
-// step hi), key = the 64-bit seed; the same four words on both sides of a
-// pair give an antisymmetric pair noise that does not depend on the particle
-// order.
+// Pair noise: Philox2x32-10 (Salmon, Moraes, Dror & Shaw, SC'11).
+// Counter = (min id, max id); key = a per-step word hashed from the 64-bit
+// seed and the step index with the SplitMix64 finaliser (Steele, Lea &
+// Flood 2014), computed once per step on the host (noise_key).  The same
+// two words on both sides of a pair give an antisymmetric pair noise that
+// does not depend on the particle order.
 // ---------------------------------------------------------------------------
 
-struct PhiloxOut {
-    uint32_t w0, w1, w2, w3;
+__host__ __device__ __forceinline__ uint64_t splitmix64_mix(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Per-step key of the pair noise.
+__host__ __device__ __forceinline__ uint32_t noise_key(uint64_t seed, uint64_t step) {
+    return (uint32_t)(splitmix64_mix(seed * 0x9E3779B97F4A7C15ull + step) >> 32);
+}
+
+struct Philox2 {
+    uint32_t w0, w1;
 };
 
-__host__ __device__ __forceinline__ PhiloxOut philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
-                                                            uint32_t k0, uint32_t k1) {
+__host__ __device__ __forceinline__ Philox2 philox2x32_10(uint32_t c0, uint32_t c1, uint32_t k) {
 #ifdef __CUDA_ARCH__
 #pragma unroll
 #endif
     for (int r = 0; r < 10; ++r) {
 #ifdef __CUDA_ARCH__
-        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t hi = __umulhi(0xD256D193u, c0), lo = 0xD256D193u * c0;
 #else
-        uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
-        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
-        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        uint64_t pr = (uint64_t)0xD256D193u * c0;
+        uint32_t hi = (uint32_t)(pr >> 32), lo = (uint32_t)pr;
 #endif
-        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
-        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+        c0 = hi ^ k ^ c1;
+        c1 = lo;
+        k += 0x9E3779B9u;
     }
-    return PhiloxOut{c0, c1, c2, c3};
+    return Philox2{c0, c1};
 }
 
-// A uniform variate with zero mean and unit variance from the top 24 bits
-// of a Philox word: sqrt(12) ((w >> 8) + 1/2) / 2^24 - sqrt(3).  Groot &
-// Warren (1997) drive the same integrator with uniform noise; only the first
-// two moments enter the fluctuation-dissipation balance.
-__device__ __forceinline__ float unit_uniform(uint32_t w) {
-    return fmaf((float)(w >> 8) + 0.5f, 3.4641016151377544f / 16777216.f, -1.7320508075688772f);
+// Three uniform variates with zero mean and unit variance from the 63 low
+// bits of the two words, 21 bits each: sqrt(12) (u + 1/2) / 2^21 - sqrt(3).
+// Groot & Warren (1997) drive the same integrator with uniform noise; only
+// the first two moments enter the fluctuation-dissipation balance.
+__device__ __forceinline__ float unit_uniform21(uint32_t u) {
+    return fmaf((float)u + 0.5f, 3.4641016151377544f / 2097152.f, -1.7320508075688772f);
 }
 
-// The three noise components xi_ij for the pair (i, j); xi_ji = -xi_ij.
+// The noise components xi_ij for the pair (i, j); xi_ji = -xi_ij.
 __device__ __forceinline__ float3 pair_noise(unsigned id_i, unsigned id_j, const GcParams& p) {
     unsigned a = id_i < id_j ? id_i : id_j;
     unsigned b = id_i < id_j ? id_j : id_i;
-    PhiloxOut w = philox4x32_10(a, b, p.step_lo, p.step_hi, p.seed_lo, p.seed_hi);
+    Philox2 w = philox2x32_10(a, b, p.noise_key);
+    uint32_t u0 = w.w0 & 0x1FFFFFu;
+    uint32_t u1 = (w.w0 >> 21) | ((w.w1 & 0x3FFu) << 11);
+    uint32_t u2 = (w.w1 >> 10) & 0x1FFFFFu;
     float s = id_i < id_j ? 1.f : -1.f;
-    return f3(s * unit_uniform(w.w0), s * unit_uniform(w.w1), s * unit_uniform(w.w2));
+    return f3(s * unit_uniform21(u0), s * unit_uniform21(u1), s * unit_uniform21(u2));
 }
 
 // ---------------------------------------------------------------------------

@@ -180,9 +180,8 @@ int gc_params_from(const Structconst& c, int noise_on, GcParams* p) {
     p->r0m = c.zeroLen;
     p->maxcut = c.MaxCut;
     p->maxcut2 = c.MaxCut * c.MaxCut;
-    uint64_t seed = (uint64_t)c.iSeed;
-    p->seed_lo = (uint32_t)seed;
-    p->seed_hi = (uint32_t)(seed >> 32);
+    p->seed = (uint64_t)c.iSeed;
+    p->noise_key = noise_key(p->seed, 0);
     return GC_OK;
 }
 
@@ -191,9 +190,7 @@ int gc_make_params(GcParams* p, bool need_grid) {
     if (!s.consts_set) return gc_fail(GC_ESTATE, "called before ConstsDataUp");
     if (need_grid && !s.grid_set) return gc_fail(GC_ESTATE, "neighbour sweep before PreConList built the grid");
     GC_TRY(gc_params_from(s.c, s.noise_on, p));
-    uint64_t st = (uint64_t)gc_noise_step();
-    p->step_lo = (uint32_t)st;
-    p->step_hi = (uint32_t)(st >> 32);
+    p->noise_key = noise_key(p->seed, (uint64_t)gc_noise_step());
     if (s.grid_set) p->g = s.grid;
     return GC_OK;
 }

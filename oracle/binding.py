@@ -65,6 +65,9 @@ def load():
         lib.or_morse_energy.restype = C.c_double
         lib.or_pair_noise.argtypes = [S, C.c_uint, C.c_uint, _D]
         lib.or_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        lib.or_philox2x32_10.argtypes = [C.POINTER(C.c_uint32), C.c_uint32, C.POINTER(C.c_uint32)]
+        lib.or_noise_key.argtypes = [C.c_uint64, C.c_uint64]
+        lib.or_noise_key.restype = C.c_uint32
         _lib = lib
     return _lib
 
@@ -170,6 +173,18 @@ class Oracle:
 
     def step(self):
         return self.call("step")
+
+
+def philox2(ctr, key):
+    lib = load()
+    c = (C.c_uint32 * 2)(*ctr)
+    o = (C.c_uint32 * 2)()
+    lib.or_philox2x32_10(c, key, o)
+    return list(o)
+
+
+def noise_key(seed, step):
+    return int(load().or_noise_key(seed, step))
 
 
 def philox(ctr, key):

@@ -19,7 +19,8 @@
  *                       Monaghan, JCP 110, 399 (1994) (repulsion, 12-4)
  *   membrane            Fedosov, Caswell & Karniadakis, Biophys. J. 98, 2215 (2010)
  *   aggregation         Morse potential, area-weighted
- *   pair noise          Philox4x32-10, Salmon et al., SC'11
+ *   pair noise          Philox2x32-10, Salmon et al., SC'11, keyed per step
+ *                       by the SplitMix64 finaliser
  *
  * Everything is double precision except the neighbour predicate, which is
  * evaluated in FP32 from the FP32-rounded positions exactly as the GPU does
@@ -122,16 +123,35 @@ void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
+/* Philox2x32-10: one 32x32 -> 64 multiply per round, Weyl key schedule. */
+void or_philox2x32_10(const uint32_t ctr[2], uint32_t key, uint32_t out[2]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], k = key;
+    for (int r = 0; r < 10; ++r) {
+        uint64_t pr = (uint64_t)0xD256D193u * c0;
+        uint32_t n0 = (uint32_t)(pr >> 32) ^ k ^ c1;
+        c1 = (uint32_t)pr;
+        c0 = n0;
+        k += 0x9E3779B9u;
+    }
+    out[0] = c0;
+    out[1] = c1;
+}
+
+/* Per-step key: SplitMix64 finaliser of seed * golden + step, high word. */
+uint32_t or_noise_key(uint64_t seed, uint64_t step) {
+    return (uint32_t)(mix64(seed * 0x9E3779B97F4A7C15ull + step) >> 32);
+}
+
+/* The pair noise: Philox2x32-10 on (min id, max id) with the step key; three
+ * 21-bit fields of the 64 output bits, each mapped to a uniform variate of
+ * zero mean and unit variance; antisymmetric in (i, j). */
 void or_pair_noise(const or_state* s, unsigned id_i, unsigned id_j, double out[3]) {
     unsigned a = id_i < id_j ? id_i : id_j, b = id_i < id_j ? id_j : id_i;
-    uint64_t st = (uint64_t)s->step, seed = (uint64_t)s->c.iSeed;
-    uint32_t ctr[4] = {a, b, (uint32_t)st, (uint32_t)(st >> 32)};
-    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
-    uint32_t w[4];
-    or_philox4x32_10(ctr, key, w);
+    uint32_t ctr[2] = {a, b}, w[2];
+    or_philox2x32_10(ctr, or_noise_key((uint64_t)s->c.iSeed, (uint64_t)s->step), w);
+    uint32_t u[3] = {w[0] & 0x1FFFFFu, (w[0] >> 21) | ((w[1] & 0x3FFu) << 11), (w[1] >> 10) & 0x1FFFFFu};
     double sg = id_i < id_j ? 1.0 : -1.0;
-    for (int k = 0; k < 3; ++k)
-        out[k] = sg * (sqrt(12.0) * (((double)(w[k] >> 8) + 0.5) / 16777216.0) - sqrt(3.0));
+    for (int k = 0; k < 3; ++k) out[k] = sg * (sqrt(12.0) * (((double)u[k] + 0.5) / 2097152.0) - sqrt(3.0));
 }
 
 /* ------------------------------------------------------------------------ */

@@ -105,8 +105,11 @@ double or_morse_energy(const or_state* s);      /* aggregation */
 /* The pair noise xi_ij (3 components) for ids i, j at the state's step. */
 void or_pair_noise(const or_state* s, unsigned id_i, unsigned id_j, double out[3]);
 
-/* Philox4x32-10 on one counter (for known-answer tests). */
+/* Philox4x32-10 and Philox2x32-10 on one counter (known-answer tests). */
 void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+void or_philox2x32_10(const uint32_t ctr[2], uint32_t key, uint32_t out[2]);
+/* Key of the pair noise at `step` for `seed`. */
+uint32_t or_noise_key(uint64_t seed, uint64_t step);
 
 #ifdef __cplusplus
 }

@@ -12,8 +12,9 @@ computed here independently of oracle/oracle.c:
   shear-modulus relation of Fedosov et al. 2010);
 * the SDPD force between two fluid particles (Espanol & Revenga 2003) with
   the noise off, written out term by term;
-* Philox4x32-10 outputs from a from-scratch Python implementation of the
-  round function of Salmon et al. (2011).
+* Philox4x32-10 and Philox2x32-10 outputs and the per-step noise key
+  (SplitMix64 finaliser) from from-scratch Python implementations of the
+  published round functions (Salmon et al. 2011; Steele, Lea & Flood 2014).
 
 Run:  python tests/golden/make_golden.py
 """
@@ -79,6 +80,29 @@ def philox(ctr, key, rounds=10):
     return c
 
 
+def philox2(ctr, key, rounds=10):
+    c0, c1, k = ctr[0], ctr[1], key
+    for _ in range(rounds):
+        pr = 0xD256D193 * c0
+        c0, c1 = ((pr >> 32) ^ k ^ c1) & M32, pr & M32
+        k = (k + 0x9E3779B9) & M32
+    return [c0, c1]
+
+
+M64 = (1 << 64) - 1
+
+
+def splitmix_mix(z):
+    z = (z + 0x9E3779B97F4A7C15) & M64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M64
+    return z ^ (z >> 31)
+
+
+def noise_key(seed, step):
+    return splitmix_mix((seed * 0x9E3779B97F4A7C15 + step) & M64) >> 32
+
+
 def main():
     radii = [0.0, 0.125, 0.25, 0.5, 0.75, 0.9]
     g = dict(
@@ -96,6 +120,10 @@ def main():
     for ctr, key in (([0, 0, 0, 0], [0, 0]), ([1, 2, 3, 4], [5, 6]), ([7, 123456, 42, 0], [1, 0]),
                      ([M32, M32, M32, M32], [M32, M32])):
         g["philox"].append(dict(ctr=ctr, key=key, out=philox(ctr, key)))
+    g["philox2"] = [dict(ctr=c, key=k, out=philox2(c, k)) for c, k in
+                     (([0, 0], 0), ([1, 2], 3), ([123456, 7654321], 0xDEADBEEF), ([M32, M32], M32))]
+    g["noise_key"] = [dict(seed=sd, step=st, key=noise_key(sd, st)) for sd, st in ((1, 0), (1, 1), (1, 17),
+                                                                                  (12345, 999), (2 ** 40 + 3, 5))]
     with open(OUT, "w") as f:
         json.dump(g, f, indent=1)
     print("wrote", OUT)

@@ -21,9 +21,29 @@ def _pair_config(x0, x1, pmask=0, box=10.0):
 
 
 def test_philox_matches_independent_python(oracle_lib):
-    from oracle.binding import philox
+    from oracle.binding import noise_key, philox, philox2
     for case in GOLDEN["philox"]:
         assert philox(case["ctr"], case["key"]) == case["out"]
+    for case in GOLDEN["philox2"]:
+        assert philox2(case["ctr"], case["key"]) == case["out"]
+    for case in GOLDEN["noise_key"]:
+        assert noise_key(case["seed"], case["step"]) == case["key"]
+
+
+def test_pair_noise_moments_and_antisymmetry(oracle_lib):
+    """xi_ij = -xi_ji; over many pairs the components have zero mean, unit
+    variance and no correlation (uniform on [-sqrt 3, sqrt 3])."""
+    from oracle.binding import Oracle
+    cfg = _pair_config([0.0, 0.0, 0.0], [0.3, 0.0, 0.0])
+    o = Oracle(cfg, noise=True)
+    rng = np.random.default_rng(0)
+    ids = rng.integers(0, 1 << 22, size=(20000, 2))
+    xs = np.array([o.pair_noise(int(a), int(b)) for a, b in ids if a != b])
+    np.testing.assert_allclose(o.pair_noise(5, 9), -o.pair_noise(9, 5))
+    assert abs(xs.mean()) < 0.02 and abs(xs.var() - 1.0) < 0.03
+    cc = np.corrcoef(xs.T)
+    assert np.abs(cc - np.eye(3)).max() < 0.03
+    assert xs.max() <= 3 ** 0.5 and xs.min() >= -(3 ** 0.5)
 
 
 def test_wendland_values_and_normalisation(oracle_lib):
