@@ -40,8 +40,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--skin", type=float, default=0.1)
+    ap.add_argument("--skin", type=float, default=0.075)
     ap.add_argument("--block", type=int, default=128)
+    ap.add_argument("--no-compact", dest="compact", action="store_false",
+                    help="force pass iterates the skin lists instead of the per-step compact lists")
     ap.add_argument("--no-plain", dest="plain", action="store_false", help="skip the FP32 boundary-path timing")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=1)
@@ -197,7 +199,7 @@ def run_ours(args):
     K = args.steps
     plain = measure_plain(cfg, dev, steps=min(K, 10), warmup=3) if args.plain else None
 
-    fs = FusedSystem(cfg, noise=args.noise, skin=args.skin, block=args.block)
+    fs = FusedSystem(cfg, noise=args.noise, skin=args.skin, block=args.block, compact=args.compact)
     fs.step(W, 1)
     torch.cuda.synchronize()
     sampler = ClockSampler()
@@ -290,7 +292,8 @@ def run_ours(args):
         "config": dict(wdesc, particles=n, membrane_vertices=cfg.ncp, triangles=cfg.ntri, edges=cfg.nedge,
                        parallelism=f"replicas x{world}" if world > 1 else "single GPU",
                        l2="working set (>1 GB: state + neighbour lists) is larger than L2; no flush",
-                       noise="on" if args.noise else "off", skin=args.skin, block=args.block),
+                       noise="on" if args.noise else "off", skin=args.skin, block=args.block,
+                       compact_lists=args.compact),
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": bi,
                 "d2h_bytes_per_step": bo, "steps": KE,

@@ -53,7 +53,8 @@ assert C.sizeof(Structconst) == 96
 class GcFusedOptions(C.Structure):
     """ctypes mirror of GcFusedOptions (include/gpucell_gb300.h)."""
 
-    _fields_ = [("skin", C.c_float), ("block", C.c_int), ("list_capacity", C.c_int), ("reserved", C.c_int * 5)]
+    _fields_ = [("skin", C.c_float), ("block", C.c_int), ("list_capacity", C.c_int), ("compact", C.c_int),
+                ("reserved", C.c_int * 4)]
 
 _P = C.c_void_p
 _I = C.c_int

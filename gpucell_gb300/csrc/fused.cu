@@ -227,10 +227,15 @@ __global__ void __launch_bounds__(kBS) fk_build_list(int n, GcParams p, const fl
 // ---------------------------------------------------------------------------
 // K8 + K11 (+ K10 for Bound2 slots)
 // ---------------------------------------------------------------------------
+// With `clist` set, fluid and membrane slots also write the entries that
+// act this step (SDPD partners within rc, Bound1 walls within the repulsion
+// range) to a second list in the same layout, so the force pass iterates
+// only interacting pairs.
 __global__ void __launch_bounds__(kBS) fk_density(int n, GcParams p, Box B, const float4* __restrict__ pos,
                                                   float4* __restrict__ vpred, const float4* __restrict__ vh,
                                                   float2* __restrict__ dp, const int* __restrict__ nbr,
-                                                  const int* __restrict__ cnt, int cap) {
+                                                  const int* __restrict__ cnt, int cap, int* __restrict__ clist,
+                                                  int* __restrict__ ccnt) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 xi4 = pos[i];
@@ -241,19 +246,27 @@ __global__ void __launch_bounds__(kBS) fk_density(int n, GcParams p, Box B, cons
     const int* lp = nbr + sell(i, 0, cap);
     if (t == PT_FLUID || t == PT_MEMB) {
         float sum = p.w0;
+        int kc = 0;
         int jn = c > 0 ? __ldg(lp) : 0;
         float4 xn = pos[jn];
         for (int k = 0; k < c; ++k) {
+            int j = jn;
             float4 xj = xn;
             if (k + 1 < c) {
                 jn = __ldg(lp + (size_t)(k + 1) * 32);
                 xn = pos[jn];
             }
             float r2 = norm2_rn(pair_image(xi, xyz(xj), B));
-            if (r2 >= p.rc2 || !is_sdpd(fid(xj), p)) continue;
-            float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
-            sum += wendland_w(r, p);
+            if (r2 >= p.rc2) continue;
+            if (is_sdpd(fid(xj), p)) {
+                float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+                sum += wendland_w(r, p);
+                if (clist && r2 > 0.f) clist[sell(i, kc++, cap)] = j;
+            } else if (clist && r2 < p.rep_r0sq && r2 > 0.f) {
+                clist[sell(i, kc++, cap)] = j;
+            }
         }
+        if (ccnt) ccnt[i] = kc;
         float rho = p.mass * sum;
         float c2 = (t == PT_MEMB) ? p.c2sq : p.c1sq;
         float inv_d = __frcp_rn(sum);
@@ -283,6 +296,9 @@ __global__ void __launch_bounds__(kBS) fk_density(int n, GcParams p, Box B, cons
 // ---------------------------------------------------------------------------
 // K12 + K13 + K14 + membrane forces + K19
 // ---------------------------------------------------------------------------
+// COMPACT: the list holds only pairs that act this step (written by
+// fk_density), so the cut-off test is already done.
+template <bool COMPACT>
 __global__ void __launch_bounds__(kBS) fk_force(int n, GcParams p, Box B, const float4* __restrict__ pos,
                                                 const float4* __restrict__ vpred, const float4* __restrict__ vh,
                                                 const float2* __restrict__ dp, float4* __restrict__ force,
@@ -315,7 +331,7 @@ __global__ void __launch_bounds__(kBS) fk_force(int n, GcParams p, Box B, const 
         }
         float3 d = pair_image(xi, xyz(xj4), B);
         float r2 = norm2_rn(d);
-        if (r2 >= p.rc2 || r2 <= 0.f) continue;   // coincident pairs exert no force
+        if (!COMPACT && (r2 >= p.rc2 || r2 <= 0.f)) continue;   // coincident pairs exert no force
         unsigned idj = fid(xj4);
         float inv_r = rsqrtf(r2);
         if (!is_sdpd(idj, p)) {   // Bound1: repulsion only
@@ -339,7 +355,8 @@ __global__ void __launch_bounds__(kBS) fk_force(int n, GcParams p, Box B, const 
         if (noise) {
             float qq = p.noise_pref * fdd;
             float q = qq > 0.f ? qq * rsqrtf(qq) : 0.f;
-            float3 xi_ = pair_noise(id, idj, p);
+            q = id < idj ? q : -q;   // the pair sign of xi_ij
+            float3 xi_ = pair_noise_unsigned(id, idj, p);
             float exi = dot3(e, xi_);
             f += q * (p.sqrtA * xi_ + ((p.sqrtAB - p.sqrtA) * exi) * e);
         }
@@ -804,6 +821,8 @@ struct GcFused {
     int *keys = nullptr, *vals = nullptr;
     int *nbr = nullptr, *cnt = nullptr;
     size_t nbr_elems = 0;
+    bool compact = false;
+    int *clist = nullptr, *ccnt = nullptr;   // per-step list of interacting pairs (same layout and capacity)
     int* rebuild = nullptr;
     int* h_rebuild = nullptr;     // pinned
     unsigned* flags = nullptr;
@@ -867,8 +886,10 @@ int alloc_list(GcFused* f, int cap) {
         return GC_OK;
     }
     if (f->nbr) cudaFree(f->nbr);
-    f->nbr = nullptr;
+    if (f->clist) cudaFree(f->clist);
+    f->nbr = f->clist = nullptr;
     GC_CUDA(cudaMalloc(&f->nbr, need * sizeof(int)), "fused: neighbour lists");
+    if (f->compact) GC_CUDA(cudaMalloc(&f->clist, need * sizeof(int)), "fused: compact lists");
     f->nbr_elems = need;
     f->cap = cap;
     return GC_OK;
@@ -948,7 +969,8 @@ int one_step(GcFused* f, int drive) {
     GC_CUDA(cudaStreamSynchronize(st), "fused: flag");
     if (*f->h_rebuild) GC_TRY(rebuild_lists(f));
     prof_mark(f);
-    fk_density<<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->nbr, f->cnt, f->cap);
+    fk_density<<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->nbr, f->cnt, f->cap,
+                                       f->compact ? f->clist : nullptr, f->compact ? f->ccnt : nullptr);
     GC_CHECK_LAUNCH("fused: density");
     prof_mark(f);
     if (f->ncell > 0) {
@@ -977,8 +999,12 @@ int one_step(GcFused* f, int drive) {
         }
     }
     prof_mark(f);
-    fk_force<<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel, f->nbr,
-                                     f->cnt, f->cap, f->ncell > 0 ? f->mforce : nullptr, drive);
+    if (f->compact)
+        fk_force<true><<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
+                                               f->clist, f->ccnt, f->cap, f->ncell > 0 ? f->mforce : nullptr, drive);
+    else
+        fk_force<false><<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
+                                                f->nbr, f->cnt, f->cap, f->ncell > 0 ? f->mforce : nullptr, drive);
     GC_CHECK_LAUNCH("fused: force");
     prof_mark(f);
     if (p.nF > p.nB2) {
@@ -1010,6 +1036,7 @@ int gc_fused_create(const Structconst* consts, const float* bbox6, int periodic_
     }
     f->noise_on = noise_on ? 1 : 0;
     if (opt) {
+        f->compact = opt->compact != 0;
         if (opt->skin > 0.f) f->skin = opt->skin;
         if (opt->block == 64 || opt->block == 128 || opt->block == 256 || opt->block == 512) f->block = opt->block;
     }
@@ -1040,6 +1067,7 @@ int gc_fused_create(const Structconst* consts, const float* bbox6, int periodic_
     if (ok == GC_OK) ok = falloc(f, &f->keys, n);
     if (ok == GC_OK) ok = falloc(f, &f->vals, n);
     if (ok == GC_OK) ok = falloc(f, &f->cnt, n);
+    if (ok == GC_OK) ok = falloc(f, &f->ccnt, n);
     if (ok == GC_OK) ok = falloc(f, &f->rebuild, 1);
     if (ok == GC_OK) ok = falloc(f, &f->flags, 1);
     if (ok == GC_OK) ok = falloc(f, &f->stat_sum, 1);
@@ -1195,7 +1223,8 @@ int gc_fused_setup(GcFused* f) {
     // density and pressure of the loaded state (the reference has them from
     // DenInit until the first step recomputes them)
     fk_density<<<gc_blocks(f->n, f->block), f->block, 0, st>>>(f->n, p, make_box(f->lgrid), f->a.pos, f->a.vpred,
-                                                               f->a.vh, f->dp, f->nbr, f->cnt, f->cap);
+                                                               f->a.vh, f->dp, f->nbr, f->cnt, f->cap, nullptr,
+                                                               nullptr);
     GC_CHECK_LAUNCH("fused: set-up density");
     f->setup_done = true;
     f->step = -1;
@@ -1349,6 +1378,7 @@ int gc_fused_destroy(GcFused* f) {
     for (cudaEvent_t e : f->ev) cudaEventDestroy(e);
     for (void* q : f->allocs) cudaFree(q);
     if (f->nbr) cudaFree(f->nbr);
+    if (f->clist) cudaFree(f->clist);
     if (f->stage) cudaFree(f->stage);
     if (f->h_rebuild) cudaFreeHost(f->h_rebuild);
     delete f;

@@ -211,23 +211,34 @@ __host__ __device__ __forceinline__ Philox2 philox2x32_10(uint32_t c0, uint32_t 
 }
 
 // Three uniform variates with zero mean and unit variance from the 63 low
-// bits of the two words, 21 bits each: sqrt(12) (u + 1/2) / 2^21 - sqrt(3).
+// bits of the two words, 21 bits u each: sqrt(12) ((u + 1/2) / 2^21 - 1/2).
 // Groot & Warren (1997) drive the same integrator with uniform noise; only
-// the first two moments enter the fluctuation-dissipation balance.
+// the first two moments enter the fluctuation-dissipation balance.  On the
+// device the 21 bits become the mantissa of a float in [1, 2), v = 1 + u/2^21,
+// and the variate is sqrt(12) v - sqrt(12) (3/2 - 2^-22): no int-to-float
+// conversion.
 __device__ __forceinline__ float unit_uniform21(uint32_t u) {
-    return fmaf((float)u + 0.5f, 3.4641016151377544f / 2097152.f, -1.7320508075688772f);
+    float v = __uint_as_float(0x3F800000u | (u << 2));
+    return fmaf(v, 3.4641016151377544f, -3.4641016151377544f * (1.5f - 2.384185791015625e-7f));
 }
 
-// The noise components xi_ij for the pair (i, j); xi_ji = -xi_ij.
-__device__ __forceinline__ float3 pair_noise(unsigned id_i, unsigned id_j, const GcParams& p) {
+// The noise components xi_ij for the pair (i, j) without the sign of the
+// pair: xi_ij = pair_sign(i, j) * pair_noise_unsigned(i, j).
+__device__ __forceinline__ float3 pair_noise_unsigned(unsigned id_i, unsigned id_j, const GcParams& p) {
     unsigned a = id_i < id_j ? id_i : id_j;
     unsigned b = id_i < id_j ? id_j : id_i;
     Philox2 w = philox2x32_10(a, b, p.noise_key);
     uint32_t u0 = w.w0 & 0x1FFFFFu;
     uint32_t u1 = (w.w0 >> 21) | ((w.w1 & 0x3FFu) << 11);
     uint32_t u2 = (w.w1 >> 10) & 0x1FFFFFu;
-    float s = id_i < id_j ? 1.f : -1.f;
-    return f3(s * unit_uniform21(u0), s * unit_uniform21(u1), s * unit_uniform21(u2));
+    return f3(unit_uniform21(u0), unit_uniform21(u1), unit_uniform21(u2));
+}
+
+__device__ __forceinline__ float pair_sign(unsigned id_i, unsigned id_j) { return id_i < id_j ? 1.f : -1.f; }
+
+// The noise components xi_ij for the pair (i, j); xi_ji = -xi_ij.
+__device__ __forceinline__ float3 pair_noise(unsigned id_i, unsigned id_j, const GcParams& p) {
+    return pair_sign(id_i, id_j) * pair_noise_unsigned(id_i, id_j, p);
 }
 
 // ---------------------------------------------------------------------------

@@ -23,12 +23,12 @@ def _ptr(a):
 
 
 class FusedSystem:
-    def __init__(self, cfg: Config, noise=True, skin=0.1, block=128, list_capacity=0):
+    def __init__(self, cfg: Config, noise=True, skin=0.1, block=128, list_capacity=0, compact=True):
         self.cfg = cfg
         self.lib = _lib.load()
         self.h = C.c_void_p()
         consts = _lib.Structconst(**cfg.consts())
-        opt = _lib.GcFusedOptions(skin=skin, block=block, list_capacity=list_capacity)
+        opt = _lib.GcFusedOptions(skin=skin, block=block, list_capacity=list_capacity, compact=1 if compact else 0)
         bbox = np.ascontiguousarray(cfg.bbox, np.float32)
         _lib.call("gc_fused_create", C.byref(consts), _ptr(bbox), cfg.pmask, 1 if noise else 0, C.byref(opt),
                   C.byref(self.h))

@@ -152,7 +152,8 @@ typedef struct {
     float skin;           /* Verlet skin in units of CutRadius (0: 0.1) */
     int block;            /* threads per block of the particle kernels: 64, 128, 256 or 512 (0: 128) */
     int list_capacity;    /* initial neighbour-list capacity per particle (0: from the density) */
-    int reserved[5];
+    int compact;          /* 1: the density pass writes the pairs that act this step for the force pass */
+    int reserved[4];
 } GcFusedOptions;
 /* bbox6 (host) as src/main.cuh:12; periodic_mask as gc_set_periodic. */
 int gc_fused_create(const Structconst* consts, const float* bbox6, int periodic_mask, int noise_on,

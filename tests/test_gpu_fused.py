@@ -29,10 +29,11 @@ def _close_rel(got, want, tol):
     assert err <= tol * scale, f"max err {err:g} vs scale {scale:g}"
 
 
-def test_fused_tracks_oracle_noise_off(cuda_device):
+@pytest.mark.parametrize("compact", [True, False])
+def test_fused_tracks_oracle_noise_off(cuda_device, compact):
     from gpucell_gb300.fused import FusedSystem
     cfg = gen.small_channel()
-    fs = FusedSystem(cfg, noise=False)
+    fs = FusedSystem(cfg, noise=False, compact=compact)
     o = _oracle(cfg, False)
     for _ in range(3):
         fs.step(1, 1)
@@ -46,12 +47,13 @@ def test_fused_tracks_oracle_noise_off(cuda_device):
     assert fs.flags() == 0
 
 
-def test_fused_matches_boundary_path_with_noise(cuda_device):
+@pytest.mark.parametrize("compact", [True, False])
+def test_fused_matches_boundary_path_with_noise(cuda_device, compact):
     from gpucell_gb300.fused import FusedSystem
     from gpucell_gb300.host import ParticleSystem
     cfg = gen.small_channel()
     ps = ParticleSystem(cfg, noise=True)
-    fs = FusedSystem(cfg, noise=True)
+    fs = FusedSystem(cfg, noise=True, compact=compact)
     for _ in range(2):
         ps.update()
         fs.step(1, 1)
