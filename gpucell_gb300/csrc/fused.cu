@@ -168,7 +168,7 @@ __global__ void fk_permute(int n, GcGrid g, const int* __restrict__ perm, SlotAr
 // permutation wraps them), so each neighbouring row of cubes has one image
 // shift, and the three cubes of a row that do not wrap are one contiguous
 // range of slots.
-__global__ void __launch_bounds__(kBS) fk_build_list(int n, GcParams p, const float4* __restrict__ pos,
+__global__ void fk_build_list(int n, GcParams p, const float4* __restrict__ pos,
                                                      const unsigned* __restrict__ start, int* __restrict__ nbr,
                                                      int* __restrict__ cnt, int cap, float cut2, unsigned* flags) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(kBS) fk_build_list(int n, GcParams p, const fl
 // act this step (SDPD partners within rc, Bound1 walls within the repulsion
 // range) to a second list in the same layout, so the force pass iterates
 // only interacting pairs.
-__global__ void __launch_bounds__(kBS) fk_density(int n, GcParams p, Box B, const float4* __restrict__ pos,
+__global__ void fk_density(int n, GcParams p, Box B, const float4* __restrict__ pos,
                                                   float4* __restrict__ vpred, const float4* __restrict__ vh,
                                                   float2* __restrict__ dp, const int* __restrict__ nbr,
                                                   const int* __restrict__ cnt, int cap, int* __restrict__ clist,
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(kBS) fk_density(int n, GcParams p, Box B, cons
 // COMPACT: the list holds only pairs that act this step (written by
 // fk_density), so the cut-off test is already done.
 template <bool COMPACT>
-__global__ void __launch_bounds__(kBS) fk_force(int n, GcParams p, Box B, const float4* __restrict__ pos,
+__global__ void fk_force(int n, GcParams p, Box B, const float4* __restrict__ pos,
                                                 const float4* __restrict__ vpred, const float4* __restrict__ vh,
                                                 const float2* __restrict__ dp, float4* __restrict__ force,
                                                 float4* __restrict__ vel, const int* __restrict__ nbr,
