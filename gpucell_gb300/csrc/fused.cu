@@ -31,7 +31,8 @@
 
 namespace {
 
-constexpr int kBS = 128;
+constexpr int kBS = 128;      // default threads per block
+constexpr int kMaxBS = 256;   // largest block the particle kernels accept
 
 __device__ __forceinline__ unsigned fid(float4 x) { return __float_as_uint(x.w); }
 __device__ __forceinline__ float3 xyz(float4 a) { return f3(a.x, a.y, a.z); }
@@ -168,7 +169,7 @@ __global__ void fk_permute(int n, GcGrid g, const int* __restrict__ perm, SlotAr
 // permutation wraps them), so each neighbouring row of cubes has one image
 // shift, and the three cubes of a row that do not wrap are one contiguous
 // range of slots.
-__global__ void fk_build_list(int n, GcParams p, const float4* __restrict__ pos,
+__global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, GcParams p, const float4* __restrict__ pos,
                                                      const unsigned* __restrict__ start, int* __restrict__ nbr,
                                                      int* __restrict__ cnt, int cap, float cut2, unsigned* flags) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -231,7 +232,7 @@ __global__ void fk_build_list(int n, GcParams p, const float4* __restrict__ pos,
 // act this step (SDPD partners within rc, Bound1 walls within the repulsion
 // range) to a second list in the same layout, so the force pass iterates
 // only interacting pairs.
-__global__ void fk_density(int n, GcParams p, Box B, const float4* __restrict__ pos,
+__global__ void __launch_bounds__(kMaxBS) fk_density(int n, GcParams p, Box B, const float4* __restrict__ pos,
                                                   float4* __restrict__ vpred, const float4* __restrict__ vh,
                                                   float2* __restrict__ dp, const int* __restrict__ nbr,
                                                   const int* __restrict__ cnt, int cap, int* __restrict__ clist,
@@ -299,7 +300,7 @@ __global__ void fk_density(int n, GcParams p, Box B, const float4* __restrict__ 
 // COMPACT: the list holds only pairs that act this step (written by
 // fk_density), so the cut-off test is already done.
 template <bool COMPACT>
-__global__ void fk_force(int n, GcParams p, Box B, const float4* __restrict__ pos,
+__global__ void __launch_bounds__(kMaxBS) fk_force(int n, GcParams p, Box B, const float4* __restrict__ pos,
                                                 const float4* __restrict__ vpred, const float4* __restrict__ vh,
                                                 const float2* __restrict__ dp, float4* __restrict__ force,
                                                 float4* __restrict__ vel, const int* __restrict__ nbr,
@@ -1038,7 +1039,7 @@ int gc_fused_create(const Structconst* consts, const float* bbox6, int periodic_
     if (opt) {
         f->compact = opt->compact != 0;
         if (opt->skin > 0.f) f->skin = opt->skin;
-        if (opt->block == 64 || opt->block == 128 || opt->block == 256 || opt->block == 512) f->block = opt->block;
+        if (opt->block == 64 || opt->block == 128 || opt->block == kMaxBS) f->block = opt->block;
     }
     int e = gc_build_grid(bbox6, c.CutRadius + f->skin, periodic_mask, &f->lgrid);
     GcGrid g0;

@@ -150,7 +150,7 @@ int gc_cudiv_Printf(int n, int* d_curpos, int* d_sortpart, float* d_totalcoor);
 typedef struct GcFused GcFused;
 typedef struct {
     float skin;           /* Verlet skin in units of CutRadius (0: 0.1) */
-    int block;            /* threads per block of the particle kernels: 64, 128, 256 or 512 (0: 128) */
+    int block;            /* threads per block of the particle kernels: 64, 128 or 256 (0: 128) */
     int list_capacity;    /* initial neighbour-list capacity per particle (0: from the density) */
     int compact;          /* 1: the density pass writes the pairs that act this step for the force pass */
     int reserved[4];
