@@ -91,6 +91,7 @@ _SIGS = {
     "gc_cupar_CalCellAggForce": [_U, _U, _U] + [_P] * 10,
     "gc_cudiv_PreConList": [_I, _I] + [_P] * 8,
     "gc_cudiv_Sort": [_I, _P, _P],
+    "gc_cudiv_Sort_noalloc": [_I, _P, _P],
     "gc_cudiv_CalBeginEndCube": [_I, _I, _P, _P],
     "gc_cudiv_SortBasicArrays": [_I] + [_P] * 8,
     "gc_cudiv_SortArraysWithCells": [_I] + [_P] * 10,

@@ -19,6 +19,8 @@
 
 #include <stdio.h>
 
+#include <mutex>
+
 namespace {
 
 constexpr int kBS = 256;
@@ -409,3 +411,107 @@ int gc_cudiv_Printf(int n, int* d_curpos, int* d_sortpart, float* d_totalcoor) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// The stable sort of cudiv::Sort without any device allocation.
+//
+// gc_cudiv_Sort grows library scratch with cudaMalloc (and may cudaFree a
+// smaller buffer first, which synchronises the device).  Some callers cannot
+// allow that: a host program that reserves the device memory it will use up
+// front and must not see a library take more, a process sharing a GPU under
+// a fixed memory cap, or a loop that must not stall on the implicit device
+// synchronisation of cudaFree.  gc_cudiv_Sort_noalloc runs the same kernels
+// with their temporaries in the fixed array below instead.
+//
+// The array is a file-scope __device__ variable: every GPU that loads the
+// library holds it (about 5.2 MB) until the process exits.  In host code its
+// name is only a stand-in for the symbol, not a device address, so its
+// device address is looked up once per device with cudaGetSymbolAddress and
+// passed to the kernels.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNaAlign = 256;
+constexpr size_t na_round(size_t b) { return (b + kNaAlign - 1) / kNaAlign * kNaAlign; }
+constexpr size_t kNaCount = na_round(((size_t)GC_NOALLOC_SORT_MAX_KEYS + 1) * sizeof(unsigned));
+constexpr size_t kNaArray = na_round((size_t)GC_NOALLOC_SORT_MAX_N * sizeof(int));
+constexpr size_t kNaBlocks = na_round(((size_t)GC_NOALLOC_SORT_MAX_KEYS / kScanTile + 2) * sizeof(unsigned));
+constexpr size_t kNaMaxKey = na_round(sizeof(int));
+// counts | rank | keys | values | input positions | scan block sums | max key
+constexpr size_t kNaBytes = kNaCount + 4 * kNaArray + kNaBlocks + kNaMaxKey;
+
+static __device__ __align__(256) unsigned char g_noalloc_sort_scratch[kNaBytes];
+
+constexpr int kNaMaxDevices = 64;
+unsigned char* g_na_base[kNaMaxDevices] = {};
+std::mutex g_na_mutex;
+
+// Device address of the scratch array on the current device (looked up on
+// the first call per device).
+int noalloc_base(unsigned char** out) {
+    int dev = 0;
+    GC_CUDA(cudaGetDevice(&dev), "Sort_noalloc: current device");
+    if (dev < 0 || dev >= kNaMaxDevices) return gc_fail(GC_EINVAL, "Sort_noalloc: device %d is out of range", dev);
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    if (!g_na_base[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_sort_scratch);
+        if (e != cudaSuccess) return gc_cuda_fail(e, "Sort_noalloc: scratch address");
+        g_na_base[dev] = (unsigned char*)p;
+    }
+    *out = g_na_base[dev];
+    return GC_OK;
+}
+
+}  // namespace
+
+extern "C" int gc_cudiv_Sort_noalloc(int n, int* keys, int* values) {
+    if (n < 0) return gc_fail(GC_EINVAL, "Sort_noalloc: n < 0");
+    if (n == 0) return GC_OK;
+    if (n > GC_NOALLOC_SORT_MAX_N)
+        return gc_fail(GC_EINVAL, "Sort_noalloc: n = %d exceeds the fixed scratch (at most %d elements)", n,
+                       GC_NOALLOC_SORT_MAX_N);
+    if (!keys || !values) return gc_fail(GC_EINVAL, "Sort_noalloc: NULL array");
+    GcState& s = gc_state();
+    cudaStream_t st = s.stream;
+    unsigned char* base = nullptr;
+    GC_TRY(noalloc_base(&base));
+    unsigned* cnt = (unsigned*)base;
+    unsigned* rank = (unsigned*)(base + kNaCount);
+    int* tkey = (int*)(base + kNaCount + kNaArray);
+    int* tval = (int*)(base + kNaCount + 2 * kNaArray);
+    int* tsrc = (int*)(base + kNaCount + 3 * kNaArray);
+    unsigned* bsum = (unsigned*)(base + kNaCount + 4 * kNaArray);
+    int* maxkey = (int*)(base + kNaCount + 4 * kNaArray + kNaBlocks);
+    int K;
+    if (s.grid_set) {
+        K = s.grid.ncells;
+    } else {
+        GC_CUDA(cudaMemsetAsync(maxkey, 0, sizeof(int), st), "Sort_noalloc: max key");
+        k_maxkey<<<gc_blocks(n, kBS), kBS, 0, st>>>(n, keys, maxkey);
+        GC_CHECK_LAUNCH("Sort_noalloc: max key");
+        int h = 0;
+        GC_CUDA(cudaMemcpyAsync(&h, maxkey, sizeof(int), cudaMemcpyDeviceToHost, st), "Sort_noalloc: max key");
+        GC_CUDA(cudaStreamSynchronize(st), "Sort_noalloc: max key");
+        K = h + 1;
+    }
+    if (K > GC_NOALLOC_SORT_MAX_KEYS)
+        return gc_fail(GC_EINVAL, "Sort_noalloc: %d keys exceed the fixed scratch (at most %d)", K,
+                       GC_NOALLOC_SORT_MAX_KEYS);
+    // the counts must start at zero; every other region is fully written
+    GC_CUDA(cudaMemsetAsync(cnt, 0, (size_t)(K + 1) * sizeof(unsigned), st), "Sort_noalloc: clear counts");
+    k_sort_count<<<gc_blocks(n, kBS), kBS, 0, st>>>(n, K, keys, cnt, rank, nullptr);
+    GC_CHECK_LAUNCH("Sort_noalloc: count");
+    int nb = (K + kScanTile - 1) / kScanTile;
+    k_scan_tiles<<<nb, kScanBS, 0, st>>>(K, cnt, cnt, bsum);
+    GC_CHECK_LAUNCH("Sort_noalloc: scan tiles");
+    k_scan_bsums<<<1, kScanBS, 0, st>>>(nb, bsum, cnt + K);
+    GC_CHECK_LAUNCH("Sort_noalloc: scan block sums");
+    k_scan_add<<<gc_blocks(K, kBS), kBS, 0, st>>>(K, cnt, bsum);
+    GC_CHECK_LAUNCH("Sort_noalloc: scan add");
+    k_sort_scatter<<<gc_blocks(n, kBS), kBS, 0, st>>>(n, K, keys, values, cnt, rank, tkey, tval, tsrc);
+    GC_CHECK_LAUNCH("Sort_noalloc: scatter");
+    k_sort_fix<<<gc_blocks((long long)K * 32, kBS), kBS, 0, st>>>(K, cnt, tkey, tval, tsrc, keys, values);
+    GC_CHECK_LAUNCH("Sort_noalloc: fix");
+    return GC_OK;
+}

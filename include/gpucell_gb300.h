@@ -126,6 +126,22 @@ int gc_cudiv_PreConList(int n, int cutradius, float* d_totalcoor, float* d_bboxs
  * the latest PreConList; without one, K is found on the device (one
  * synchronous 4-byte copy). */
 int gc_cudiv_Sort(int n, int* keys, int* values);
+/* No counterpart in the reference: the sort of gc_cudiv_Sort (same stable
+ * order, same key rule) for callers that cannot let the library allocate
+ * device memory -- a host program that reserves the device memory it will
+ * use up front, a process sharing the GPU under a fixed memory cap, or a loop
+ * that must not stall on the device synchronisation of cudaFree.  Its
+ * temporaries live in one fixed array of about 5.2 MB that every GPU loading
+ * the library holds until the process exits; it calls no cudaMalloc or
+ * cudaFree.  Limits: n <= GC_NOALLOC_SORT_MAX_N elements and keys in
+ * [0, GC_NOALLOC_SORT_MAX_KEYS); larger inputs return GC_EINVAL.  The first
+ * call on each device looks up the array's device address (do that call
+ * before any stream capture).  All calls share the array: calls that may
+ * overlap on the GPU (different streams, or different host threads) race and
+ * must be serialised by the caller. */
+#define GC_NOALLOC_SORT_MAX_N    262144
+#define GC_NOALLOC_SORT_MAX_KEYS 262144
+int gc_cudiv_Sort_noalloc(int n, int* keys, int* values);
 /* src/ConfigDomain.cuh:13, src/Particle.cu:672 */
 int gc_cudiv_CalBeginEndCube(int n, int sizecube, int* d_cubepart, int* d_beginendcube);
 /* src/ConfigDomain.cuh:14, src/Particle.cu:677 */
