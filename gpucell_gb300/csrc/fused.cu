@@ -228,15 +228,21 @@ __global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, GcParams p, const
 // ---------------------------------------------------------------------------
 // K8 + K11 (+ K10 for Bound2 slots)
 // ---------------------------------------------------------------------------
-// With `clist` set, fluid and membrane slots also write the entries that
-// act this step (SDPD partners within rc, Bound1 walls within the repulsion
-// range) to a second list in the same layout, so the force pass iterates
-// only interacting pairs.
+// With `cmask` set, fluid and membrane slots also record which of their list
+// entries act this step (SDPD partners within rc, Bound1 walls within the
+// repulsion range): one bit per entry, 32 entries per word, words of 32 slots
+// interleaved like the lists (word w of slot i at ((i/32)*mw + w)*32 + i%32),
+// and the number of set bits in ccnt.  The force pass then iterates only the
+// set bits, so no lane idles on an entry that does not act.
+__device__ __forceinline__ size_t mrow(int i, int w, int mw) {
+    return ((size_t)(i >> 5) * mw + w) * 32 + (i & 31);
+}
+
 __global__ void __launch_bounds__(kMaxBS) fk_density(int n, GcParams p, Box B, const float4* __restrict__ pos,
                                                   float4* __restrict__ vpred, const float4* __restrict__ vh,
                                                   float2* __restrict__ dp, const int* __restrict__ nbr,
-                                                  const int* __restrict__ cnt, int cap, int* __restrict__ clist,
-                                                  int* __restrict__ ccnt) {
+                                                  const int* __restrict__ cnt, int cap, unsigned* __restrict__ cmask,
+                                                  int mw, int* __restrict__ ccnt) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 xi4 = pos[i];
@@ -248,23 +254,29 @@ __global__ void __launch_bounds__(kMaxBS) fk_density(int n, GcParams p, Box B, c
     if (t == PT_FLUID || t == PT_MEMB) {
         float sum = p.w0;
         int kc = 0;
+        unsigned m = 0;
         int jn = c > 0 ? __ldg(lp) : 0;
         float4 xn = pos[jn];
         for (int k = 0; k < c; ++k) {
-            int j = jn;
             float4 xj = xn;
             if (k + 1 < c) {
                 jn = __ldg(lp + (size_t)(k + 1) * 32);
                 xn = pos[jn];
             }
             float r2 = norm2_rn(pair_image(xi, xyz(xj), B));
-            if (r2 >= p.rc2) continue;
-            if (is_sdpd(fid(xj), p)) {
-                float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
-                sum += wendland_w(r, p);
-                if (clist && r2 > 0.f) clist[sell(i, kc++, cap)] = j;
-            } else if (clist && r2 < p.rep_r0sq && r2 > 0.f) {
-                clist[sell(i, kc++, cap)] = j;
+            if (r2 < p.rc2) {
+                if (is_sdpd(fid(xj), p)) {
+                    float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+                    sum += wendland_w(r, p);
+                    if (r2 > 0.f) m |= 1u << (k & 31);
+                } else if (r2 < p.rep_r0sq && r2 > 0.f) {
+                    m |= 1u << (k & 31);
+                }
+            }
+            if (cmask && ((k & 31) == 31 || k + 1 == c)) {
+                cmask[mrow(i, k >> 5, mw)] = m;
+                kc += __popc(m);
+                m = 0;
             }
         }
         if (ccnt) ccnt[i] = kc;
@@ -297,14 +309,15 @@ __global__ void __launch_bounds__(kMaxBS) fk_density(int n, GcParams p, Box B, c
 // ---------------------------------------------------------------------------
 // K12 + K13 + K14 + membrane forces + K19
 // ---------------------------------------------------------------------------
-// COMPACT: the list holds only pairs that act this step (written by
-// fk_density), so the cut-off test is already done.
+// COMPACT: iterate only the entries fk_density marked as acting this step,
+// so the cut-off test is already done.
 template <bool COMPACT>
 __global__ void __launch_bounds__(kMaxBS) fk_force(int n, GcParams p, Box B, const float4* __restrict__ pos,
                                                 const float4* __restrict__ vpred, const float4* __restrict__ vh,
                                                 const float2* __restrict__ dp, float4* __restrict__ force,
                                                 float4* __restrict__ vel, const int* __restrict__ nbr,
                                                 const int* __restrict__ cnt, int cap,
+                                                const unsigned* __restrict__ cmask, int mw,
                                                 const float4* __restrict__ mforce, int drive) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -321,13 +334,34 @@ __global__ void __launch_bounds__(kMaxBS) fk_force(int n, GcParams p, Box B, con
     float3 f = f3(0.f, 0.f, 0.f);
     int c = cnt[i];
     const int* lp = nbr + sell(i, 0, cap);
-    int jn = c > 0 ? __ldg(lp) : 0;
-    float4 xn = pos[jn];
+    const unsigned* mp = COMPACT ? cmask + mrow(i, 0, mw) : nullptr;
+    unsigned m = 0;
+    int base = -32;
+    // index of the next acting entry (COMPACT) or of the next entry
+    auto next_k = [&](int k) -> int {
+        if constexpr (COMPACT) {
+            while (m == 0) {
+                base += 32;
+                m = __ldg(mp + (size_t)(base >> 5) * 32);
+            }
+            int b = __ffs(m) - 1;
+            m &= m - 1;
+            return base + b;
+        } else {
+            return k;
+        }
+    };
+    int jn = 0;
+    float4 xn;
+    if (c > 0) {
+        jn = __ldg(lp + (size_t)next_k(0) * 32);
+        xn = pos[jn];
+    }
     for (int k = 0; k < c; ++k) {
         int j = jn;
         float4 xj4 = xn;
         if (k + 1 < c) {   // prefetch the next entry while this one is computed
-            jn = __ldg(lp + (size_t)(k + 1) * 32);
+            jn = __ldg(lp + (size_t)next_k(k + 1) * 32);
             xn = pos[jn];
         }
         float3 d = pair_image(xi, xyz(xj4), B);
@@ -823,7 +857,9 @@ struct GcFused {
     int *nbr = nullptr, *cnt = nullptr;
     size_t nbr_elems = 0;
     bool compact = false;
-    int *clist = nullptr, *ccnt = nullptr;   // per-step list of interacting pairs (same layout and capacity)
+    unsigned* cmask = nullptr;   // per-step bit mask of the acting list entries
+    int* ccnt = nullptr;         // number of acting entries
+    int mw = 0;                  // mask words per slot
     int* rebuild = nullptr;
     int* h_rebuild = nullptr;     // pinned
     unsigned* flags = nullptr;
@@ -887,10 +923,13 @@ int alloc_list(GcFused* f, int cap) {
         return GC_OK;
     }
     if (f->nbr) cudaFree(f->nbr);
-    if (f->clist) cudaFree(f->clist);
-    f->nbr = f->clist = nullptr;
+    if (f->cmask) cudaFree(f->cmask);
+    f->nbr = nullptr;
+    f->cmask = nullptr;
     GC_CUDA(cudaMalloc(&f->nbr, need * sizeof(int)), "fused: neighbour lists");
-    if (f->compact) GC_CUDA(cudaMalloc(&f->clist, need * sizeof(int)), "fused: compact lists");
+    f->mw = (cap + 31) / 32;
+    if (f->compact)
+        GC_CUDA(cudaMalloc(&f->cmask, (size_t)((f->n + 31) / 32) * 32 * f->mw * sizeof(unsigned)), "fused: masks");
     f->nbr_elems = need;
     f->cap = cap;
     return GC_OK;
@@ -971,7 +1010,7 @@ int one_step(GcFused* f, int drive) {
     if (*f->h_rebuild) GC_TRY(rebuild_lists(f));
     prof_mark(f);
     fk_density<<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->nbr, f->cnt, f->cap,
-                                       f->compact ? f->clist : nullptr, f->compact ? f->ccnt : nullptr);
+                                       f->compact ? f->cmask : nullptr, f->mw, f->compact ? f->ccnt : nullptr);
     GC_CHECK_LAUNCH("fused: density");
     prof_mark(f);
     if (f->ncell > 0) {
@@ -1002,10 +1041,12 @@ int one_step(GcFused* f, int drive) {
     prof_mark(f);
     if (f->compact)
         fk_force<true><<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
-                                               f->clist, f->ccnt, f->cap, f->ncell > 0 ? f->mforce : nullptr, drive);
+                                               f->nbr, f->ccnt, f->cap, f->cmask, f->mw,
+                                               f->ncell > 0 ? f->mforce : nullptr, drive);
     else
         fk_force<false><<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
-                                                f->nbr, f->cnt, f->cap, f->ncell > 0 ? f->mforce : nullptr, drive);
+                                                f->nbr, f->cnt, f->cap, nullptr, 0,
+                                                f->ncell > 0 ? f->mforce : nullptr, drive);
     GC_CHECK_LAUNCH("fused: force");
     prof_mark(f);
     if (p.nF > p.nB2) {
@@ -1224,7 +1265,7 @@ int gc_fused_setup(GcFused* f) {
     // density and pressure of the loaded state (the reference has them from
     // DenInit until the first step recomputes them)
     fk_density<<<gc_blocks(f->n, f->block), f->block, 0, st>>>(f->n, p, make_box(f->lgrid), f->a.pos, f->a.vpred,
-                                                               f->a.vh, f->dp, f->nbr, f->cnt, f->cap, nullptr,
+                                                               f->a.vh, f->dp, f->nbr, f->cnt, f->cap, nullptr, 0,
                                                                nullptr);
     GC_CHECK_LAUNCH("fused: set-up density");
     f->setup_done = true;
@@ -1379,7 +1420,7 @@ int gc_fused_destroy(GcFused* f) {
     for (cudaEvent_t e : f->ev) cudaEventDestroy(e);
     for (void* q : f->allocs) cudaFree(q);
     if (f->nbr) cudaFree(f->nbr);
-    if (f->clist) cudaFree(f->clist);
+    if (f->cmask) cudaFree(f->cmask);
     if (f->stage) cudaFree(f->stage);
     if (f->h_rebuild) cudaFreeHost(f->h_rebuild);
     delete f;

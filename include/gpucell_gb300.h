@@ -168,7 +168,8 @@ typedef struct {
     float skin;           /* Verlet skin in units of CutRadius (0: 0.1) */
     int block;            /* threads per block of the particle kernels: 64, 128 or 256 (0: 128) */
     int list_capacity;    /* initial neighbour-list capacity per particle (0: from the density) */
-    int compact;          /* 1: the density pass writes the pairs that act this step for the force pass */
+    int compact;          /* 1: the density pass marks the list entries that act this step, and the force
+                             pass iterates only those */
     int reserved[4];
 } GcFusedOptions;
 /* bbox6 (host) as src/main.cuh:12; periodic_mask as gc_set_periodic. */
