@@ -68,6 +68,8 @@ _SIGS = {
     "gc_set_periodic": [_I],
     "gc_get_periodic": [],
     "gc_set_noise": [_I],
+    "gc_set_engine": [_I],
+    "gc_get_engine": [],
     "gc_set_step": [C.c_longlong],
     "gc_get_step": [],
     "gc_set_stream": [_P],

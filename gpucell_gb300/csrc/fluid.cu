@@ -313,7 +313,17 @@ extern "C" {
 
 int gc_cupar_UpdateFluidCoor(int n, int* d_sortpart, float* d_totalforce, float* d_totalcoor, float* d_velrhop) {
     GcState& s0 = gc_state();
+    s0.ref.sortpart = d_sortpart;
+    s0.ref.force = d_totalforce;
+    s0.ref.coor = d_totalcoor;
+    s0.ref.velrhop = d_velrhop;
     s0.step += 1;   // first call of every step (src/Particle.cu:1312)
+    // With the fused engine, every step after the first is run whole at
+    // SetFluidExtForce (which carries DriveOn); the other calls of the step
+    // only record their buffers.
+    s0.in_fused_step = s0.engine_mode == 1 && s0.plain_steps >= 1;
+    if (s0.in_fused_step) return GC_OK;
+    s0.plain_steps += 1;
     GC_PRE("UpdateFluidCoor", false);
     k_update_coor<<<nb, SDPDSIZE, 0, s.stream>>>(n, p, d_sortpart, (const float3*)d_totalforce, (float3*)d_totalcoor,
                                                 (const float4*)d_velrhop, gc_flags_ptr());
@@ -322,6 +332,9 @@ int gc_cupar_UpdateFluidCoor(int n, int* d_sortpart, float* d_totalforce, float*
 }
 
 int gc_cupar_AppFluidPeriodicBC(int n, int* d_sortpart, float* d_totalcoor, int* d_nthrobound, float* d_bboxsdpd) {
+    gc_state().ref.nthro = d_nthrobound;
+    gc_state().ref.bbox = d_bboxsdpd;
+    if (gc_state().in_fused_step) return GC_OK;
     GC_PRE("AppFluidPeriodicBC", false);
     p.g.pmask = s.periodic_mask;
     k_periodic<<<nb, SDPDSIZE, 0, s.stream>>>(n, p, d_sortpart, (float3*)d_totalcoor, (int3*)d_nthrobound, d_bboxsdpd,
@@ -332,6 +345,7 @@ int gc_cupar_AppFluidPeriodicBC(int n, int* d_sortpart, float* d_totalcoor, int*
 
 int gc_cupar_CalFluidDen(int n, float* d_totalcoor, float* d_velrhop, int* d_cc, int* d_ncube, float* d_outerregion,
                          int* d_sortpart, int* d_beginendcube) {
+    if (gc_state().in_fused_step) return GC_OK;
     (void)d_ncube; (void)d_outerregion;
     GC_PRE("CalFluidDen", true);
     k_density<<<nb, SDPDSIZE, 0, s.stream>>>(n, p, (const float3*)d_totalcoor, (float4*)d_velrhop, (const int3*)d_cc,
@@ -341,6 +355,8 @@ int gc_cupar_CalFluidDen(int n, float* d_totalcoor, float* d_velrhop, int* d_cc,
 }
 
 int gc_cupar_PredictFluidVel(int n, int* d_sortpart, float* d_velrhop, float* d_velhalf, float* d_totalforce) {
+    gc_state().ref.velhalf = d_velhalf;
+    if (gc_state().in_fused_step) return GC_OK;
     GC_PRE("PredictFluidVel", false);
     s.velhalf_ptr = d_velhalf;
     k_predict<<<nb, SDPDSIZE, 0, s.stream>>>(n, p, d_sortpart, (float4*)d_velrhop, (float3*)d_velhalf,
@@ -351,6 +367,7 @@ int gc_cupar_PredictFluidVel(int n, int* d_sortpart, float* d_velrhop, float* d_
 
 int gc_cupar_CalBound2Vel(int n, float* d_totalcoor, float* d_velrhop, int* d_cc, int* d_ncube, float* d_outerregion,
                           int* d_sortpart, int* d_beginendcube) {
+    if (gc_state().in_fused_step) return GC_OK;
     (void)d_ncube; (void)d_outerregion;
     GC_PRE("CalBound2Vel", true);
     if (p.nF == p.nB2) return GC_OK;   // no Bound2 particles
@@ -368,6 +385,8 @@ int gc_cupar_CalBound2Vel(int n, float* d_totalcoor, float* d_velrhop, int* d_cc
 }
 
 int gc_cupar_EOS(int n, int* d_sortpart, float* d_velrhop, float* d_press) {
+    gc_state().ref.press = d_press;
+    if (gc_state().in_fused_step) return GC_OK;
     GC_PRE("EOS", false);
     k_eos<<<nb, SDPDSIZE, 0, s.stream>>>(n, p, d_sortpart, (const float4*)d_velrhop, d_press);
     GC_CHECK_LAUNCH("EOS");
@@ -377,6 +396,7 @@ int gc_cupar_EOS(int n, int* d_sortpart, float* d_velrhop, float* d_press) {
 int gc_cupar_CalFluidSDPDForce(int n, float* h_sdpdforce, float* d_totalcoor, float* d_velrhop, int* d_cc,
                                int* d_ncube, int* d_sortpart, float* d_outerregion, int* d_beginendcube,
                                float* d_totalforce, float* d_press) {
+    if (gc_state().in_fused_step) return GC_OK;
     (void)h_sdpdforce; (void)d_ncube; (void)d_outerregion;
     GC_PRE("CalFluidSDPDForce", true);
     k_sdpd<<<nb, SDPDSIZE, 0, s.stream>>>(n, p, (const float3*)d_totalcoor, (const float4*)d_velrhop,
@@ -388,6 +408,7 @@ int gc_cupar_CalFluidSDPDForce(int n, float* h_sdpdforce, float* d_totalcoor, fl
 
 int gc_cupar_CalFluidRepForce(int n, float* d_totalcoor, int* d_cc, int* d_ncube, int* d_sortpart,
                               float* d_outerregion, int* d_beginendcube, float* d_totalforce) {
+    if (gc_state().in_fused_step) return GC_OK;
     (void)d_ncube; (void)d_outerregion;
     GC_PRE("CalFluidRepForce", true);
     if (p.nB2 == 0) return GC_OK;   // no Bound1 particles
@@ -398,6 +419,7 @@ int gc_cupar_CalFluidRepForce(int n, float* d_totalcoor, int* d_cc, int* d_ncube
 }
 
 int gc_cupar_SetFluidExtForce(int driveon, int n, int* d_sortpart, float* d_totalforce) {
+    if (gc_state().in_fused_step) return gc_engine_step(driveon);
     GC_PRE("SetFluidExtForce", false);
     if (!driveon || p.gx == 0.f) return GC_OK;
     k_ext<<<nb, SDPDSIZE, 0, s.stream>>>(n, p, d_sortpart, (float3*)d_totalforce);
@@ -407,6 +429,8 @@ int gc_cupar_SetFluidExtForce(int driveon, int n, int* d_sortpart, float* d_tota
 
 int gc_cupar_CorrectFliudVel(int n, int* d_sortpart, float* d_totalforce, float* d_velhalf, float* d_velrhop,
                              float* d_totalcoor, int* d_cc, int* d_ncube, float* d_outerregion, int* d_beginendcube) {
+    gc_state().ref.velhalf = d_velhalf;
+    if (gc_state().in_fused_step) return GC_OK;
     (void)d_totalcoor; (void)d_cc; (void)d_ncube; (void)d_outerregion; (void)d_beginendcube;
     GC_PRE("CorrectFliudVel", false);
     s.velhalf_ptr = d_velhalf;

@@ -267,6 +267,26 @@ enum GcScratchSlot {
     SCR_COUNT_
 };
 
+// Caller buffers seen by the boundary entry points (device pointers), kept so
+// that the fused engine can run GPUCell's step on them (GPUCELL_ENGINE=fused).
+struct GcRefPtrs {
+    int *sortpart = nullptr, *curpos = nullptr;
+    float *coor = nullptr, *velrhop = nullptr, *velhalf = nullptr, *force = nullptr, *press = nullptr;
+    int* nthro = nullptr;
+    const float* bbox = nullptr;
+    // membranes
+    int ncell = 0, ntri = 0, nedge = 0;
+    int *tri = nullptr, *betri = nullptr, *edge = nullptr, *celltab = nullptr;
+    float *shearmod = nullptr, *bendmod = nullptr, *hlarea = nullptr, *hgarea = nullptr, *hvol = nullptr;
+    float *refedgelen = nullptr, *maxrefedgelen = nullptr, *perlen = nullptr, *hpow = nullptr, *hbending = nullptr,
+          *reftriangle = nullptr;
+    float *trinordir = nullptr, *triarea = nullptr, *reftriarea = nullptr, *tricenter = nullptr;
+    float *refarea_para = nullptr, *refvol_para = nullptr, *area_para = nullptr, *vol_para = nullptr;
+    float *area = nullptr, *vol = nullptr, *pararea = nullptr, *defforce = nullptr, *aggforce = nullptr;
+};
+
+struct GcFused;
+
 struct GcState {
     Structconst c;
     bool consts_set = false;
@@ -275,6 +295,12 @@ struct GcState {
     long long step = -1;           // last step index seen by UpdateFluidCoor
     cudaStream_t stream = 0;
     float* velhalf_ptr = nullptr;  // caller's VelHalf, for the wall velocity
+    // GPUCELL_ENGINE=fused: GPUCell's call sequence drives the fused step
+    int engine_mode = 0;           // 0: one kernel per entry point; 1: fused step
+    GcFused* engine = nullptr;
+    long long plain_steps = 0;     // steps run on the entry-point kernels since ConstsDataUp
+    bool in_fused_step = false;    // between UpdateFluidCoor and the end of a fused step
+    GcRefPtrs ref;
     // grid cache
     bool grid_set = false;
     const float* grid_bbox_ptr = nullptr;
@@ -295,6 +321,11 @@ int gc_cuda_fail(cudaError_t e, const char* what);
 // (with the error text set).
 void* gc_scratch(int slot, size_t bytes);
 unsigned* gc_flags_ptr();
+// Fused engine behind the entry points (fused.cu).  gc_engine_step runs one
+// fused step on the recorded caller buffers and writes the caller-visible
+// state back; gc_engine_reset drops the engine.
+int gc_engine_step(int drive_on);
+void gc_engine_reset();
 // Parameter block for the given constants (no grid, step 0).
 int gc_params_from(const Structconst& c, int noise_on, GcParams* p);
 // Parameter block for the current constants, grid and step.

@@ -368,6 +368,15 @@ int gc_cupar_CalGeoPara(long stepcount, int ntri, int ncell, float* d_bbox, int*
                         float* d_triarea, float* d_reftriarea, float* d_tricenter, float* d_refarea_para,
                         float* d_refvol_para, float* d_area_para, float* d_vol_para, float* d_area, float* d_vol,
                         float* d_pararea) {
+    {
+        GcRefPtrs& r = gc_state().ref;
+        r.ncell = ncell; r.ntri = ntri; r.curpos = d_curpos; r.tri = d_tri; r.betri = d_beginendtri;
+        r.nthro = d_nthrobound; r.coor = d_totalcoor; r.trinordir = d_trinordir; r.triarea = d_triarea;
+        r.reftriarea = d_reftriarea; r.tricenter = d_tricenter; r.refarea_para = d_refarea_para;
+        r.refvol_para = d_refvol_para; r.area_para = d_area_para; r.vol_para = d_vol_para; r.area = d_area;
+        r.vol = d_vol; r.pararea = d_pararea; r.bbox = d_bbox;
+    }
+    if (gc_state().in_fused_step) return GC_OK;
     GcState& s = gc_state();
     if (ncell < 0 || ntri < 0) return gc_fail(GC_EINVAL, "CalGeoPara: negative sizes");
     if (ncell == 0) return GC_OK;   // the reference calls it with nCell = 0 too (src/Particle.cu:476)
@@ -388,6 +397,13 @@ int gc_cupar_SetMechPara(int ncell, int nedge, int* d_edge, int* d_curpos, float
                          float* d_maxrefedgelen, float* d_bendmodpara, float* d_shearmodpara, float* d_hbending,
                          float* d_powerindex, float* d_perlenWLC, float* d_hpow, float* d_reftriangle,
                          float* d_trinordir, float* d_tricenter, float* d_coor) {
+    {
+        GcRefPtrs& r = gc_state().ref;
+        r.nedge = nedge; r.edge = d_edge; r.refedgelen = d_refedgelen; r.maxrefedgelen = d_maxrefedgelen;
+        r.bendmod = d_bendmodpara; r.shearmod = d_shearmodpara; r.hbending = d_hbending; r.perlen = d_perlenWLC;
+        r.hpow = d_hpow; r.reftriangle = d_reftriangle;
+    }
+    if (gc_state().in_fused_step) return GC_OK;
     (void)d_trinordir; (void)d_tricenter;
     GcState& s = gc_state();
     if (ncell <= 0 || nedge <= 0) return GC_OK;
@@ -408,6 +424,12 @@ int gc_cupar_CalCellDefForce(int ncell, unsigned nedge, unsigned ntri, unsigned 
                              float* d_hlarea_para, float* d_hgarea_para, float* d_area_para, float* d_refarea_para,
                              float* d_hvol_para, float* d_vol_para, float* d_refvol_para, float* d_totalforce,
                              int* d_sortpart, int* d_curpos) {
+    {
+        GcRefPtrs& r = gc_state().ref;
+        r.hlarea = d_hlarea_para; r.hgarea = d_hgarea_para; r.hvol = d_hvol_para; r.defforce = d_defforce;
+        r.edge = d_edge; r.nedge = (int)nedge; r.tri = d_tri; r.ntri = (int)ntri;
+    }
+    if (gc_state().in_fused_step) return GC_OK;
     (void)d_bbox; (void)h_defforce; (void)d_nthrobound; (void)d_trinordir; (void)d_tricenter; (void)d_triarea;
     (void)d_sortpart;
     GcState& s = gc_state();
@@ -440,6 +462,11 @@ int gc_cupar_CalCellDefForce(int ncell, unsigned nedge, unsigned ntri, unsigned 
 int gc_cupar_CalCellAggForce(unsigned ncell, unsigned n, unsigned ncellpar, float* d_totalcoor, float* d_aggforce,
                              int* d_cc, int* d_ncube, int* d_sortpart, int* d_celltab, float* d_outerregion,
                              int* d_beginendcube, float* d_totalforce, float* d_pararea) {
+    {
+        GcRefPtrs& r = gc_state().ref;
+        r.celltab = d_celltab; r.aggforce = d_aggforce;
+    }
+    if (gc_state().in_fused_step) return GC_OK;
     (void)d_ncube; (void)d_outerregion;
     GcState& s = gc_state();
     if (ncell == 0 || ncellpar == 0) return GC_OK;

@@ -292,6 +292,7 @@ extern "C" {
 // with the reference geometry, are not read.
 int gc_cudiv_PreConList(int n, int cutradius, float* d_totalcoor, float* d_bboxsph, float* d_invwid, int* d_ncube,
                         int* d_cc, int* d_cubepart, int* d_sortpart, int* d_oldpos) {
+    if (gc_state().in_fused_step) return GC_OK;
     (void)cutradius; (void)d_invwid; (void)d_ncube;
     GcState& s = gc_state();
     if (n < 0) return gc_fail(GC_EINVAL, "PreConList: n < 0");
@@ -307,6 +308,7 @@ int gc_cudiv_PreConList(int n, int cutradius, float* d_totalcoor, float* d_bboxs
 
 // K5 -- src/ConfigDomain.cuh:12, src/Particle.cu:669.
 int gc_cudiv_Sort(int n, int* keys, int* values) {
+    if (gc_state().in_fused_step) return GC_OK;
     GcState& s = gc_state();
     if (n < 0) return gc_fail(GC_EINVAL, "Sort: n < 0");
     if (n == 0) return GC_OK;
@@ -330,6 +332,7 @@ int gc_cudiv_Sort(int n, int* keys, int* values) {
 
 // K6 -- src/ConfigDomain.cuh:13, src/Particle.cu:672.
 int gc_cudiv_CalBeginEndCube(int n, int sizecube, int* d_cubepart, int* d_beginendcube) {
+    if (gc_state().in_fused_step) return GC_OK;
     GcState& s = gc_state();
     if (n < 0 || sizecube <= 0) return gc_fail(GC_EINVAL, "CalBeginEndCube: bad sizes (%d, %d)", n, sizecube);
     if (s.grid_set && s.grid.ncells > sizecube)
@@ -379,6 +382,7 @@ static int sort_arrays(int n, int* d_sortpart, int* d_oldpos, int* d_curpos, flo
 // K7 -- src/ConfigDomain.cuh:14, src/Particle.cu:677 (no membrane cells).
 int gc_cudiv_SortBasicArrays(int n, int* d_sortpart, int* d_oldpos, float* d_totalcoor, int* d_cc, float* d_velrhop,
                              float* d_velhalf, float* d_totalforce, float* d_press) {
+    if (gc_state().in_fused_step) return GC_OK;
     return sort_arrays(n, d_sortpart, d_oldpos, nullptr, d_totalcoor, d_cc, d_velrhop, d_velhalf, d_totalforce,
                        d_press, nullptr);
 }
@@ -388,6 +392,8 @@ int gc_cudiv_SortBasicArrays(int n, int* d_sortpart, int* d_oldpos, float* d_tot
 int gc_cudiv_SortArraysWithCells(int n, int* d_sortpart, int* d_oldpos, int* d_curpos, float* d_totalcoor, int* d_cc,
                                  float* d_velrhop, float* d_velhalf, float* d_totalforce, float* d_press,
                                  int* d_nthrobound) {
+    gc_state().ref.curpos = d_curpos;
+    if (gc_state().in_fused_step) return GC_OK;
     if (!d_curpos) return gc_fail(GC_EINVAL, "SortArraysWithCells: curpos is NULL");
     return sort_arrays(n, d_sortpart, d_oldpos, d_curpos, d_totalcoor, d_cc, d_velrhop, d_velhalf, d_totalforce,
                        d_press, d_nthrobound);

@@ -36,6 +36,8 @@ void init_from_env() {
     }
     const char* nz = getenv("GPUCELL_NOISE");
     if (nz && (strcmp(nz, "0") == 0 || strcmp(nz, "off") == 0)) g_state.noise_on = 0;
+    const char* en = getenv("GPUCELL_ENGINE");
+    if (en && strcmp(en, "fused") == 0) g_state.engine_mode = 1;
     atexit(gc_atexit);
 }
 }  // namespace
@@ -211,6 +213,19 @@ int gc_set_periodic(int mask) {
 
 int gc_get_periodic(void) { return gc_state().periodic_mask; }
 
+int gc_set_engine(int mode) {
+    if (mode != 0 && mode != 1) return gc_fail(GC_EINVAL, "engine %d is neither 0 (entry-point kernels) nor 1 (fused)", mode);
+    GcState& s = gc_state();
+    if (s.engine_mode != mode) {
+        gc_engine_reset();
+        s.in_fused_step = false;
+    }
+    s.engine_mode = mode;
+    return GC_OK;
+}
+
+int gc_get_engine(void) { return gc_state().engine_mode; }
+
 int gc_set_noise(int on) {
     gc_state().noise_on = on ? 1 : 0;
     return GC_OK;
@@ -242,6 +257,8 @@ int gc_device_status(unsigned* flags) {
 
 int gc_shutdown(void) {
     GcState& s = gc_state();
+    gc_engine_reset();
+    s.in_fused_step = false;
     for (int i = 0; i < SCR_COUNT_; ++i) {
         if (s.scratch[i]) cudaFree(s.scratch[i]);
         s.scratch[i] = nullptr;
@@ -273,6 +290,10 @@ int gc_cupar_ConstsDataUp(const Structconst* consts) {
     s.grid_set = false;
     s.grid_bbox_ptr = nullptr;
     s.velhalf_ptr = nullptr;
+    gc_engine_reset();
+    s.ref = GcRefPtrs();
+    s.plain_steps = 0;
+    s.in_fused_step = false;
     if (!gc_flags_ptr()) return GC_ENOMEM;
     return GC_OK;
 }

@@ -57,6 +57,17 @@ int gc_version(void);
  * value.  Takes effect at the next gc_cudiv_PreConList. */
 int gc_set_periodic(int mask);
 int gc_get_periodic(void);
+/* How the boundary entry points compute a step: 0 (default) runs one kernel
+ * per entry point on the caller's buffers; 1 runs, from the second step
+ * after ConstsDataUp on, the whole step as the fused step of gc_fused_*
+ * inside SetFluidExtForce (which carries DriveOn), writes the state the host
+ * reads back into the caller's buffers at the end of the step, and turns
+ * the other calls of the step into no-ops.  The first step runs on the
+ * entry-point kernels and records the caller's buffers.  The caller must not
+ * change its buffers between steps (GPUCell's host frame only reads them).
+ * GPUCELL_ENGINE=fused selects 1 at load time. */
+int gc_set_engine(int mode);
+int gc_get_engine(void);
 /* Thermal pair noise on (1, default) or off (0). GPUCELL_NOISE=0 turns it
  * off at load time. */
 int gc_set_noise(int on);
