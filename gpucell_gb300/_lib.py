@@ -54,7 +54,22 @@ class GcFusedOptions(C.Structure):
     """ctypes mirror of GcFusedOptions (include/gpucell_gb300.h)."""
 
     _fields_ = [("skin", C.c_float), ("block", C.c_int), ("list_capacity", C.c_int), ("compact", C.c_int),
-                ("reserved", C.c_int * 4)]
+                ("graph", C.c_int), ("reserved", C.c_int * 3)]
+
+
+assert C.sizeof(GcFusedOptions) == 32
+
+
+class GcSystemDesc(C.Structure):
+    """ctypes mirror of GcSystemDesc (include/gpucell_gb300.h): one system of an ensemble."""
+
+    _fields_ = [("consts", Structconst), ("bbox", C.c_float * 6), ("periodic_mask", C.c_int),
+                ("reserved", C.c_int)]
+
+
+assert C.sizeof(GcSystemDesc) == 128
+
+GC_TUNE_CACHE = 1
 
 _P = C.c_void_p
 _I = C.c_int
@@ -111,7 +126,17 @@ _SIGS = {
     "gc_fused_flags": [_P, _P],
     "gc_fused_profile": [_P, _I],
     "gc_fused_profile_read": [_P, _P, _P, _P],
+    "gc_fused_get_options": [_P, _P],
+    "gc_fused_set_options": [_P, _P],
+    "gc_fused_autotune": [_P, _I, _I, _I, _P, _P],
     "gc_fused_destroy": [_P],
+    "gc_ensemble_create": [_I, _P, _I, _P, _P],
+    "gc_ensemble_size": [_P, _P, _P],
+    "gc_ensemble_set_cells": [_P, _I, _I, _I, _I] + [_P] * 9,
+    "gc_ensemble_load": [_P, _I] + [_P] * 5 + [_I],
+    "gc_ensemble_store": [_P, _I] + [_P] * 7 + [_I],
+    "gc_ensemble_store_cells": [_P, _I] + [_P] * 7 + [_I],
+    "gc_ensemble_cell_sums": [_P, _I, _P, _P],
 }
 _RESTYPES = {"gc_last_error": C.c_char_p, "gc_get_step": C.c_longlong, "gc_launch_count": C.c_ulonglong}
 

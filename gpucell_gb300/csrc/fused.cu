@@ -1,13 +1,22 @@
-// fused.cu -- the fused SDPD + membrane timestep on library-owned state.
+// fused.cu -- the fused SDPD + membrane timestep on library-owned state, for
+// one simulation or for an ensemble of independent ones in the same launches.
 //
 // Same method and the same step order as the boundary entry points
 // (Particle::UpdatePar, src/Particle.cu:1310-1329), restructured for the GPU:
 //
 //   * State lives in the library, in slot order (sorted by cube), as float4
-//     records: position + id, velocity, predicted velocity, VelHalf, force,
-//     and (1/d, P/d^2) per particle.  Membrane vertices additionally have a
-//     membrane-ordered copy of their position and crossing counts, so the
-//     membrane kernels index topology directly.
+//     records: position + global id, velocity, predicted velocity, VelHalf,
+//     force, and (1/d, P/d^2) per particle.  Membrane vertices additionally
+//     have a membrane-ordered copy of their position and crossing counts, so
+//     the membrane kernels index topology directly.
+//   * An ensemble of independent simulations ("systems") shares the arrays.
+//     System s owns the global ids [id0_s, end_s), in the same type order as
+//     one simulation (Bound1, Bound2, fluid, membrane), its own box, cube
+//     grid, body force and noise seed, and a contiguous range of the global
+//     cube numbering; so the sort and every pass run once over all systems
+//     and no pair ever spans two systems.  Each slot carries its system
+//     index.  One simulation is an ensemble of one whose kernels take the
+//     system from their parameters instead of the table.
 //   * Neighbours come from Verlet lists with a skin: built from a 27-cube
 //     scan at cut-off rc + skin, stored 32 slots interleaved (entry k of slot
 //     i at ((i/32)*cap + k)*32 + i%32, so a warp reads 128 contiguous bytes
@@ -20,12 +29,20 @@
 //     wall repulsion + body force + membrane forces + corrector (K12, K13,
 //     K14, K17/K18 add, K19); wall velocity again (K10).
 //   * Per-cell membrane area and volume are summed in FP64.
+//   * Optionally each step is one captured CUDA graph: the rebuild decision
+//     is taken on the device (a conditional node runs the re-sort and list
+//     build only when some particle moved more than skin/2), the noise key of
+//     the step is derived on the device from a step counter, and the host
+//     synchronises once per gc_fused_step call instead of once per step.
 #include "gc_internal.cuh"
 
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
 
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -41,11 +58,50 @@ __device__ __forceinline__ size_t sell(int i, int k, int cap) {
     return ((size_t)(i >> 5) * cap + k) * 32 + (i & 31);
 }
 
+// One system of an ensemble: global id ranges, grids, body force, seed.
+struct SysInfo {
+    uint64_t seed;                   // iSeed of the system (pair noise)
+    unsigned id0, b2, fl, cs, end;   // first id; first Bound2, fluid and membrane id; one past the last
+    unsigned m0;                     // first membrane index (membrane-ordered arrays)
+    int cube0;                       // first global cube of the list grid
+    int mcube0;                      // first global cube of the aggregation grid
+    float gx;                        // body force in x (ConstExtForce)
+    float invL[3];
+    GcGrid g;                        // list grid: the box, cubes at least rc + skin wide
+    GcGrid mg;                       // aggregation grid: cubes at least MaxCut wide
+};
+
+__device__ __forceinline__ int stype(unsigned id, const SysInfo& S) {
+    return id < S.b2 ? PT_B1 : (id < S.fl ? PT_B2 : (id < S.cs ? PT_FLUID : PT_MEMB));
+}
+
+// System of the given global id (binary search over the id ranges).
+__device__ __forceinline__ int find_sys(const SysInfo* sys, int nsys, unsigned id) {
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (sys[mid].id0 <= id) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // Box constants of the per-step kernels.
 struct Box {
     float L[3], invL[3];
     int pmask;
 };
+
+__device__ __forceinline__ Box box_of(const SysInfo& S) {
+    Box b;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        b.L[a] = S.g.L[a];
+        b.invL[a] = S.invL[a];
+    }
+    b.pmask = S.g.pmask;
+    return b;
+}
 
 // Minimum image of a list pair.  A listed pair is either far closer than
 // L/2 or close to L apart along a periodic axis, so d - L rint(d/L) makes
@@ -59,10 +115,43 @@ __device__ __forceinline__ float3 pair_image(float3 a, float3 b, const Box& B) {
     return d;
 }
 
+// The per-step kernels exist in two forms.  ENS = false: one system, given
+// by value in the kernel parameters (constant bank, no per-thread loads).
+// ENS = true: the system of each slot comes from the per-slot index and the
+// device table (ensembles, and captured steps, whose noise keys are derived
+// on the device).
+#define GC_SYS_OF(S, i) const SysInfo& S = ENS ? sys[sysid ? sysid[i] : 0] : s0
+
+// ---------------------------------------------------------------------------
+// Step prologue on the device: advance the step counter, derive every
+// system's noise key for the new step, clear the rebuild flag.
+// ---------------------------------------------------------------------------
+__global__ void fk_step_begin(int nsys, const SysInfo* __restrict__ sys, long long* __restrict__ dstep,
+                              unsigned* __restrict__ nkey, int* __restrict__ rebuild) {
+    long long s = *dstep + 1;
+    for (int k = threadIdx.x; k < nsys; k += blockDim.x) nkey[k] = noise_key(sys[k].seed, (uint64_t)s);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *dstep = s;
+        *rebuild = 0;
+    }
+}
+
+// Sets the condition of the rebuild node of a captured step and counts the
+// rebuilds.  Launched only inside a captured graph.
+__global__ void fk_set_cond(cudaGraphConditionalHandle h, const int* __restrict__ rebuild,
+                            unsigned long long* __restrict__ count) {
+    unsigned v = *rebuild != 0;
+    cudaGraphSetConditional(h, v);
+    if (v) *count += 1;
+}
+
 // ---------------------------------------------------------------------------
 // K2 + K3 + K9 for fluid and membrane slots
 // ---------------------------------------------------------------------------
-__global__ void fk_integrate(int n, GcParams p, float4* __restrict__ pos, const float4* __restrict__ vel,
+template <bool ENS>
+__global__ void fk_integrate(int n, GcParams p, SysInfo s0, const SysInfo* __restrict__ sys,
+                             const int* __restrict__ sysid, float4* __restrict__ pos, const float4* __restrict__ vel,
                              float4* __restrict__ vh, float4* __restrict__ vpred, const float4* __restrict__ force,
                              const float4* __restrict__ refpos, int4* __restrict__ nthro, float half_skin2,
                              int* __restrict__ rebuild, float4* __restrict__ mpos, int4* __restrict__ mnthro,
@@ -72,7 +161,8 @@ __global__ void fk_integrate(int n, GcParams p, float4* __restrict__ pos, const 
     if (i < n) {
         float4 x = pos[i];
         unsigned id = fid(x);
-        if (is_mobile(id, p)) {
+        GC_SYS_OF(S, i);
+        if (id >= S.fl) {
             float4 v = vel[i], f = force[i];
             float h = 0.5f * p.dt * p.dt * p.inv_mass;
             x.x += p.dt * v.x + h * f.x;
@@ -85,10 +175,10 @@ __global__ void fk_integrate(int n, GcParams p, float4* __restrict__ pos, const 
             int* ts[3] = {&t.x, &t.y, &t.z};
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                if (!(p.g.pmask & (1 << a))) continue;
+                if (!(S.g.pmask & (1 << a))) continue;
                 float c = *xs[a];
-                if (c >= p.g.hi[a]) { c -= p.g.L[a]; *ts[a] += 1; crossed = true; }
-                else if (c < p.g.lo[a]) { c += p.g.L[a]; *ts[a] -= 1; crossed = true; }
+                if (c >= S.g.hi[a]) { c -= S.g.L[a]; *ts[a] += 1; crossed = true; }
+                else if (c < S.g.lo[a]) { c += S.g.L[a]; *ts[a] -= 1; crossed = true; }
                 *xs[a] = c;
             }
             if (crossed) nthro[i] = t;
@@ -97,10 +187,10 @@ __global__ void fk_integrate(int n, GcParams p, float4* __restrict__ pos, const 
             float4 w = vh[i];
             vh[i] = make_float4(v.x + hs * f.x, v.y + hs * f.y, v.z + hs * f.z, w.w);
             vpred[i] = make_float4(v.x + l * f.x, v.y + l * f.y, v.z + l * f.z, 0.f);
-            float3 d = min_image(xyz(x), xyz(refpos[i]), p.g);
+            float3 d = min_image(xyz(x), xyz(refpos[i]), S.g);
             far = norm2_rn(d) > half_skin2;
-            if (id >= p.nC) {
-                unsigned m = id - p.nC;
+            if (id >= S.cs) {
+                unsigned m = S.m0 + (id - S.cs);
                 mpos[m] = x;
                 mnthro[m] = t;
             }
@@ -112,28 +202,32 @@ __global__ void fk_integrate(int n, GcParams p, float4* __restrict__ pos, const 
 // ---------------------------------------------------------------------------
 // Rebuild: cube keys, permutation, neighbour lists
 // ---------------------------------------------------------------------------
-__global__ void fk_cellkey(int n, GcGrid g, const float4* __restrict__ pos, int* __restrict__ keys,
-                           int* __restrict__ vals) {
+__global__ void fk_cellkey(int n, const SysInfo* __restrict__ sys, const int* __restrict__ sysid,
+                           const float4* __restrict__ pos, int* __restrict__ keys, int* __restrict__ vals) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const SysInfo& S = sys[sysid ? sysid[i] : 0];
     float4 x = pos[i];
-    keys[i] = cube_key(cube_coord(x.x, 0, g), cube_coord(x.y, 1, g), cube_coord(x.z, 2, g), g);
+    keys[i] = S.cube0 + cube_key(cube_coord(x.x, 0, S.g), cube_coord(x.y, 1, S.g), cube_coord(x.z, 2, S.g), S.g);
     vals[i] = i;
 }
 
 struct SlotArrays {
     float4 *pos, *vel, *vpred, *vh, *force;
     int4* nthro;
+    int* sys;   // system of each slot (nullptr for one system)
 };
 
 // Gathers the slot arrays into the new order and wraps every position into
-// the box on periodic axes (counting the crossings), so that the list build
+// its box on periodic axes (counting the crossings), so that the list build
 // can use one image shift per row of cubes.
-__global__ void fk_permute(int n, GcGrid g, const int* __restrict__ perm, SlotArrays src, SlotArrays dst,
-                           float4* __restrict__ refpos, int* __restrict__ slot_of) {
+__global__ void fk_permute(int n, const SysInfo* __restrict__ sys, const int* __restrict__ perm, SlotArrays src,
+                           SlotArrays dst, float4* __restrict__ refpos, int* __restrict__ slot_of) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     int o = perm[q];
+    int s = src.sys ? src.sys[o] : 0;
+    const GcGrid& g = sys[s].g;
     float4 x = src.pos[o];
     int4 t = src.nthro[o];
     float* xs[3] = {&x.x, &x.y, &x.z};
@@ -158,18 +252,34 @@ __global__ void fk_permute(int n, GcGrid g, const int* __restrict__ perm, SlotAr
     dst.vh[q] = src.vh[o];
     dst.force[q] = src.force[o];
     dst.nthro[q] = t;
+    if (dst.sys) dst.sys[q] = s;
     refpos[q] = x;
     slot_of[fid(x)] = q;
 }
 
-// One thread per slot scans the cubes of the list grid around its own.
-// Fluid and membrane slots list every particle within rc + skin; Bound2
-// slots list the moving particles (for their wall velocity); Bound1 slots
-// list nothing.  Positions are inside the box on periodic axes (the
+// Copies the permuted slot arrays back (captured steps, whose launches are
+// bound to fixed buffers, cannot swap them).
+__global__ void fk_copy_slots(int n, SlotArrays src, SlotArrays dst) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    dst.pos[q] = src.pos[q];
+    dst.vel[q] = src.vel[q];
+    dst.vpred[q] = src.vpred[q];
+    dst.vh[q] = src.vh[q];
+    dst.force[q] = src.force[q];
+    dst.nthro[q] = src.nthro[q];
+    if (dst.sys) dst.sys[q] = src.sys[q];
+}
+
+// One thread per slot scans the cubes of its system's list grid around its
+// own.  Fluid and membrane slots list every particle within rc + skin;
+// Bound2 slots list the moving particles (for their wall velocity); Bound1
+// slots list nothing.  Positions are inside the box on periodic axes (the
 // permutation wraps them), so each neighbouring row of cubes has one image
 // shift, and the three cubes of a row that do not wrap are one contiguous
 // range of slots.
-__global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, GcParams p, const float4* __restrict__ pos,
+__global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, const SysInfo* __restrict__ sys,
+                                                     const int* __restrict__ sysid, const float4* __restrict__ pos,
                                                      const unsigned* __restrict__ start, int* __restrict__ nbr,
                                                      int* __restrict__ cnt, int cap, float cut2, unsigned* flags) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -177,16 +287,18 @@ __global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, GcParams p, const
     float4 xi4 = pos[i];
     float3 xi = xyz(xi4);
     unsigned id = fid(xi4);
-    int t = ptype(id, p);
+    const SysInfo& S = sys[sysid ? sysid[i] : 0];
+    int t = stype(id, S);
     int k = 0;
-    const GcGrid& g = p.g;
+    const GcGrid& g = S.g;
+    const unsigned fl = S.fl;
     auto scan = [&](unsigned b, unsigned e, float sx, float sy, float sz) {
         for (unsigned j = b; j < e; ++j) {
             float4 xj = pos[j];
             float dx = (xi.x - xj.x) + sx, dy = (xi.y - xj.y) + sy, dz = (xi.z - xj.z) + sz;
             float r2 = dx * dx + dy * dy + dz * dz;
             if (r2 >= cut2 || (int)j == i) continue;
-            if (t == PT_B2 && !is_mobile(fid(xj), p)) continue;
+            if (t == PT_B2 && fid(xj) < fl) continue;
             if (k < cap) nbr[sell(i, k, cap)] = (int)j;
             ++k;
         }
@@ -203,7 +315,7 @@ __global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, GcParams p, const
                 float sy = 0.f;
                 if (y < 0) { if (!(g.pmask & 2)) continue; y += g.n[1]; sy = g.L[1]; }
                 else if (y >= g.n[1]) { if (!(g.pmask & 2)) continue; y -= g.n[1]; sy = -g.L[1]; }
-                int row = g.n[0] * (y + g.n[1] * z);
+                int row = S.cube0 + g.n[0] * (y + g.n[1] * z);
                 if (cx >= 1 && cx + 1 < g.n[0]) {
                     scan(start[row + cx - 1], start[row + cx + 2], 0.f, sy, sz);
                 } else {
@@ -228,6 +340,7 @@ __global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, GcParams p, const
 // ---------------------------------------------------------------------------
 // K8 + K11 (+ K10 for Bound2 slots)
 // ---------------------------------------------------------------------------
+
 // With `cmask` set, fluid and membrane slots also record which of their list
 // entries act this step (SDPD partners within rc, Bound1 walls within the
 // repulsion range): one bit per entry, 32 entries per word, words of 32 slots
@@ -238,7 +351,9 @@ __device__ __forceinline__ size_t mrow(int i, int w, int mw) {
     return ((size_t)(i >> 5) * mw + w) * 32 + (i & 31);
 }
 
-__global__ void __launch_bounds__(kMaxBS) fk_density(int n, GcParams p, Box B, const float4* __restrict__ pos,
+template <bool ENS>
+__global__ void __launch_bounds__(kMaxBS) fk_density(int n, GcParams p, SysInfo s0, const SysInfo* __restrict__ sys,
+                                                  const int* __restrict__ sysid, const float4* __restrict__ pos,
                                                   float4* __restrict__ vpred, const float4* __restrict__ vh,
                                                   float2* __restrict__ dp, const int* __restrict__ nbr,
                                                   const int* __restrict__ cnt, int cap, unsigned* __restrict__ cmask,
@@ -248,7 +363,10 @@ __global__ void __launch_bounds__(kMaxBS) fk_density(int n, GcParams p, Box B, c
     float4 xi4 = pos[i];
     float3 xi = xyz(xi4);
     unsigned id = fid(xi4);
-    int t = ptype(id, p);
+    GC_SYS_OF(S, i);
+    const Box B = box_of(S);
+    const unsigned b2 = S.b2;
+    int t = stype(id, S);
     int c = cnt[i];
     const int* lp = nbr + sell(i, 0, cap);
     if (t == PT_FLUID || t == PT_MEMB) {
@@ -265,7 +383,7 @@ __global__ void __launch_bounds__(kMaxBS) fk_density(int n, GcParams p, Box B, c
             }
             float r2 = norm2_rn(pair_image(xi, xyz(xj), B));
             if (r2 < p.rc2) {
-                if (is_sdpd(fid(xj), p)) {
+                if (fid(xj) >= b2) {
                     float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
                     sum += wendland_w(r, p);
                     if (r2 > 0.f) m |= 1u << (k & 31);
@@ -310,24 +428,31 @@ __global__ void __launch_bounds__(kMaxBS) fk_density(int n, GcParams p, Box B, c
 // K12 + K13 + K14 + membrane forces + K19
 // ---------------------------------------------------------------------------
 // COMPACT: iterate only the entries fk_density marked as acting this step,
-// so the cut-off test is already done.
-template <bool COMPACT>
-__global__ void __launch_bounds__(kMaxBS, 6) fk_force(int n, GcParams p, Box B, const float4* __restrict__ pos,
-                                                const float4* __restrict__ vpred, const float4* __restrict__ vh,
-                                                const float2* __restrict__ dp, float4* __restrict__ force,
-                                                float4* __restrict__ vel, const int* __restrict__ nbr,
-                                                const int* __restrict__ cnt, int cap,
-                                                const unsigned* __restrict__ cmask, int mw,
-                                                const float4* __restrict__ mforce, int drive) {
+// so the cut-off test is already done.  The pair noise is keyed by the ids
+// local to the system, so a system draws the same noise in an ensemble as
+// alone.
+template <bool COMPACT, bool ENS>
+__global__ void __launch_bounds__(kMaxBS, ENS ? 5 : 6)
+    fk_force(int n, GcParams p, SysInfo s0, const SysInfo* __restrict__ sys, const int* __restrict__ sysid,
+             const unsigned* __restrict__ nkey, const float4* __restrict__ pos, const float4* __restrict__ vpred,
+             const float4* __restrict__ vh, const float2* __restrict__ dp, float4* __restrict__ force,
+             float4* __restrict__ vel, const int* __restrict__ nbr, const int* __restrict__ cnt, int cap,
+             const unsigned* __restrict__ cmask, int mw, const float4* __restrict__ mforce, int drive) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 xi4 = pos[i];
     float3 xi = xyz(xi4);
     unsigned id = fid(xi4);
-    if (!is_mobile(id, p)) {
+    const int s = ENS ? (sysid ? sysid[i] : 0) : 0;
+    GC_SYS_OF(S, i);
+    if (id < S.fl) {
         force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
+    const Box B = box_of(S);
+    const unsigned b2 = S.b2;
+    const unsigned id0 = S.id0;
+    const uint32_t key = ENS ? nkey[s] : p.noise_key;
     float4 vi = vpred[i];
     float2 dpi = dp[i];
     bool noise = p.noise_pref > 0.f;
@@ -369,7 +494,7 @@ __global__ void __launch_bounds__(kMaxBS, 6) fk_force(int n, GcParams p, Box B, 
         if (!COMPACT && (r2 >= p.rc2 || r2 <= 0.f)) continue;   // coincident pairs exert no force
         unsigned idj = fid(xj4);
         float inv_r = rsqrtf(r2);
-        if (!is_sdpd(idj, p)) {   // Bound1: repulsion only
+        if (idj < b2) {   // Bound1: repulsion only
             if (r2 < p.rep_r0sq) {
                 float ir2 = inv_r * inv_r;
                 float q2 = p.rep_r0sq * ir2, q4 = q2 * q2, q12 = q4 * q4 * q4;
@@ -391,32 +516,36 @@ __global__ void __launch_bounds__(kMaxBS, 6) fk_force(int n, GcParams p, Box B, 
             float qq = p.noise_pref * fdd;
             float q = qq > 0.f ? qq * rsqrtf(qq) : 0.f;
             q = id < idj ? q : -q;   // the pair sign of xi_ij
-            float3 xi_ = pair_noise_unsigned(id, idj, p);
+            float3 xi_ = pair_noise_unsigned_k(id - id0, idj - id0, key);
             float exi = dot3(e, xi_);
             f += q * (p.sqrtA * xi_ + ((p.sqrtAB - p.sqrtA) * exi) * e);
         }
     }
-    if (drive) f.x += p.gx;
-    if (id >= p.nC && mforce) {
-        float4 mf = mforce[id - p.nC];
+    if (drive) f.x += S.gx;
+    if (id >= S.cs && mforce) {
+        float4 mf = mforce[S.m0 + (id - S.cs)];
         f += f3(mf.x, mf.y, mf.z);
     }
     // a non-finite force shows up as a non-finite position in the next
     // fk_integrate, which raises GC_FLAG_NONFINITE
     force[i] = make_float4(f.x, f.y, f.z, 0.f);
     float4 h = vh[i];
-    float s = 0.5f * p.dt * p.inv_mass;
-    vel[i] = make_float4(h.x + s * f.x, h.y + s * f.y, h.z + s * f.z, 0.f);
+    float sc = 0.5f * p.dt * p.inv_mass;
+    vel[i] = make_float4(h.x + sc * f.x, h.y + sc * f.y, h.z + sc * f.z, 0.f);
 }
 
 // second K10: wall velocity from the corrected velocities
-__global__ void fk_wallvel(int n, GcParams p, Box B, const float4* __restrict__ pos, float4* __restrict__ vel,
+template <bool ENS>
+__global__ void fk_wallvel(int n, GcParams p, SysInfo s0, const SysInfo* __restrict__ sys,
+                           const int* __restrict__ sysid, const float4* __restrict__ pos, float4* __restrict__ vel,
                            const float4* __restrict__ vh, const int* __restrict__ nbr, const int* __restrict__ cnt,
                            int cap) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 xi4 = pos[i];
-    if (ptype(fid(xi4), p) != PT_B2) return;
+    GC_SYS_OF(S, i);
+    if (stype(fid(xi4), S) != PT_B2) return;
+    const Box B = box_of(S);
     float3 xi = xyz(xi4);
     float3 num = f3(0.f, 0.f, 0.f);
     float den = 0.f;
@@ -437,7 +566,9 @@ __global__ void fk_wallvel(int n, GcParams p, Box B, const float4* __restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// Membranes (membrane order; positions unwrapped with crossing counts)
+// Membranes (membrane order; positions unwrapped with crossing counts).
+// Vertex, triangle and cell indices are global over the ensemble; msys and
+// cellsys give the system of a vertex and of a cell (nullptr: system 0).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float3 mdiff(const float4* mpos, const int4* mnt, int a, int b, const GcGrid& g) {
     float4 xa = mpos[a], xb = mpos[b];
@@ -468,7 +599,8 @@ __device__ double block_sum_d(double v, double* sh) {
 }
 
 // Triangle geometry and per-cell area/volume (FP64 sums), one block per cell.
-__global__ void fk_mgeo(GcParams p, int ncell, int ntri, const int3* __restrict__ tri, const int2* __restrict__ betri,
+__global__ void fk_mgeo(GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ cellsys, int ncell,
+                        int ntri, const int3* __restrict__ tri, const int2* __restrict__ betri,
                         const float4* __restrict__ mpos, const int4* __restrict__ mnt, float* __restrict__ tarea,
                         float4* __restrict__ tnorm, float4* __restrict__ tcen, float* __restrict__ reftarea,
                         double* __restrict__ carea, double* __restrict__ cvol, double* __restrict__ crefarea,
@@ -480,23 +612,29 @@ __global__ void fk_mgeo(GcParams p, int ncell, int ntri, const int3* __restrict_
         if (threadIdx.x == 0) raise_flag(flags, GC_FLAG_BAD_INDEX);
         return;
     }
+    const GcGrid& g = sys[cellsys ? cellsys[c] : 0].g;
+    int ncp = (int)p.nCP;
     int r = tri[be.x].x - 1;
+    if (r < 0 || r >= ncp) {
+        if (threadIdx.x == 0) raise_flag(flags, GC_FLAG_BAD_INDEX);
+        return;
+    }
     float4 xr = mpos[r];
     int4 tr = mnt[r];
     float3 xru = f3(xr.x, xr.y, xr.z);
-    if (p.g.pmask & 1) xru.x += (float)tr.x * p.g.L[0];
-    if (p.g.pmask & 2) xru.y += (float)tr.y * p.g.L[1];
-    if (p.g.pmask & 4) xru.z += (float)tr.z * p.g.L[2];
+    if (g.pmask & 1) xru.x += (float)tr.x * g.L[0];
+    if (g.pmask & 2) xru.y += (float)tr.y * g.L[1];
+    if (g.pmask & 4) xru.z += (float)tr.z * g.L[2];
     double accA = 0.0, accV = 0.0;
     for (int t = be.x + threadIdx.x; t <= be.y; t += blockDim.x) {
         int3 v = tri[t];
         int a = v.x - 1, b = v.y - 1, cc = v.z - 1;
-        if (a < 0 || b < 0 || cc < 0 || a >= (int)p.nCP || b >= (int)p.nCP || cc >= (int)p.nCP) {
+        if (a < 0 || b < 0 || cc < 0 || a >= ncp || b >= ncp || cc >= ncp) {
             raise_flag(flags, GC_FLAG_BAD_INDEX);
             continue;
         }
-        float3 u1 = mdiff(mpos, mnt, a, r, p.g);
-        float3 e1 = mdiff(mpos, mnt, b, a, p.g), e2 = mdiff(mpos, mnt, cc, a, p.g);
+        float3 u1 = mdiff(mpos, mnt, a, r, g);
+        float3 e1 = mdiff(mpos, mnt, b, a, g), e2 = mdiff(mpos, mnt, cc, a, g);
         float3 xi = cross3(e1, e2);
         float len = sqrtf(dot3(xi, xi));
         float A = 0.5f * len;
@@ -555,21 +693,26 @@ __device__ __forceinline__ Dih dihedral_f(float3 xi, float3 xj, float3 xk, float
     return D;
 }
 
-__global__ void fk_mech_setup(GcParams p, int nedge, const int6* __restrict__ edge, const float4* __restrict__ mpos,
+__device__ __forceinline__ bool edge_ok(int6 E, int ncp, int* a, int* b, int* c, int* d) {
+    *a = E.x - 1; *b = E.y - 1; *c = E.z - 1; *d = E.k - 1;
+    return *a >= 0 && *b >= 0 && *c >= 0 && *d >= 0 && *a < ncp && *b < ncp && *c < ncp && *d < ncp;
+}
+
+__global__ void fk_mech_setup(GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ msys, int nedge,
+                              const int6* __restrict__ edge, const float4* __restrict__ mpos,
                               const int4* __restrict__ mnt, const float* __restrict__ shear,
                               const float* __restrict__ bend, float* __restrict__ l0a, float* __restrict__ lmax,
                               float* __restrict__ perlen, float* __restrict__ hpow, float* __restrict__ hbend,
                               float* __restrict__ refang, unsigned* flags) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nedge) return;
-    int6 E = edge[e];
-    int a = E.x - 1, b = E.y - 1, c = E.z - 1, d = E.k - 1;
-    int ncp = (int)p.nCP;
-    if (a < 0 || b < 0 || c < 0 || d < 0 || a >= ncp || b >= ncp || c >= ncp || d >= ncp) {
+    int a, b, c, d;
+    if (!edge_ok(edge[e], (int)p.nCP, &a, &b, &c, &d)) {
         raise_flag(flags, GC_FLAG_BAD_INDEX);
         return;
     }
-    float3 xb = mdiff(mpos, mnt, b, a, p.g), xc = mdiff(mpos, mnt, c, a, p.g), xd = mdiff(mpos, mnt, d, a, p.g);
+    const GcGrid& g = sys[msys ? msys[a] : 0].g;
+    float3 xb = mdiff(mpos, mnt, b, a, g), xc = mdiff(mpos, mnt, c, a, g), xd = mdiff(mpos, mnt, d, a, g);
     float l0 = sqrtf(dot3(xb, xb));
     const float x0 = 1.f / 2.2f, m = 2.f;
     float u = 1.f - x0;
@@ -593,22 +736,21 @@ __device__ __forceinline__ void add4(float4* o, float3 f) {
     atomicAdd(&o->z, f.z);
 }
 
-__global__ void fk_medge(GcParams p, int nedge, const int6* __restrict__ edge, const float4* __restrict__ mpos,
-                         const int4* __restrict__ mnt, const float* __restrict__ lmax,
-                         const float* __restrict__ perlen, const float* __restrict__ hpow,
-                         const float* __restrict__ refang, const float* __restrict__ hbend,
-                         float4* __restrict__ mforce, unsigned* flags) {
+__global__ void fk_medge(GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ msys, int nedge,
+                         const int6* __restrict__ edge, const float4* __restrict__ mpos, const int4* __restrict__ mnt,
+                         const float* __restrict__ lmax, const float* __restrict__ perlen,
+                         const float* __restrict__ hpow, const float* __restrict__ refang,
+                         const float* __restrict__ hbend, float4* __restrict__ mforce, unsigned* flags) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nedge) return;
-    int6 E = edge[e];
-    int a = E.x - 1, b = E.y - 1, c = E.z - 1, d = E.k - 1;
-    int ncp = (int)p.nCP;
-    if (a < 0 || b < 0 || c < 0 || d < 0 || a >= ncp || b >= ncp || c >= ncp || d >= ncp) {
+    int a, b, c, d;
+    if (!edge_ok(edge[e], (int)p.nCP, &a, &b, &c, &d)) {
         raise_flag(flags, GC_FLAG_BAD_INDEX);
         return;
     }
+    const GcGrid& g = sys[msys ? msys[a] : 0].g;
     float3 z = f3(0.f, 0.f, 0.f);
-    float3 xb = mdiff(mpos, mnt, b, a, p.g), xc = mdiff(mpos, mnt, c, a, p.g), xd = mdiff(mpos, mnt, d, a, p.g);
+    float3 xb = mdiff(mpos, mnt, b, a, g), xc = mdiff(mpos, mnt, c, a, g), xd = mdiff(mpos, mnt, d, a, g);
     float3 f1 = z, f2 = z, f3v = z, f4 = z;
     float pl = perlen[e];
     float r = sqrtf(dot3(xb, xb));
@@ -641,16 +783,18 @@ __global__ void fk_medge(GcParams p, int nedge, const int6* __restrict__ edge, c
     add4(&mforce[d], f4);
 }
 
-__global__ void fk_mtri(GcParams p, int ncell, const int2* __restrict__ betri, const int3* __restrict__ tri,
-                        const float4* __restrict__ mpos, const int4* __restrict__ mnt,
-                        const float* __restrict__ reftarea, const float* __restrict__ hl,
-                        const float* __restrict__ hg, const float* __restrict__ hv, const double* __restrict__ carea,
-                        const double* __restrict__ cvol, const double* __restrict__ crefarea,
-                        const double* __restrict__ crefvol, float4* __restrict__ mforce, int ntri) {
+__global__ void fk_mtri(GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ cellsys, int ncell,
+                        const int2* __restrict__ betri, const int3* __restrict__ tri, const float4* __restrict__ mpos,
+                        const int4* __restrict__ mnt, const float* __restrict__ reftarea,
+                        const float* __restrict__ hl, const float* __restrict__ hg, const float* __restrict__ hv,
+                        const double* __restrict__ carea, const double* __restrict__ cvol,
+                        const double* __restrict__ crefarea, const double* __restrict__ crefvol,
+                        float4* __restrict__ mforce, int ntri) {
     // one block per cell: the cell's coefficients are read once
     int c = blockIdx.x;
     int2 be = betri[c];
     if (be.x < 0 || be.y >= ntri || be.y < be.x) return;
+    const GcGrid& g = sys[cellsys ? cellsys[c] : 0].g;
     float dA = (float)((carea[c] - crefarea[c]) / crefarea[c]);
     float dV = (float)((cvol[c] - crefvol[c]) / crefvol[c]);
     int ncp = (int)p.nCP;
@@ -658,7 +802,7 @@ __global__ void fk_mtri(GcParams p, int ncell, const int2* __restrict__ betri, c
         int3 v = tri[t];
         int a = v.x - 1, b = v.y - 1, cc = v.z - 1;
         if (a < 0 || b < 0 || cc < 0 || a >= ncp || b >= ncp || cc >= ncp) continue;
-        float3 x2 = mdiff(mpos, mnt, b, a, p.g), x3 = mdiff(mpos, mnt, cc, a, p.g);
+        float3 x2 = mdiff(mpos, mnt, b, a, g), x3 = mdiff(mpos, mnt, cc, a, g);
         float3 xi = cross3(x2, x3);
         float len = sqrtf(dot3(xi, xi));
         if (!(len > 0.f)) continue;
@@ -675,23 +819,26 @@ __global__ void fk_mtri(GcParams p, int ncell, const int2* __restrict__ betri, c
     }
 }
 
-// Morse aggregation on a membrane-only grid (cubes at least MaxCut wide).
-__global__ void fk_mkey(int ncp, GcGrid g, const float4* __restrict__ mpos, int* __restrict__ keys,
-                        int* __restrict__ vals) {
+// Morse aggregation on membrane-only grids (cubes at least MaxCut wide).
+__global__ void fk_mkey(int ncp, const SysInfo* __restrict__ sys, const int* __restrict__ msys,
+                        const float4* __restrict__ mpos, int* __restrict__ keys, int* __restrict__ vals) {
     int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= ncp) return;
+    const SysInfo& S = sys[msys ? msys[v] : 0];
     float4 x = mpos[v];
-    keys[v] = cube_key(cube_coord(x.x, 0, g), cube_coord(x.y, 1, g), cube_coord(x.z, 2, g), g);
+    keys[v] = S.mcube0 + cube_key(cube_coord(x.x, 0, S.mg), cube_coord(x.y, 1, S.mg), cube_coord(x.z, 2, S.mg), S.mg);
     vals[v] = v;
 }
 
-__global__ void fk_magg(int ncp, GcParams p, GcGrid g, const int* __restrict__ order,
-                        const unsigned* __restrict__ start, const float4* __restrict__ mpos,
-                        const int* __restrict__ celltab, const float* __restrict__ parea, float4* __restrict__ magg,
-                        float4* __restrict__ mforce) {
+__global__ void fk_magg(int ncp, GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ msys,
+                        const int* __restrict__ order, const unsigned* __restrict__ start,
+                        const float4* __restrict__ mpos, const int* __restrict__ celltab,
+                        const float* __restrict__ parea, float4* __restrict__ magg, float4* __restrict__ mforce) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= ncp) return;
     int v = order[q];
+    const SysInfo& S = sys[msys ? msys[v] : 0];
+    const GcGrid& g = S.mg;
     float4 x4 = mpos[v];
     float3 xi = xyz(x4);
     int ci = celltab[v];
@@ -707,7 +854,7 @@ __global__ void fk_magg(int ncp, GcParams p, GcGrid g, const int* __restrict__ o
             for (int dx = -1; dx <= 1; ++dx) {
                 int x = cube_step(cx, dx, 0, g);
                 if (x < 0) continue;
-                int c = cube_key(x, y, z, g);
+                int c = S.mcube0 + cube_key(x, y, z, g);
                 for (unsigned s = start[c]; s < start[c + 1]; ++s) {
                     int w = order[s];
                     if (celltab[w] == ci) continue;
@@ -730,89 +877,108 @@ __global__ void fk_magg(int ncp, GcParams p, GcGrid g, const int* __restrict__ o
 }
 
 // ---------------------------------------------------------------------------
-// Import / export in original order
+// Import / export in original (global id) order, for the ids
+// [id_base, id_base + count).  Host-side arrays are indexed from id_base.
 // ---------------------------------------------------------------------------
-__global__ void fk_load(int n, GcParams p, const float* __restrict__ x, const float* __restrict__ v,
-                        const float* __restrict__ vhalf, const float* __restrict__ f, const int* __restrict__ nt,
+// Before set-up the slots are in id order (slot = id); afterwards a load
+// replaces the state in the current slot order (the displacement check of
+// the next step decides whether the lists need a rebuild).
+__global__ void fk_load(int count, unsigned id_base, const SysInfo* __restrict__ sys, int nsys, int keep,
+                        const float* __restrict__ x, const float* __restrict__ v, const float* __restrict__ vhalf,
+                        const float* __restrict__ f, const int* __restrict__ nt, int* __restrict__ slot_of,
                         float4* __restrict__ pos, float4* __restrict__ vel, float4* __restrict__ vh,
-                        float4* __restrict__ force, int4* __restrict__ nthro) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    pos[i] = make_float4(x[3 * i], x[3 * i + 1], x[3 * i + 2], __uint_as_float((unsigned)i));
-    vel[i] = v ? make_float4(v[3 * i], v[3 * i + 1], v[3 * i + 2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
-    vh[i] = vhalf ? make_float4(vhalf[3 * i], vhalf[3 * i + 1], vhalf[3 * i + 2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
-    force[i] = f ? make_float4(f[3 * i], f[3 * i + 1], f[3 * i + 2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
-    nthro[i] = nt ? make_int4(nt[3 * i], nt[3 * i + 1], nt[3 * i + 2], 0) : make_int4(0, 0, 0, 0);
-}
-
-// Load into the current slot order (a set-up handle keeps its lists; the
-// displacement check decides whether they need a rebuild).
-__global__ void fk_load_keep(int n, GcParams p, const int* __restrict__ slot_of, const float* __restrict__ x,
-                             const float* __restrict__ v, const float* __restrict__ vhalf,
-                             const float* __restrict__ f, const int* __restrict__ nt, float4* __restrict__ pos,
-                             float4* __restrict__ vel, float4* __restrict__ vh, float4* __restrict__ force,
-                             int4* __restrict__ nthro, float4* __restrict__ mpos, int4* __restrict__ mnthro) {
-    int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n) return;
-    int i = slot_of[id];
-    float4 a = make_float4(x[3 * id], x[3 * id + 1], x[3 * id + 2], __uint_as_float((unsigned)id));
+                        float4* __restrict__ force, int4* __restrict__ nthro, float4* __restrict__ mpos,
+                        int4* __restrict__ mnthro) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    unsigned id = id_base + k;
+    int i;
+    if (keep) {
+        i = slot_of[id];
+    } else {
+        i = (int)id;
+        slot_of[id] = i;
+    }
+    float4 a = make_float4(x[3 * k], x[3 * k + 1], x[3 * k + 2], __uint_as_float(id));
     pos[i] = a;
-    if (v) vel[i] = make_float4(v[3 * id], v[3 * id + 1], v[3 * id + 2], 0.f);
-    if (vhalf) vh[i] = make_float4(vhalf[3 * id], vhalf[3 * id + 1], vhalf[3 * id + 2], 0.f);
-    if (f) force[i] = make_float4(f[3 * id], f[3 * id + 1], f[3 * id + 2], 0.f);
-    int4 t = nt ? make_int4(nt[3 * id], nt[3 * id + 1], nt[3 * id + 2], 0) : nthro[i];
-    if (nt) nthro[i] = t;
-    if (id >= (int)p.nC && mpos) {
-        mpos[id - p.nC] = a;
-        mnthro[id - p.nC] = t;
+    float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (v) vel[i] = make_float4(v[3 * k], v[3 * k + 1], v[3 * k + 2], 0.f);
+    else if (!keep) vel[i] = z;
+    if (vhalf) vh[i] = make_float4(vhalf[3 * k], vhalf[3 * k + 1], vhalf[3 * k + 2], 0.f);
+    else if (!keep) vh[i] = z;
+    if (f) force[i] = make_float4(f[3 * k], f[3 * k + 1], f[3 * k + 2], 0.f);
+    else if (!keep) force[i] = z;
+    int4 t = nt ? make_int4(nt[3 * k], nt[3 * k + 1], nt[3 * k + 2], 0) : (keep ? nthro[i] : make_int4(0, 0, 0, 0));
+    if (nt || !keep) nthro[i] = t;
+    if (mpos) {
+        const SysInfo& S = sys[find_sys(sys, nsys, id)];
+        if (id >= S.cs) {
+            mpos[S.m0 + id - S.cs] = a;
+            mnthro[S.m0 + id - S.cs] = t;
+        }
     }
 }
 
-__global__ void fk_store(int n, GcParams p, const float4* __restrict__ pos, const float4* __restrict__ vel,
+// Membrane-ordered positions from the slots (set-up).
+__global__ void fk_gather_mpos(int ncp, const SysInfo* __restrict__ sys, const int* __restrict__ msys,
+                               const int* __restrict__ slot_of, const float4* __restrict__ pos,
+                               const int4* __restrict__ nthro, float4* __restrict__ mpos, int4* __restrict__ mnthro) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= ncp) return;
+    const SysInfo& S = sys[msys ? msys[m] : 0];
+    int i = slot_of[S.cs + (unsigned)(m - (int)S.m0)];
+    mpos[m] = pos[i];
+    mnthro[m] = nthro[i];
+}
+
+__global__ void fk_store(int count, unsigned id_base, GcParams p, const int* __restrict__ slot_of,
+                         const float4* __restrict__ pos, const float4* __restrict__ vel,
                          const float4* __restrict__ vh, const float4* __restrict__ force,
                          const float2* __restrict__ dp, const int4* __restrict__ nthro, float* __restrict__ x,
                          float* __restrict__ v, float* __restrict__ rho, float* __restrict__ press,
                          float* __restrict__ f, float* __restrict__ vhalf, int* __restrict__ nt) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float4 a = pos[i];
-    unsigned id = fid(a);
-    if (x) { x[3 * id] = a.x; x[3 * id + 1] = a.y; x[3 * id + 2] = a.z; }
-    if (v) { float4 b = vel[i]; v[3 * id] = b.x; v[3 * id + 1] = b.y; v[3 * id + 2] = b.z; }
-    if (vhalf) { float4 b = vh[i]; vhalf[3 * id] = b.x; vhalf[3 * id + 1] = b.y; vhalf[3 * id + 2] = b.z; }
-    if (f) { float4 b = force[i]; f[3 * id] = b.x; f[3 * id + 1] = b.y; f[3 * id + 2] = b.z; }
-    if (nt) { int4 b = nthro[i]; nt[3 * id] = b.x; nt[3 * id + 1] = b.y; nt[3 * id + 2] = b.z; }
-    float2 q = dp[i];
-    if (rho) rho[id] = p.mass / q.x;
-    if (press) press[id] = q.y / (q.x * q.x);
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int i = slot_of[id_base + k];
+    if (x) { float4 a = pos[i]; x[3 * k] = a.x; x[3 * k + 1] = a.y; x[3 * k + 2] = a.z; }
+    if (v) { float4 b = vel[i]; v[3 * k] = b.x; v[3 * k + 1] = b.y; v[3 * k + 2] = b.z; }
+    if (vhalf) { float4 b = vh[i]; vhalf[3 * k] = b.x; vhalf[3 * k + 1] = b.y; vhalf[3 * k + 2] = b.z; }
+    if (f) { float4 b = force[i]; f[3 * k] = b.x; f[3 * k + 1] = b.y; f[3 * k + 2] = b.z; }
+    if (nt) { int4 b = nthro[i]; nt[3 * k] = b.x; nt[3 * k + 1] = b.y; nt[3 * k + 2] = b.z; }
+    if (rho || press) {
+        float2 q = dp[i];
+        if (rho) rho[k] = p.mass / q.x;
+        if (press) press[k] = q.y / (q.x * q.x);
+    }
 }
 
-__global__ void fk_store_cells(int ncp, int ntri, const float4* __restrict__ mforce, const float4* __restrict__ magg,
-                               const float* __restrict__ parea, const float4* __restrict__ tnorm,
-                               const float4* __restrict__ tcen, float* __restrict__ defforce,
-                               float* __restrict__ aggforce, float* __restrict__ pararea, float* __restrict__ trinor,
-                               float* __restrict__ tricen, int have_agg) {
+// membrane outputs: vertices [m0, m0 + ncp), triangles [t0, t0 + ntri)
+__global__ void fk_store_cells(int ncp, int m0, int ntri, int t0, const float4* __restrict__ mforce,
+                               const float4* __restrict__ magg, const float* __restrict__ parea,
+                               const float4* __restrict__ tnorm, const float4* __restrict__ tcen,
+                               float* __restrict__ defforce, float* __restrict__ aggforce, float* __restrict__ pararea,
+                               float* __restrict__ trinor, float* __restrict__ tricen, int have_agg) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < ncp) {
-        float4 a = have_agg ? magg[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        float4 m = mforce[i];
+        float4 a = have_agg ? magg[m0 + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 m = mforce[m0 + i];
         if (defforce) { defforce[3 * i] = m.x - a.x; defforce[3 * i + 1] = m.y - a.y; defforce[3 * i + 2] = m.z - a.z; }
         if (aggforce) { aggforce[3 * i] = a.x; aggforce[3 * i + 1] = a.y; aggforce[3 * i + 2] = a.z; }
-        if (pararea) pararea[i] = parea[i];
+        if (pararea) pararea[i] = parea[m0 + i];
     }
     if (i < ntri) {
-        float4 b = tnorm[i], c = tcen[i];
+        float4 b = tnorm[t0 + i], c = tcen[t0 + i];
         if (trinor) { trinor[3 * i] = b.x; trinor[3 * i + 1] = b.y; trinor[3 * i + 2] = b.z; }
         if (tricen) { tricen[3 * i] = c.x; tricen[3 * i + 1] = c.y; tricen[3 * i + 2] = c.z; }
     }
 }
 
-__global__ void fk_cast_cells(int ncell, const double* __restrict__ a, const double* __restrict__ v,
+__global__ void fk_cast_cells(int ncell, int c0, const double* __restrict__ a, const double* __restrict__ v,
                               float* __restrict__ area, float* __restrict__ vol) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
-    if (area) area[c] = (float)a[c];
-    if (vol) vol[c] = (float)v[c];
+    if (area) area[c] = (float)a[c0 + c];
+    if (vol) vol[c] = (float)v[c0 + c];
 }
 
 __global__ void fk_count_stats(int n, const int* __restrict__ cnt, unsigned long long* __restrict__ sum,
@@ -832,20 +998,58 @@ __global__ void fk_count_stats(int n, const int* __restrict__ cnt, unsigned long
     }
 }
 
+// system index of the slots (set-up, slot = id)
+__global__ void fk_fill_sys(int n, const SysInfo* __restrict__ sys, int nsys, int* __restrict__ sysid) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) sysid[i] = find_sys(sys, nsys, (unsigned)i);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 
+namespace {
+
+// Membrane topology of one system as given (local, 1-based), until set-up.
+struct HostCells {
+    bool set = false;
+    int ncell = 0, ntri = 0, nedge = 0;
+    std::vector<int> tri, edge, betri, celltab;
+    std::vector<float> shear, bend, hl, hg, hv;
+};
+
+// Device copy of the dynamic state (snapshots for captured steps and the
+// autotuner).
+struct StateCopy {
+    SlotArrays s{};
+    float4* mpos = nullptr;
+    int4* mnthro = nullptr;
+    long long* dstep = nullptr;
+    bool have = false;
+};
+
+}  // namespace
+
 struct GcFused {
     GcParams p;
-    GcGrid lgrid;                 // list/sort grid (cubes >= rc + skin)
-    GcGrid mgrid;                 // membrane aggregation grid (cubes >= MaxCut)
-    float skin = 0.1f;
+    int nsys = 1;
+    std::vector<SysInfo> hsys;
+    std::vector<GcSystemDesc> desc;
+    std::vector<HostCells> hcells;
+    std::vector<int> c0, t0;       // first cell and triangle of each system (after set-up)
+    std::vector<char> sys_loaded;
+    SysInfo* dsys = nullptr;
+    int K = 0, Kagg = 0;           // cubes of all list grids, of all aggregation grids
+    float skin_rel = 0.1f;         // skin in units of CutRadius
+    float skin = 0.1f;             // skin length
     int n = 0, cap = 0, block = kBS;
     int noise_on = 1;
-    long long step = -1;          // index keying the noise of the latest step
+    bool compact = false;
+    bool graph = false;            // steps run as captured graphs
+    bool ens = false;              // kernels read the system table
+    long long step = -1;           // index keying the noise of the latest step
     long long rebuilds = 0, steps = 0;
     cudaStream_t st = 0;
     // slot arrays (current, and the permutation target)
@@ -856,21 +1060,37 @@ struct GcFused {
     int *keys = nullptr, *vals = nullptr;
     int *nbr = nullptr, *cnt = nullptr;
     size_t nbr_elems = 0;
-    bool compact = false;
     unsigned* cmask = nullptr;   // per-step bit mask of the acting list entries
+    size_t cmask_elems = 0;
     int* ccnt = nullptr;         // number of acting entries
     int mw = 0;                  // mask words per slot
     int* rebuild = nullptr;
-    int* h_rebuild = nullptr;     // pinned
     unsigned* flags = nullptr;
+    unsigned* oflag = nullptr;   // list overflow inside captured steps
     unsigned long long* stat_sum = nullptr;
     int* stat_max = nullptr;
-    // membranes
+    long long* dstep = nullptr;  // device step counter (ensembles, captured steps)
+    unsigned* nkey = nullptr;    // per-system noise key of the current step
+    unsigned long long* drebuilds = nullptr;   // rebuilds inside captured steps
+    // pinned words read back after steps: rebuild flag, overflow flag, device rebuild count
+    struct Pinned {
+        int rebuild;
+        unsigned oflag;
+        unsigned long long drebuilds;
+    }* h = nullptr;
+    unsigned long long drebuilds_seen = 0;
+    // counting-sort temporaries (owned, so a captured step can use them)
+    void* sortmem = nullptr;
+    size_t sortmem_bytes = 0;
+    int sort_n = 0, sort_K = 0;
+    GcSortBufs sb{};
+    // membranes (global indices over the ensemble)
     int ncell = 0, ntri = 0, nedge = 0, ncp = 0;
     int3* tri = nullptr;
     int6* edge = nullptr;
     int2* betri = nullptr;
     int* celltab = nullptr;
+    int *msys = nullptr, *cellsys = nullptr;
     float *shear = nullptr, *bend = nullptr, *hl = nullptr, *hg = nullptr, *hv = nullptr;
     float *l0 = nullptr, *lmax = nullptr, *perlen = nullptr, *hpow = nullptr, *hbend = nullptr, *refang = nullptr;
     float *tarea = nullptr, *reftarea = nullptr;
@@ -880,9 +1100,17 @@ struct GcFused {
     int4* mnthro = nullptr;
     float* parea = nullptr;
     int *mkeys = nullptr, *mvals = nullptr;
+    bool cells_adopted = false;   // membranes taken from the boundary entry points' buffers
     bool have_agg = false;
     bool setup_done = false;
-    bool loaded = false;
+    // captured steps
+    cudaStream_t gst = nullptr, gst2 = nullptr;
+    cudaGraph_t cg[2] = {};
+    cudaGraphExec_t gexec[2] = {};
+    bool graph_dirty = true;
+    long long kernels_step = 0, kernels_rebuild = 0;   // kernels per captured step and per rebuild body
+    StateCopy snap;    // state at the start of a captured gc_fused_step call
+    StateCopy tsnap;   // state at the start of an autotune
     // optional CUDA-event timing of the dominant kernels (fk_density, fk_force)
     bool profile = false;
     std::vector<cudaEvent_t> ev;   // pairs: density start/stop, force start/stop
@@ -916,48 +1144,123 @@ int stage_bytes(GcFused* f, size_t bytes) {
     return GC_OK;
 }
 
-int alloc_list(GcFused* f, int cap) {
-    size_t need = (size_t)((f->n + 31) / 32) * 32 * (size_t)cap;
-    if (f->nbr && need <= f->nbr_elems) {
-        f->cap = cap;
-        return GC_OK;
+void drop_graphs(GcFused* f) {
+    for (int d = 0; d < 2; ++d) {
+        if (f->gexec[d]) cudaGraphExecDestroy(f->gexec[d]);
+        if (f->cg[d]) cudaGraphDestroy(f->cg[d]);
+        f->gexec[d] = nullptr;
+        f->cg[d] = nullptr;
     }
-    if (f->nbr) cudaFree(f->nbr);
-    if (f->cmask) cudaFree(f->cmask);
-    f->nbr = nullptr;
-    f->cmask = nullptr;
-    GC_CUDA(cudaMalloc(&f->nbr, need * sizeof(int)), "fused: neighbour lists");
+    f->graph_dirty = true;
+}
+
+int alloc_list(GcFused* f, int cap) {
+    size_t rows = (size_t)((f->n + 31) / 32) * 32;
+    size_t need = rows * (size_t)cap;
+    if (!f->nbr || need > f->nbr_elems) {
+        if (f->nbr) cudaFree(f->nbr);
+        f->nbr = nullptr;
+        f->nbr_elems = 0;
+        GC_CUDA(cudaMalloc(&f->nbr, need * sizeof(int)), "fused: neighbour lists");
+        f->nbr_elems = need;
+        drop_graphs(f);
+    }
     f->mw = (cap + 31) / 32;
-    if (f->compact)
-        GC_CUDA(cudaMalloc(&f->cmask, (size_t)((f->n + 31) / 32) * 32 * f->mw * sizeof(unsigned)), "fused: masks");
-    f->nbr_elems = need;
+    if (f->compact) {
+        size_t mneed = rows * (size_t)f->mw;
+        if (!f->cmask || mneed > f->cmask_elems) {
+            if (f->cmask) cudaFree(f->cmask);
+            f->cmask = nullptr;
+            f->cmask_elems = 0;
+            GC_CUDA(cudaMalloc(&f->cmask, mneed * sizeof(unsigned)), "fused: masks");
+            f->cmask_elems = mneed;
+            drop_graphs(f);
+        }
+    }
+    if (f->cap != cap) drop_graphs(f);
     f->cap = cap;
     return GC_OK;
 }
 
+int ensure_sort_bufs(GcFused* f) {
+    int nn = f->n > f->ncp ? f->n : f->ncp;
+    int KK = f->K > f->Kagg ? f->K : f->Kagg;
+    if (f->sortmem && nn <= f->sort_n && KK <= f->sort_K) return GC_OK;
+    if (f->sortmem) cudaFree(f->sortmem);
+    f->sortmem = nullptr;
+    size_t bytes = gc_sort_bufs_bytes(nn, KK);
+    GC_CUDA(cudaMalloc(&f->sortmem, bytes), "fused: sort temporaries");
+    f->sortmem_bytes = bytes;
+    f->sort_n = nn;
+    f->sort_K = KK;
+    gc_sort_bufs_carve(f->sortmem, nn, KK, &f->sb);
+    drop_graphs(f);
+    return GC_OK;
+}
+
+// Per-system list grids (cubes at least rc + skin wide) and aggregation
+// grids, their global cube offsets, and the device copy of the table.
+int build_grids(GcFused* f) {
+    int K = 0, Kagg = 0;
+    for (int s = 0; s < f->nsys; ++s) {
+        SysInfo& S = f->hsys[s];
+        const GcSystemDesc& d = f->desc[s];
+        GC_TRY(gc_build_grid(d.bbox, d.consts.CutRadius + f->skin, d.periodic_mask, &S.g));
+        for (int a = 0; a < 3; ++a) S.invL[a] = 1.f / S.g.L[a];
+        S.cube0 = K;
+        K += S.g.ncells;
+        if (f->have_agg) {
+            GC_TRY(gc_build_grid(d.bbox, f->p.maxcut, d.periodic_mask, &S.mg));
+            S.mcube0 = Kagg;
+            Kagg += S.mg.ncells;
+        } else {
+            S.mg = S.g;
+            S.mcube0 = 0;
+        }
+    }
+    f->K = K;
+    f->Kagg = Kagg;
+    if (f->dsys)
+        GC_CUDA(cudaMemcpyAsync(f->dsys, f->hsys.data(), sizeof(SysInfo) * f->nsys, cudaMemcpyHostToDevice, f->st),
+                "fused: system table");
+    GC_TRY(ensure_sort_bufs(f));
+    drop_graphs(f);
+    return GC_OK;
+}
+
+int sync_dstep(GcFused* f) {
+    long long v = f->step;
+    GC_CUDA(cudaMemcpyAsync(f->dstep, &v, sizeof(v), cudaMemcpyHostToDevice, f->st), "fused: step counter");
+    GC_CUDA(cudaStreamSynchronize(f->st), "fused: step counter");
+    return GC_OK;
+}
+
+const SysInfo& s0(GcFused* f) { return f->hsys[0]; }
+
+// Re-sort and list build on the host-driven path (swaps the slot arrays;
+// grows the lists and rebuilds when a particle had more neighbours than the
+// lists hold).
 int rebuild_lists(GcFused* f) {
     const int n = f->n;
     const int nb = gc_blocks(n, f->block);
     cudaStream_t st = f->st;
-    fk_cellkey<<<nb, f->block, 0, st>>>(n, f->lgrid, f->a.pos, f->keys, f->vals);
+    fk_cellkey<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->a.pos, f->keys, f->vals);
     GC_CHECK_LAUNCH("fused: cube keys");
-    GC_TRY(gc_counting_sort(n, f->lgrid.ncells, f->keys, f->vals, st));
-    fk_permute<<<nb, f->block, 0, st>>>(n, f->lgrid, f->vals, f->a, f->b, f->refpos, f->slot_of);
+    GC_TRY(gc_counting_sort_bufs(n, f->K, f->keys, f->vals, f->sb, f->flags, st));
+    fk_permute<<<nb, f->block, 0, st>>>(n, f->dsys, f->vals, f->a, f->b, f->refpos, f->slot_of);
     GC_CHECK_LAUNCH("fused: permute");
     std::swap(f->a, f->b);
-    GcParams lp = f->p;
-    lp.g = f->lgrid;
+    drop_graphs(f);   // captured steps are bound to the old slot arrays
     float cut = f->p.rc + f->skin;
     float cut2 = cut * cut;
     for (int attempt = 0; attempt < 4; ++attempt) {
-        GC_CUDA(cudaMemsetAsync(f->flags, 0, sizeof(unsigned), st), "fused: flags");
-        fk_build_list<<<nb, f->block, 0, st>>>(n, lp, f->a.pos, gc_sort_starts(), f->nbr, f->cnt, f->cap, cut2,
-                                              f->flags);
+        GC_CUDA(cudaMemsetAsync(f->oflag, 0, sizeof(unsigned), st), "fused: flags");
+        fk_build_list<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->a.pos, f->sb.cnt, f->nbr, f->cnt, f->cap,
+                                              cut2, f->oflag);
         GC_CHECK_LAUNCH("fused: build lists");
-        unsigned h = 0;
-        GC_CUDA(cudaMemcpyAsync(&h, f->flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "fused: flags");
+        GC_CUDA(cudaMemcpyAsync(&f->h->oflag, f->oflag, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "fused: flags");
         GC_CUDA(cudaStreamSynchronize(st), "fused: flags");
-        if (!(h & GC_FLAG_CELL_OVERFLOW)) break;
+        if (!(f->h->oflag & GC_FLAG_CELL_OVERFLOW)) break;
         if (attempt == 3) return gc_fail(GC_EDEVICE, "fused: neighbour lists overflow %d entries", f->cap);
         // a particle had more neighbours than the list holds: grow and rebuild
         GC_TRY(alloc_list(f, f->cap * 2));
@@ -975,183 +1278,359 @@ cudaEvent_t prof_event(GcFused* f) {
     return f->ev[f->ev_used++];
 }
 
-void prof_mark(GcFused* f) {
+void prof_mark(GcFused* f, cudaStream_t st) {
     if (!f->profile) return;
     cudaEvent_t e = prof_event(f);
-    if (e) cudaEventRecord(e, f->st);
+    if (e) cudaEventRecord(e, st);
 }
 
-Box make_box(const GcGrid& g) {
-    Box b;
-    for (int a = 0; a < 3; ++a) {
-        b.L[a] = g.L[a];
-        b.invL[a] = 1.f / g.L[a];
+// ---- launches shared by the host-driven and the captured step --------------
+
+int launch_integrate(GcFused* f, cudaStream_t st, const GcParams& p) {
+    const int n = f->n, nb = gc_blocks(n, f->block);
+    float hs = 0.5f * f->skin * 0.99f;
+    if (f->ens)
+        fk_integrate<true><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vel, f->a.vh,
+                                                     f->a.vpred, f->a.force, f->refpos, f->a.nthro, hs * hs,
+                                                     f->rebuild, f->mpos, f->mnthro, f->flags);
+    else
+        fk_integrate<false><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vel, f->a.vh,
+                                                      f->a.vpred, f->a.force, f->refpos, f->a.nthro, hs * hs,
+                                                      f->rebuild, f->mpos, f->mnthro, f->flags);
+    GC_CHECK_LAUNCH("fused: integrate");
+    return GC_OK;
+}
+
+int launch_density(GcFused* f, cudaStream_t st, const GcParams& p, bool mark) {
+    const int n = f->n, nb = gc_blocks(n, f->block);
+    unsigned* cm = mark && f->compact ? f->cmask : nullptr;
+    int* cc = mark && f->compact ? f->ccnt : nullptr;
+    if (f->ens)
+        fk_density<true><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vpred, f->a.vh,
+                                                   f->dp, f->nbr, f->cnt, f->cap, cm, f->mw, cc);
+    else
+        fk_density<false><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vpred, f->a.vh,
+                                                    f->dp, f->nbr, f->cnt, f->cap, cm, f->mw, cc);
+    GC_CHECK_LAUNCH("fused: density");
+    return GC_OK;
+}
+
+int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p) {
+    if (f->ncell <= 0) return GC_OK;
+    GC_CUDA(cudaMemsetAsync(f->mforce, 0, (size_t)f->ncp * sizeof(float4), st), "fused: clear mforce");
+    GC_CUDA(cudaMemsetAsync(f->parea, 0, (size_t)f->ncp * sizeof(float), st), "fused: clear parea");
+    fk_mgeo<<<f->ncell, 256, 0, st>>>(p, f->dsys, f->cellsys, f->ncell, f->ntri, f->tri, f->betri, f->mpos, f->mnthro,
+                                     f->tarea, f->tnorm, f->tcen, f->reftarea, f->carea, f->cvol, f->crefarea,
+                                     f->crefvol, f->parea, 0, f->flags);
+    GC_CHECK_LAUNCH("fused: membrane geometry");
+    fk_medge<<<gc_blocks(f->nedge, f->block), f->block, 0, st>>>(p, f->dsys, f->msys, f->nedge, f->edge, f->mpos,
+                                                                 f->mnthro, f->lmax, f->perlen, f->hpow, f->refang,
+                                                                 f->hbend, f->mforce, f->flags);
+    GC_CHECK_LAUNCH("fused: membrane edges");
+    fk_mtri<<<f->ncell, 256, 0, st>>>(p, f->dsys, f->cellsys, f->ncell, f->betri, f->tri, f->mpos, f->mnthro,
+                                     f->reftarea, f->hl, f->hg, f->hv, f->carea, f->cvol, f->crefarea, f->crefvol,
+                                     f->mforce, f->ntri);
+    GC_CHECK_LAUNCH("fused: membrane triangles");
+    if (f->have_agg) {
+        fk_mkey<<<gc_blocks(f->ncp, f->block), f->block, 0, st>>>(f->ncp, f->dsys, f->msys, f->mpos, f->mkeys,
+                                                                  f->mvals);
+        GC_CHECK_LAUNCH("fused: aggregation keys");
+        GC_TRY(gc_counting_sort_bufs(f->ncp, f->Kagg, f->mkeys, f->mvals, f->sb, f->flags, st));
+        fk_magg<<<gc_blocks(f->ncp, f->block), f->block, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mvals, f->sb.cnt,
+                                                                  f->mpos, f->celltab, f->parea, f->magg, f->mforce);
+        GC_CHECK_LAUNCH("fused: aggregation");
     }
-    b.pmask = g.pmask;
-    return b;
+    return GC_OK;
 }
 
+template <bool COMPACT>
+void force_launch(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
+    const int n = f->n, nb = gc_blocks(n, f->block);
+    const float4* mf = f->ncell > 0 ? f->mforce : nullptr;
+    const int* c = COMPACT ? f->ccnt : f->cnt;
+    const unsigned* cm = COMPACT ? f->cmask : nullptr;
+    if (f->ens)
+        fk_force<COMPACT, true><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos,
+                                                          f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel, f->nbr,
+                                                          c, f->cap, cm, f->mw, mf, drive);
+    else
+        fk_force<COMPACT, false><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos,
+                                                           f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel, f->nbr,
+                                                           c, f->cap, cm, f->mw, mf, drive);
+}
+
+int launch_force(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
+    if (f->compact) force_launch<true>(f, st, p, drive);
+    else force_launch<false>(f, st, p, drive);
+    GC_CHECK_LAUNCH("fused: force");
+    return GC_OK;
+}
+
+bool any_bound2(const GcFused* f) {
+    for (const SysInfo& S : f->hsys)
+        if (S.fl > S.b2) return true;
+    return false;
+}
+
+int launch_wallvel(GcFused* f, cudaStream_t st, const GcParams& p) {
+    if (!any_bound2(f)) return GC_OK;
+    const int n = f->n, nb = gc_blocks(n, f->block);
+    if (f->ens)
+        fk_wallvel<true><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vel, f->a.vh, f->nbr,
+                                                   f->cnt, f->cap);
+    else
+        fk_wallvel<false><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vel, f->a.vh,
+                                                    f->nbr, f->cnt, f->cap);
+    GC_CHECK_LAUNCH("fused: wall velocity");
+    return GC_OK;
+}
+
+int launch_step_begin(GcFused* f, cudaStream_t st) {
+    fk_step_begin<<<1, 256, 0, st>>>(f->nsys, f->dsys, f->dstep, f->nkey, f->rebuild);
+    GC_CHECK_LAUNCH("fused: step prologue");
+    return GC_OK;
+}
+
+// One step on the host-driven path: the host reads the rebuild flag.
 int one_step(GcFused* f, int drive) {
-    const int n = f->n;
-    const Box B = make_box(f->lgrid);
-    const int nb = gc_blocks(n, f->block);
     cudaStream_t st = f->st;
     f->step += 1;
-    f->p.noise_key = noise_key(f->p.seed, (uint64_t)f->step);
     GcParams p = f->p;
-    p.g = f->lgrid;
-    float hs = 0.5f * f->skin * 0.99f;
-    GC_CUDA(cudaMemsetAsync(f->rebuild, 0, sizeof(int), st), "fused: flag");
-    fk_integrate<<<nb, f->block, 0, st>>>(n, p, f->a.pos, f->a.vel, f->a.vh, f->a.vpred, f->a.force, f->refpos,
-                                         f->a.nthro, hs * hs, f->rebuild, f->mpos, f->mnthro, f->flags);
-    GC_CHECK_LAUNCH("fused: integrate");
-    GC_CUDA(cudaMemcpyAsync(f->h_rebuild, f->rebuild, sizeof(int), cudaMemcpyDeviceToHost, st), "fused: flag");
+    p.noise_key = noise_key(p.seed, (uint64_t)f->step);
+    if (f->ens) GC_TRY(launch_step_begin(f, st));
+    else GC_CUDA(cudaMemsetAsync(f->rebuild, 0, sizeof(int), st), "fused: flag");
+    GC_TRY(launch_integrate(f, st, p));
+    GC_CUDA(cudaMemcpyAsync(&f->h->rebuild, f->rebuild, sizeof(int), cudaMemcpyDeviceToHost, st), "fused: flag");
     GC_CUDA(cudaStreamSynchronize(st), "fused: flag");
-    if (*f->h_rebuild) GC_TRY(rebuild_lists(f));
-    prof_mark(f);
-    fk_density<<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->nbr, f->cnt, f->cap,
-                                       f->compact ? f->cmask : nullptr, f->mw, f->compact ? f->ccnt : nullptr);
-    GC_CHECK_LAUNCH("fused: density");
-    prof_mark(f);
-    if (f->ncell > 0) {
-        GC_CUDA(cudaMemsetAsync(f->mforce, 0, (size_t)f->ncp * sizeof(float4), st), "fused: clear mforce");
-        GC_CUDA(cudaMemsetAsync(f->parea, 0, (size_t)f->ncp * sizeof(float), st), "fused: clear parea");
-        fk_mgeo<<<f->ncell, 256, 0, st>>>(p, f->ncell, f->ntri, f->tri, f->betri, f->mpos, f->mnthro, f->tarea,
-                                         f->tnorm, f->tcen, f->reftarea, f->carea, f->cvol, f->crefarea, f->crefvol,
-                                         f->parea, 0, f->flags);
-        GC_CHECK_LAUNCH("fused: membrane geometry");
-        fk_medge<<<gc_blocks(f->nedge, f->block), f->block, 0, st>>>(p, f->nedge, f->edge, f->mpos, f->mnthro,
-                                                                     f->lmax, f->perlen, f->hpow, f->refang,
-                                                                     f->hbend, f->mforce, f->flags);
-        GC_CHECK_LAUNCH("fused: membrane edges");
-        fk_mtri<<<f->ncell, 256, 0, st>>>(p, f->ncell, f->betri, f->tri, f->mpos, f->mnthro, f->reftarea, f->hl,
-                                         f->hg, f->hv, f->carea, f->cvol, f->crefarea, f->crefvol, f->mforce,
-                                         f->ntri);
-        GC_CHECK_LAUNCH("fused: membrane triangles");
-        if (f->have_agg) {
-            fk_mkey<<<gc_blocks(f->ncp, f->block), f->block, 0, st>>>(f->ncp, f->mgrid, f->mpos, f->mkeys, f->mvals);
-            GC_CHECK_LAUNCH("fused: aggregation keys");
-            GC_TRY(gc_counting_sort(f->ncp, f->mgrid.ncells, f->mkeys, f->mvals, st));
-            fk_magg<<<gc_blocks(f->ncp, f->block), f->block, 0, st>>>(f->ncp, p, f->mgrid, f->mvals, gc_sort_starts(),
-                                                                      f->mpos, f->celltab, f->parea, f->magg,
-                                                                      f->mforce);
-            GC_CHECK_LAUNCH("fused: aggregation");
-        }
-    }
-    prof_mark(f);
-    if (f->compact)
-        fk_force<true><<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
-                                               f->nbr, f->ccnt, f->cap, f->cmask, f->mw,
-                                               f->ncell > 0 ? f->mforce : nullptr, drive);
-    else
-        fk_force<false><<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
-                                                f->nbr, f->cnt, f->cap, nullptr, 0,
-                                                f->ncell > 0 ? f->mforce : nullptr, drive);
-    GC_CHECK_LAUNCH("fused: force");
-    prof_mark(f);
-    if (p.nF > p.nB2) {
-        fk_wallvel<<<nb, f->block, 0, st>>>(n, p, B, f->a.pos, f->a.vel, f->a.vh, f->nbr, f->cnt, f->cap);
-        GC_CHECK_LAUNCH("fused: wall velocity");
-    }
+    if (f->h->rebuild) GC_TRY(rebuild_lists(f));
+    prof_mark(f, st);
+    GC_TRY(launch_density(f, st, p, true));
+    prof_mark(f, st);
+    GC_TRY(launch_membranes(f, st, p));
+    prof_mark(f, st);
+    GC_TRY(launch_force(f, st, p, drive));
+    prof_mark(f, st);
+    GC_TRY(launch_wallvel(f, st, p));
     f->steps++;
     return GC_OK;
 }
 
-}  // namespace
+// ---- captured steps -------------------------------------------------------
 
-extern "C" {
-
-int gc_fused_create(const Structconst* consts, const float* bbox6, int periodic_mask, int noise_on,
-                    const GcFusedOptions* opt, GcFused** out) {
-    if (!consts || !bbox6 || !out) return gc_fail(GC_EINVAL, "fused_create: NULL argument");
-    if (periodic_mask < 0 || periodic_mask > 7) return gc_fail(GC_EINVAL, "fused_create: bad periodic mask");
-    const Structconst& c = *consts;
-    if (!(c.nBound2Start <= c.nFluidStart && c.nFluidStart <= c.nCellStart && c.nCellStart + c.nCellPar == c.nTotalPar))
-        return gc_fail(GC_EINVAL, "fused_create: inconsistent type boundaries");
-    if (c.nTotalPar >= (1u << 30)) return gc_fail(GC_EINVAL, "fused_create: too many particles");
-    GcFused* f = new GcFused();
-    f->st = gc_state().stream;
-    int rc = gc_params_from(c, noise_on, &f->p);   // the same builder as the boundary entry points
-    if (rc != GC_OK) {
-        delete f;
-        return rc;
-    }
-    f->noise_on = noise_on ? 1 : 0;
-    if (opt) {
-        f->compact = opt->compact != 0;
-        if (opt->skin > 0.f) f->skin = opt->skin;
-        if (opt->block == 64 || opt->block == 128 || opt->block == kMaxBS) f->block = opt->block;
-    }
-    int e = gc_build_grid(bbox6, c.CutRadius + f->skin, periodic_mask, &f->lgrid);
-    GcGrid g0;
-    if (e == GC_OK) e = gc_build_grid(bbox6, c.CutRadius, periodic_mask, &g0);
-    if (e != GC_OK) {
-        delete f;
-        return e;
-    }
-    // the per-step predicate uses the box of the rc grid (same lo, hi, L)
-    f->p.g = f->lgrid;
-    f->n = (int)c.nTotalPar;
-    int n = f->n;
-    int ok = GC_OK;
-    SlotArrays* sa[2] = {&f->a, &f->b};
-    for (SlotArrays* s : sa) {
-        if (ok == GC_OK) ok = falloc(f, &s->pos, n);
-        if (ok == GC_OK) ok = falloc(f, &s->vel, n);
-        if (ok == GC_OK) ok = falloc(f, &s->vpred, n);
-        if (ok == GC_OK) ok = falloc(f, &s->vh, n);
-        if (ok == GC_OK) ok = falloc(f, &s->force, n);
-        if (ok == GC_OK) ok = falloc(f, &s->nthro, n);
-    }
-    if (ok == GC_OK) ok = falloc(f, &f->refpos, n);
-    if (ok == GC_OK) ok = falloc(f, &f->dp, n);
-    if (ok == GC_OK) ok = falloc(f, &f->slot_of, n);
-    if (ok == GC_OK) ok = falloc(f, &f->keys, n);
-    if (ok == GC_OK) ok = falloc(f, &f->vals, n);
-    if (ok == GC_OK) ok = falloc(f, &f->cnt, n);
-    if (ok == GC_OK) ok = falloc(f, &f->ccnt, n);
-    if (ok == GC_OK) ok = falloc(f, &f->rebuild, 1);
-    if (ok == GC_OK) ok = falloc(f, &f->flags, 1);
-    if (ok == GC_OK) ok = falloc(f, &f->stat_sum, 1);
-    if (ok == GC_OK) ok = falloc(f, &f->stat_max, 1);
-    if (ok == GC_OK && cudaMallocHost(&f->h_rebuild, sizeof(int)) != cudaSuccess)
-        ok = gc_fail(GC_ENOMEM, "fused: pinned flag");
-    if (ok == GC_OK) {
-        // list capacity: expected neighbours within rc + skin at the mean
-        // density, with room for membranes and fluctuations
-        double vol = (double)f->lgrid.L[0] * f->lgrid.L[1] * f->lgrid.L[2];
-        double dens = n / vol;
-        double cutr = c.CutRadius + f->skin;
-        int capn = (int)(2.0 * 4.18879 * cutr * cutr * cutr * dens) + 32;
-        if (opt && opt->list_capacity > 0) capn = opt->list_capacity;
-        capn = (capn + 7) & ~7;
-        ok = alloc_list(f, capn);
-    }
-    if (ok != GC_OK) {
-        gc_fused_destroy(f);
-        return ok;
-    }
-    GC_CUDA(cudaMemsetAsync(f->flags, 0, sizeof(unsigned), f->st), "fused: flags");
-    *out = f;
+// The rebuild of a captured step: the same sort and list build as
+// rebuild_lists, permuting into the spare arrays and copying back, with the
+// list capacity fixed (an overflow raises oflag, which the host checks after
+// the call's steps and recovers from).
+int launch_rebuild_body(GcFused* f, cudaStream_t st) {
+    const int n = f->n, nb = gc_blocks(n, f->block);
+    fk_cellkey<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->a.pos, f->keys, f->vals);
+    GC_CHECK_LAUNCH("fused: cube keys");
+    GC_TRY(gc_counting_sort_bufs(n, f->K, f->keys, f->vals, f->sb, f->flags, st));
+    fk_permute<<<nb, f->block, 0, st>>>(n, f->dsys, f->vals, f->a, f->b, f->refpos, f->slot_of);
+    GC_CHECK_LAUNCH("fused: permute");
+    fk_copy_slots<<<nb, f->block, 0, st>>>(n, f->b, f->a);
+    GC_CHECK_LAUNCH("fused: copy slots");
+    float cut = f->p.rc + f->skin;
+    fk_build_list<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->a.pos, f->sb.cnt, f->nbr, f->cnt, f->cap,
+                                          cut * cut, f->oflag);
+    GC_CHECK_LAUNCH("fused: build lists");
     return GC_OK;
 }
 
-int gc_fused_set_cells(GcFused* f, int ncell, int ntri, int nedge, const int* tri, const int* edge, const int* betri,
-                       const int* celltab, const float* shearmod, const float* bendmod, const float* hlarea,
-                       const float* hgarea, const float* hvol) {
-    if (!f) return gc_fail(GC_EINVAL, "fused_set_cells: NULL handle");
-    if (ncell <= 0) return GC_OK;
-    int ncp = (int)f->p.nCP;
-    if (ncp <= 0 || ntri <= 0 || nedge <= 0) return gc_fail(GC_EINVAL, "fused_set_cells: empty topology");
-    for (int k = 0; k < 3 * ntri; ++k)
-        if (tri[k] < 1 || tri[k] > ncp) return gc_fail(GC_EINVAL, "fused_set_cells: triangle index out of range");
-    for (int k = 0; k < nedge; ++k)
-        for (int q = 0; q < 4; ++q)
-            if (edge[6 * k + q] < 1 || edge[6 * k + q] > ncp)
-                return gc_fail(GC_EINVAL, "fused_set_cells: edge index out of range");
-    for (int k = 0; k < ncell; ++k)
-        if (betri[2 * k] < 0 || betri[2 * k + 1] >= ntri || betri[2 * k + 1] < betri[2 * k])
-            return gc_fail(GC_EINVAL, "fused_set_cells: bad triangle range of cell %d", k);
+int capture_step(GcFused* f, int drive) {
+    if (!f->gst) GC_CUDA(cudaStreamCreateWithFlags(&f->gst, cudaStreamNonBlocking), "fused: capture stream");
+    if (!f->gst2) GC_CUDA(cudaStreamCreateWithFlags(&f->gst2, cudaStreamNonBlocking), "fused: capture stream");
+    cudaStream_t st = f->gst;
+    GcParams p = f->p;
+    unsigned long long l0 = gc_launch_count();
+    GC_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "fused: begin capture");
+    int rc = GC_OK;
+    cudaGraph_t g = nullptr;
+    cudaGraphConditionalHandle hcond = 0;
+    long long main_kernels = 0, body_kernels = 0;
+    do {
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps);
+        if (e != cudaSuccess) { rc = gc_cuda_fail(e, "fused: capture info"); break; }
+        e = cudaGraphConditionalHandleCreate(&hcond, g, 0, cudaGraphCondAssignDefault);
+        if (e != cudaSuccess) { rc = gc_cuda_fail(e, "fused: conditional handle"); break; }
+        if ((rc = launch_step_begin(f, st)) != GC_OK) break;
+        if ((rc = launch_integrate(f, st, p)) != GC_OK) break;
+        fk_set_cond<<<1, 1, 0, st>>>(hcond, f->rebuild, f->drebuilds);
+        gc_count_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) { rc = gc_cuda_fail(e, "fused: set condition"); break; }
+        e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps);
+        if (e != cudaSuccess) { rc = gc_cuda_fail(e, "fused: capture info"); break; }
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = hcond;
+        np.conditional.type = cudaGraphCondTypeIf;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        e = cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np);
+        if (e != cudaSuccess) { rc = gc_cuda_fail(e, "fused: conditional node"); break; }
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+        if (e != cudaSuccess) { rc = gc_cuda_fail(e, "fused: capture dependencies"); break; }
+        unsigned long long lb = gc_launch_count();
+        e = cudaStreamBeginCaptureToGraph(f->gst2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) { rc = gc_cuda_fail(e, "fused: capture rebuild"); break; }
+        rc = launch_rebuild_body(f, f->gst2);
+        cudaGraph_t body_out = nullptr;
+        e = cudaStreamEndCapture(f->gst2, &body_out);
+        if (rc != GC_OK) break;
+        if (e != cudaSuccess) { rc = gc_cuda_fail(e, "fused: end rebuild capture"); break; }
+        body_kernels = (long long)(gc_launch_count() - lb);
+        if ((rc = launch_density(f, st, p, true)) != GC_OK) break;
+        if ((rc = launch_membranes(f, st, p)) != GC_OK) break;
+        if ((rc = launch_force(f, st, p, drive)) != GC_OK) break;
+        if ((rc = launch_wallvel(f, st, p)) != GC_OK) break;
+    } while (0);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    unsigned long long l1 = gc_launch_count();
+    gc_add_launches(-(long long)(l1 - l0));   // capturing launches nothing
+    if (rc != GC_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return gc_cuda_fail(e, "fused: end capture");
+    main_kernels = (long long)(l1 - l0) - body_kernels;
+    cudaGraphExec_t ex = nullptr;
+    e = cudaGraphInstantiate(&ex, graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        return gc_cuda_fail(e, "fused: instantiate step graph");
+    }
+    f->cg[drive] = graph;
+    f->gexec[drive] = ex;
+    f->kernels_step = main_kernels;
+    f->kernels_rebuild = body_kernels;
+    return GC_OK;
+}
+
+int alloc_copy(GcFused* f, StateCopy* c) {
+    if (c->have) return GC_OK;
+    size_t n = f->n;
+    GC_TRY(falloc(f, &c->s.pos, n));
+    GC_TRY(falloc(f, &c->s.vel, n));
+    GC_TRY(falloc(f, &c->s.vpred, n));
+    GC_TRY(falloc(f, &c->s.vh, n));
+    GC_TRY(falloc(f, &c->s.force, n));
+    GC_TRY(falloc(f, &c->s.nthro, n));
+    if (f->a.sys) GC_TRY(falloc(f, &c->s.sys, n));
+    if (f->ncp > 0) {
+        GC_TRY(falloc(f, &c->mpos, f->ncp));
+        GC_TRY(falloc(f, &c->mnthro, f->ncp));
+    }
+    GC_TRY(falloc(f, &c->dstep, 1));
+    c->have = true;
+    return GC_OK;
+}
+
+int copy_state(GcFused* f, const SlotArrays& src, const float4* mpos, const int4* mnt, const long long* dstep,
+               SlotArrays& dst, float4* dmpos, int4* dmnt, long long* ddstep) {
+    cudaStream_t st = f->st;
+    size_t n = f->n;
+    auto cp = [&](void* d, const void* s, size_t bytes) -> int {
+        if (!d || !s || !bytes) return GC_OK;
+        GC_CUDA(cudaMemcpyAsync(d, s, bytes, cudaMemcpyDeviceToDevice, st), "fused: state copy");
+        return GC_OK;
+    };
+    GC_TRY(cp(dst.pos, src.pos, n * 16));
+    GC_TRY(cp(dst.vel, src.vel, n * 16));
+    GC_TRY(cp(dst.vpred, src.vpred, n * 16));
+    GC_TRY(cp(dst.vh, src.vh, n * 16));
+    GC_TRY(cp(dst.force, src.force, n * 16));
+    GC_TRY(cp(dst.nthro, src.nthro, n * 16));
+    GC_TRY(cp(dst.sys, src.sys, n * 4));
+    GC_TRY(cp(dmpos, mpos, (size_t)f->ncp * 16));
+    GC_TRY(cp(dmnt, mnt, (size_t)f->ncp * 16));
+    GC_TRY(cp(ddstep, dstep, 8));
+    return GC_OK;
+}
+
+int save_state(GcFused* f, StateCopy* c) {
+    GC_TRY(alloc_copy(f, c));
+    return copy_state(f, f->a, f->mpos, f->mnthro, f->dstep, c->s, c->mpos, c->mnthro, c->dstep);
+}
+
+int restore_state(GcFused* f, StateCopy* c) {
+    return copy_state(f, c->s, c->mpos, c->mnthro, c->dstep, f->a, f->mpos, f->mnthro, f->dstep);
+}
+
+// Re-sort and rebuild outside a step, then recompute what the outputs show
+// (density and pressure in the new slot order, membrane forces).
+int refresh(GcFused* f) {
+    GC_TRY(rebuild_lists(f));
+    GcParams p = f->p;
+    p.noise_key = noise_key(p.seed, (uint64_t)(f->step < 0 ? 0 : f->step));
+    GC_TRY(launch_density(f, f->st, p, true));
+    GC_TRY(launch_membranes(f, f->st, p));
+    return GC_OK;
+}
+
+// Fresh lists with room for growth, then capture.
+int prepare_graph(GcFused* f, int drive) {
+    if (f->graph_dirty) {
+        GC_TRY(rebuild_lists(f));
+        // capacity for captured steps: the longest list now plus a margin
+        GC_CUDA(cudaMemsetAsync(f->stat_max, 0, sizeof(int), f->st), "fused: stats");
+        GC_CUDA(cudaMemsetAsync(f->stat_sum, 0, sizeof(unsigned long long), f->st), "fused: stats");
+        fk_count_stats<<<gc_blocks(f->n, 256), 256, 0, f->st>>>(f->n, f->cnt, f->stat_sum, f->stat_max);
+        GC_CHECK_LAUNCH("fused: stats");
+        int mx = 0;
+        GC_CUDA(cudaMemcpyAsync(&mx, f->stat_max, 4, cudaMemcpyDeviceToHost, f->st), "fused: stats");
+        GC_CUDA(cudaStreamSynchronize(f->st), "fused: stats");
+        int want = ((int)(1.25 * mx) + 16 + 7) & ~7;
+        if (want > f->cap) {
+            GC_TRY(alloc_list(f, want));
+            GC_TRY(rebuild_lists(f));
+        }
+        GC_TRY(sync_dstep(f));
+        drop_graphs(f);
+        f->graph_dirty = false;
+    }
+    if (!f->gexec[drive]) GC_TRY(capture_step(f, drive));
+    return GC_OK;
+}
+
+int graph_steps(GcFused* f, int nsteps, int drive) {
+    if (nsteps <= 0) return GC_OK;
+    long long step0 = f->step;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        GC_TRY(prepare_graph(f, drive));
+        GC_TRY(save_state(f, &f->snap));
+        GC_CUDA(cudaMemsetAsync(f->oflag, 0, sizeof(unsigned), f->st), "fused: flags");
+        for (int k = 0; k < nsteps; ++k)
+            GC_CUDA(cudaGraphLaunch(f->gexec[drive], f->st), "fused: launch step graph");
+        GC_CUDA(cudaMemcpyAsync(&f->h->oflag, f->oflag, sizeof(unsigned), cudaMemcpyDeviceToHost, f->st), "fused: flags");
+        GC_CUDA(cudaMemcpyAsync(&f->h->drebuilds, f->drebuilds, 8, cudaMemcpyDeviceToHost, f->st), "fused: flags");
+        GC_CUDA(cudaStreamSynchronize(f->st), "fused: step graphs");
+        long long nreb = (long long)(f->h->drebuilds - f->drebuilds_seen);
+        f->drebuilds_seen = f->h->drebuilds;
+        gc_add_launches(f->kernels_step * nsteps + f->kernels_rebuild * nreb);
+        if (!(f->h->oflag & GC_FLAG_CELL_OVERFLOW)) {
+            f->step = step0 + nsteps;
+            f->steps += nsteps;
+            f->rebuilds += nreb;
+            return GC_OK;
+        }
+        // a list overflowed: go back to the state before these steps, grow
+        // the lists and run them again
+        GC_TRY(restore_state(f, &f->snap));
+        f->step = step0;
+        GC_TRY(alloc_list(f, f->cap + f->cap / 2 + 8));
+        f->graph_dirty = true;
+    }
+    return gc_fail(GC_EDEVICE, "fused: neighbour lists keep overflowing in captured steps (capacity %d)", f->cap);
+}
+
+// ---- membranes: device arrays ---------------------------------------------
+
+int alloc_cells(GcFused* f, int ncell, int ntri, int nedge, int ncp) {
     f->ncell = ncell;
     f->ntri = ntri;
     f->nedge = nedge;
@@ -1168,42 +1647,310 @@ int gc_fused_set_cells(GcFused* f, int ncell, int ntri, int nedge, const int* tr
     GC_TRY(falloc(f, &f->tcen, ntri));
     double** c1[] = {&f->carea, &f->cvol, &f->crefarea, &f->crefvol};
     for (double** q : c1) GC_TRY(falloc(f, q, ncell));
-    GC_TRY(falloc(f, &f->mpos, ncp));
     GC_TRY(falloc(f, &f->mforce, ncp));
     GC_TRY(falloc(f, &f->magg, ncp));
-    GC_TRY(falloc(f, &f->mnthro, ncp));
     GC_TRY(falloc(f, &f->parea, ncp));
     GC_TRY(falloc(f, &f->mkeys, ncp));
     GC_TRY(falloc(f, &f->mvals, ncp));
-    cudaStream_t st = f->st;
-    GC_CUDA(cudaMemcpyAsync(f->tri, tri, (size_t)ntri * 12, cudaMemcpyHostToDevice, st), "fused: tri");
-    GC_CUDA(cudaMemcpyAsync(f->edge, edge, (size_t)nedge * 24, cudaMemcpyHostToDevice, st), "fused: edge");
-    GC_CUDA(cudaMemcpyAsync(f->betri, betri, (size_t)ncell * 8, cudaMemcpyHostToDevice, st), "fused: betri");
-    GC_CUDA(cudaMemcpyAsync(f->celltab, celltab, (size_t)ncp * 4, cudaMemcpyHostToDevice, st), "fused: celltab");
-    GC_CUDA(cudaMemcpyAsync(f->shear, shearmod, (size_t)nedge * 4, cudaMemcpyHostToDevice, st), "fused: shear");
-    GC_CUDA(cudaMemcpyAsync(f->bend, bendmod, (size_t)nedge * 4, cudaMemcpyHostToDevice, st), "fused: bend");
-    GC_CUDA(cudaMemcpyAsync(f->hl, hlarea, (size_t)ntri * 4, cudaMemcpyHostToDevice, st), "fused: hl");
-    GC_CUDA(cudaMemcpyAsync(f->hg, hgarea, (size_t)ntri * 4, cudaMemcpyHostToDevice, st), "fused: hg");
-    GC_CUDA(cudaMemcpyAsync(f->hv, hvol, (size_t)ntri * 4, cudaMemcpyHostToDevice, st), "fused: hv");
-    GC_CUDA(cudaMemsetAsync(f->magg, 0, (size_t)ncp * sizeof(float4), st), "fused: magg");
-    if (f->p.De != 0.f && f->p.maxcut > 0.f) {
-        float bb[6] = {f->lgrid.lo[0], f->lgrid.hi[0], f->lgrid.lo[1], f->lgrid.hi[1], f->lgrid.lo[2], f->lgrid.hi[2]};
-        GC_TRY(gc_build_grid(bb, f->p.maxcut, f->lgrid.pmask, &f->mgrid));
-        f->have_agg = true;
-    }
-    GC_CUDA(cudaStreamSynchronize(st), "fused: set cells");
+    GC_CUDA(cudaMemsetAsync(f->magg, 0, (size_t)ncp * sizeof(float4), f->st), "fused: magg");
+    f->have_agg = f->p.De != 0.f && f->p.maxcut > 0.f;
     return GC_OK;
 }
 
-int gc_fused_load(GcFused* f, const float* pos, const float* vel, const float* velhalf, const float* force,
-                  const int* nthro, int from_device) {
-    if (!f || !pos) return gc_fail(GC_EINVAL, "fused_load: NULL argument");
+// Concatenates the systems' topologies with global vertex, triangle and cell
+// offsets and uploads them.
+int finalize_cells(GcFused* f) {
+    int ncell = 0, ntri = 0, nedge = 0;
+    f->c0.assign(f->nsys, 0);
+    f->t0.assign(f->nsys, 0);
+    for (int s = 0; s < f->nsys; ++s) {
+        f->c0[s] = ncell;
+        f->t0[s] = ntri;
+        const HostCells& h = f->hcells[s];
+        if (!h.set) continue;
+        ncell += h.ncell;
+        ntri += h.ntri;
+        nedge += h.nedge;
+    }
+    if (ncell == 0) return GC_OK;
+    std::vector<int> tri(3 * (size_t)ntri), edge(6 * (size_t)nedge), betri(2 * (size_t)ncell), celltab(f->ncp, -1);
+    std::vector<float> shear(nedge), bend(nedge), hl(ntri), hg(ntri), hv(ntri);
+    std::vector<int> msys(f->ncp, 0), cellsys(ncell, 0);
+    size_t ot = 0, oe = 0, oc = 0;
+    for (int s = 0; s < f->nsys; ++s) {
+        const HostCells& h = f->hcells[s];
+        const SysInfo& S = f->hsys[s];
+        int m0 = (int)S.m0, ncps = (int)(S.end - S.cs);
+        for (int v = 0; v < ncps; ++v) msys[m0 + v] = s;
+        if (!h.set) continue;
+        int t0 = f->t0[s], c0 = f->c0[s];
+        for (int k = 0; k < 3 * h.ntri; ++k) tri[3 * ot + k] = h.tri[k] + m0;
+        for (int k = 0; k < h.nedge; ++k) {
+            for (int q = 0; q < 4; ++q) edge[6 * (oe + k) + q] = h.edge[6 * k + q] + m0;
+            for (int q = 4; q < 6; ++q) edge[6 * (oe + k) + q] = h.edge[6 * k + q] + t0;
+        }
+        for (int k = 0; k < h.ncell; ++k) {
+            betri[2 * (oc + k)] = h.betri[2 * k] + t0;
+            betri[2 * (oc + k) + 1] = h.betri[2 * k + 1] + t0;
+            cellsys[oc + k] = s;
+        }
+        for (int v = 0; v < ncps; ++v) celltab[m0 + v] = h.celltab[v] + c0;
+        std::copy(h.shear.begin(), h.shear.end(), shear.begin() + oe);
+        std::copy(h.bend.begin(), h.bend.end(), bend.begin() + oe);
+        std::copy(h.hl.begin(), h.hl.end(), hl.begin() + ot);
+        std::copy(h.hg.begin(), h.hg.end(), hg.begin() + ot);
+        std::copy(h.hv.begin(), h.hv.end(), hv.begin() + ot);
+        ot += h.ntri;
+        oe += h.nedge;
+        oc += h.ncell;
+    }
+    GC_TRY(alloc_cells(f, ncell, ntri, nedge, f->ncp));
+    cudaStream_t st = f->st;
+    auto up = [&](void* d, const void* s, size_t bytes) -> int {
+        GC_CUDA(cudaMemcpyAsync(d, s, bytes, cudaMemcpyHostToDevice, st), "fused: upload cells");
+        return GC_OK;
+    };
+    GC_TRY(up(f->tri, tri.data(), tri.size() * 4));
+    GC_TRY(up(f->edge, edge.data(), edge.size() * 4));
+    GC_TRY(up(f->betri, betri.data(), betri.size() * 4));
+    GC_TRY(up(f->celltab, celltab.data(), celltab.size() * 4));
+    GC_TRY(up(f->shear, shear.data(), shear.size() * 4));
+    GC_TRY(up(f->bend, bend.data(), bend.size() * 4));
+    GC_TRY(up(f->hl, hl.data(), hl.size() * 4));
+    GC_TRY(up(f->hg, hg.data(), hg.size() * 4));
+    GC_TRY(up(f->hv, hv.data(), hv.size() * 4));
+    if (f->nsys > 1) {
+        GC_TRY(falloc(f, &f->msys, f->ncp));
+        GC_TRY(falloc(f, &f->cellsys, ncell));
+        GC_TRY(up(f->msys, msys.data(), msys.size() * 4));
+        GC_TRY(up(f->cellsys, cellsys.data(), cellsys.size() * 4));
+    }
+    GC_CUDA(cudaStreamSynchronize(st), "fused: upload cells");   // the host vectors go out of scope
+    return GC_OK;
+}
+
+bool same_physics(const Structconst& a, const Structconst& b) {
+    return a.CutRadius == b.CutRadius && a.Mass == b.Mass && a.SoundSpeed1 == b.SoundSpeed1 &&
+           a.SoundSpeed2 == b.SoundSpeed2 && a.DenInit == b.DenInit && a.VVsigma == b.VVsigma &&
+           a.ShearVis == b.ShearVis && a.BulkVis == b.BulkVis && a.TimeStep == b.TimeStep &&
+           a.surEnergy == b.surEnergy && a.MaxCut == b.MaxCut && a.zeroLen == b.zeroLen && a.scaFac == b.scaFac &&
+           a.Temp == b.Temp;
+}
+
+int check_sys(GcFused* f, int sys, const char* what) {
+    if (!f) return gc_fail(GC_EINVAL, "%s: NULL handle", what);
+    if (sys < 0 || sys >= f->nsys) return gc_fail(GC_EINVAL, "%s: system %d outside 0..%d", what, sys, f->nsys - 1);
+    return GC_OK;
+}
+
+int apply_options(GcFused* f, const GcFusedOptions* opt) {
+    if (!opt) return GC_OK;
+    if (opt->block != 0 && opt->block != 64 && opt->block != 128 && opt->block != kMaxBS)
+        return gc_fail(GC_EINVAL, "fused: block %d is not 64, 128 or 256", opt->block);
+    if (opt->skin < 0.f || opt->skin > 1.f) return gc_fail(GC_EINVAL, "fused: skin %g outside [0, 1] rc", opt->skin);
+    if (opt->skin > 0.f) f->skin_rel = opt->skin;
+    if (opt->block) f->block = opt->block;
+    f->compact = opt->compact != 0;
+    f->graph = opt->graph != 0;
+    return GC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFusedOptions* opt, GcFused** out) {
+    if (!d || !out) return gc_fail(GC_EINVAL, "ensemble_create: NULL argument");
+    if (nsys < 1) return gc_fail(GC_EINVAL, "ensemble_create: %d systems", nsys);
+    unsigned long long ntot = 0, ncp = 0;
+    for (int s = 0; s < nsys; ++s) {
+        const Structconst& c = d[s].consts;
+        if (d[s].periodic_mask < 0 || d[s].periodic_mask > 7)
+            return gc_fail(GC_EINVAL, "ensemble_create: system %d: bad periodic mask", s);
+        if (!(c.nBound2Start <= c.nFluidStart && c.nFluidStart <= c.nCellStart &&
+              c.nCellStart + c.nCellPar == c.nTotalPar))
+            return gc_fail(GC_EINVAL, "ensemble_create: system %d: inconsistent type boundaries", s);
+        if (!same_physics(c, d[0].consts))
+            return gc_fail(GC_EINVAL, "ensemble_create: system %d has other physics than system 0 (only counts, "
+                                      "iSeed and ConstExtForce may differ)", s);
+        ntot += c.nTotalPar;
+        ncp += c.nCellPar;
+    }
+    if (ntot == 0) return gc_fail(GC_EINVAL, "ensemble_create: no particles");
+    if (ntot >= (1ull << 30)) return gc_fail(GC_EINVAL, "ensemble_create: too many particles");
+    GcFused* f = new GcFused();
+    f->st = gc_state().stream;
+    int rc = gc_params_from(d[0].consts, noise_on, &f->p);   // the same builder as the boundary entry points
+    if (rc == GC_OK) rc = apply_options(f, opt);
+    if (rc != GC_OK) {
+        delete f;
+        return rc;
+    }
+    f->nsys = nsys;
+    f->desc.assign(d, d + nsys);
+    f->hcells.resize(nsys);
+    f->sys_loaded.assign(nsys, 0);
+    f->noise_on = noise_on ? 1 : 0;
+    f->n = (int)ntot;
+    f->ncp = (int)ncp;
+    f->p.nT = (unsigned)ntot;
+    f->p.nCP = (unsigned)ncp;
+    f->skin = f->skin_rel * f->p.rc;
+    f->ens = nsys > 1 || f->graph;
+    f->hsys.resize(nsys);
+    unsigned id0 = 0, m0 = 0;
+    for (int s = 0; s < nsys; ++s) {
+        const Structconst& c = d[s].consts;
+        SysInfo& S = f->hsys[s];
+        memset(&S, 0, sizeof(S));
+        S.seed = (uint64_t)c.iSeed;
+        S.id0 = id0;
+        S.b2 = id0 + c.nBound2Start;
+        S.fl = id0 + c.nFluidStart;
+        S.cs = id0 + c.nCellStart;
+        S.end = id0 + c.nTotalPar;
+        S.m0 = m0;
+        S.gx = c.ConstExtForce;
+        id0 += c.nTotalPar;
+        m0 += c.nCellPar;
+    }
     const int n = f->n;
+    int ok = GC_OK;
+    SlotArrays* sa[2] = {&f->a, &f->b};
+    for (SlotArrays* s : sa) {
+        if (ok == GC_OK) ok = falloc(f, &s->pos, n);
+        if (ok == GC_OK) ok = falloc(f, &s->vel, n);
+        if (ok == GC_OK) ok = falloc(f, &s->vpred, n);
+        if (ok == GC_OK) ok = falloc(f, &s->vh, n);
+        if (ok == GC_OK) ok = falloc(f, &s->force, n);
+        if (ok == GC_OK) ok = falloc(f, &s->nthro, n);
+        if (ok == GC_OK && nsys > 1) ok = falloc(f, &s->sys, n);
+    }
+    if (ok == GC_OK) ok = falloc(f, &f->refpos, n);
+    if (ok == GC_OK) ok = falloc(f, &f->dp, n);
+    if (ok == GC_OK) ok = falloc(f, &f->slot_of, n);
+    if (ok == GC_OK) ok = falloc(f, &f->keys, n > f->ncp ? n : f->ncp);
+    if (ok == GC_OK) ok = falloc(f, &f->vals, n > f->ncp ? n : f->ncp);
+    if (ok == GC_OK) ok = falloc(f, &f->cnt, n);
+    if (ok == GC_OK) ok = falloc(f, &f->ccnt, n);
+    if (ok == GC_OK) ok = falloc(f, &f->rebuild, 1);
+    if (ok == GC_OK) ok = falloc(f, &f->flags, 1);
+    if (ok == GC_OK) ok = falloc(f, &f->oflag, 1);
+    if (ok == GC_OK) ok = falloc(f, &f->stat_sum, 1);
+    if (ok == GC_OK) ok = falloc(f, &f->stat_max, 1);
+    if (ok == GC_OK) ok = falloc(f, &f->dstep, 1);
+    if (ok == GC_OK) ok = falloc(f, &f->nkey, nsys);
+    if (ok == GC_OK) ok = falloc(f, &f->drebuilds, 1);
+    if (ok == GC_OK) ok = falloc(f, &f->dsys, nsys);
+    if (ok == GC_OK && f->ncp > 0) ok = falloc(f, &f->mpos, f->ncp);
+    if (ok == GC_OK && f->ncp > 0) ok = falloc(f, &f->mnthro, f->ncp);
+    if (ok == GC_OK && cudaMallocHost(&f->h, sizeof(GcFused::Pinned)) != cudaSuccess)
+        ok = gc_fail(GC_ENOMEM, "fused: pinned words");
+    if (ok == GC_OK) ok = build_grids(f);
+    if (ok == GC_OK) {
+        // list capacity: expected neighbours within rc + skin at the largest
+        // mean density of a system, with room for membranes and fluctuations
+        double dens = 0.0;
+        for (int s = 0; s < nsys; ++s) {
+            const GcGrid& g = f->hsys[s].g;
+            double vol = (double)g.L[0] * g.L[1] * g.L[2];
+            double ds = d[s].consts.nTotalPar / vol;
+            if (ds > dens) dens = ds;
+        }
+        double cutr = f->p.rc + f->skin;
+        int capn = (int)(2.0 * 4.18879 * cutr * cutr * cutr * dens) + 32;
+        if (opt && opt->list_capacity > 0) capn = opt->list_capacity;
+        capn = (capn + 7) & ~7;
+        ok = alloc_list(f, capn);
+    }
+    if (ok == GC_OK) {
+        f->h->drebuilds = 0;
+        if (cudaMemsetAsync(f->flags, 0, sizeof(unsigned), f->st) != cudaSuccess ||
+            cudaMemsetAsync(f->drebuilds, 0, 8, f->st) != cudaSuccess ||
+            cudaMemsetAsync(f->dstep, 0xff, 8, f->st) != cudaSuccess)   // -1
+            ok = gc_fail(GC_ECUDA, "fused: clear counters");
+    }
+    if (ok != GC_OK) {
+        gc_fused_destroy(f);
+        return ok;
+    }
+    *out = f;
+    return GC_OK;
+}
+
+int gc_fused_create(const Structconst* consts, const float* bbox6, int periodic_mask, int noise_on,
+                    const GcFusedOptions* opt, GcFused** out) {
+    if (!consts || !bbox6 || !out) return gc_fail(GC_EINVAL, "fused_create: NULL argument");
+    if (periodic_mask < 0 || periodic_mask > 7) return gc_fail(GC_EINVAL, "fused_create: bad periodic mask");
+    GcSystemDesc d;
+    memset(&d, 0, sizeof(d));
+    d.consts = *consts;
+    memcpy(d.bbox, bbox6, sizeof(d.bbox));
+    d.periodic_mask = periodic_mask;
+    return gc_ensemble_create(1, &d, noise_on, opt, out);
+}
+
+int gc_ensemble_size(GcFused* f, int* nsys, long long* nparticles) {
+    if (!f) return gc_fail(GC_EINVAL, "ensemble_size: NULL handle");
+    if (nsys) *nsys = f->nsys;
+    if (nparticles) *nparticles = f->n;
+    return GC_OK;
+}
+
+int gc_ensemble_set_cells(GcFused* f, int sys, int ncell, int ntri, int nedge, const int* tri, const int* edge,
+                          const int* betri, const int* celltab, const float* shearmod, const float* bendmod,
+                          const float* hlarea, const float* hgarea, const float* hvol) {
+    GC_TRY(check_sys(f, sys, "set_cells"));
+    if (f->setup_done || f->cells_adopted) return gc_fail(GC_ESTATE, "set_cells: call before gc_fused_setup");
+    if (ncell <= 0) return GC_OK;
+    int ncp = (int)f->desc[sys].consts.nCellPar;
+    if (ncp <= 0 || ntri <= 0 || nedge <= 0) return gc_fail(GC_EINVAL, "set_cells: empty topology");
+    if (!tri || !edge || !betri || !celltab || !shearmod || !bendmod || !hlarea || !hgarea || !hvol)
+        return gc_fail(GC_EINVAL, "set_cells: NULL array");
+    for (int k = 0; k < 3 * ntri; ++k)
+        if (tri[k] < 1 || tri[k] > ncp) return gc_fail(GC_EINVAL, "set_cells: triangle index out of range");
+    for (int k = 0; k < nedge; ++k)
+        for (int q = 0; q < 4; ++q)
+            if (edge[6 * k + q] < 1 || edge[6 * k + q] > ncp)
+                return gc_fail(GC_EINVAL, "set_cells: edge index out of range");
+    for (int k = 0; k < ncell; ++k)
+        if (betri[2 * k] < 0 || betri[2 * k + 1] >= ntri || betri[2 * k + 1] < betri[2 * k])
+            return gc_fail(GC_EINVAL, "set_cells: bad triangle range of cell %d", k);
+    HostCells& h = f->hcells[sys];
+    h.set = true;
+    h.ncell = ncell;
+    h.ntri = ntri;
+    h.nedge = nedge;
+    h.tri.assign(tri, tri + 3 * (size_t)ntri);
+    h.edge.assign(edge, edge + 6 * (size_t)nedge);
+    h.betri.assign(betri, betri + 2 * (size_t)ncell);
+    h.celltab.assign(celltab, celltab + ncp);
+    h.shear.assign(shearmod, shearmod + nedge);
+    h.bend.assign(bendmod, bendmod + nedge);
+    h.hl.assign(hlarea, hlarea + ntri);
+    h.hg.assign(hgarea, hgarea + ntri);
+    h.hv.assign(hvol, hvol + ntri);
+    return GC_OK;
+}
+
+int gc_fused_set_cells(GcFused* f, int ncell, int ntri, int nedge, const int* tri, const int* edge, const int* betri,
+                       const int* celltab, const float* shearmod, const float* bendmod, const float* hlarea,
+                       const float* hgarea, const float* hvol) {
+    if (!f) return gc_fail(GC_EINVAL, "fused_set_cells: NULL handle");
+    if (f->nsys != 1) return gc_fail(GC_EINVAL, "fused_set_cells: an ensemble takes gc_ensemble_set_cells");
+    return gc_ensemble_set_cells(f, 0, ncell, ntri, nedge, tri, edge, betri, celltab, shearmod, bendmod, hlarea,
+                                 hgarea, hvol);
+}
+
+// Loads the ids [id_base, id_base + count) from host or device arrays.
+static int load_range(GcFused* f, unsigned id_base, int count, const float* pos, const float* vel,
+                      const float* velhalf, const float* force, const int* nthro, int from_device) {
+    if (count <= 0) return GC_OK;
     cudaStream_t st = f->st;
     const float *dx = pos, *dv = vel, *dh = velhalf, *df = force;
     const int* dn = nthro;
     if (!from_device) {
-        size_t b3 = (size_t)n * 12;
+        size_t b3 = (size_t)count * 12;
         GC_TRY(stage_bytes(f, 5 * b3));
         char* s = (char*)f->stage;
         cudaError_t ce = cudaSuccess;
@@ -1220,77 +1967,93 @@ int gc_fused_load(GcFused* f, const float* pos, const float* vel, const float* v
         dn = (const int*)up(nthro, 4 * b3);
         GC_CUDA(ce, "fused_load: upload");
     }
-    if (f->setup_done) {
-        fk_load_keep<<<gc_blocks(n, f->block), f->block, 0, st>>>(n, f->p, f->slot_of, dx, dv, dh, df, dn, f->a.pos,
-                                                                  f->a.vel, f->a.vh, f->a.force, f->a.nthro,
-                                                                  f->ncell > 0 ? f->mpos : nullptr, f->mnthro);
-        GC_CHECK_LAUNCH("fused: load in slot order");
-        return GC_OK;
-    }
-    fk_load<<<gc_blocks(n, f->block), f->block, 0, st>>>(n, f->p, dx, dv, dh, df, dn, f->a.pos, f->a.vel, f->a.vh,
-                                                        f->a.force, f->a.nthro);
+    int keep = f->setup_done ? 1 : 0;
+    fk_load<<<gc_blocks(count, f->block), f->block, 0, st>>>(count, id_base, f->dsys, f->nsys, keep, dx, dv, dh, df,
+                                                             dn, f->slot_of, f->a.pos, f->a.vel, f->a.vh, f->a.force,
+                                                             f->a.nthro, keep && f->ncell > 0 ? f->mpos : nullptr,
+                                                             f->mnthro);
     GC_CHECK_LAUNCH("fused: load");
-    GC_CUDA(cudaMemcpyAsync(f->a.vpred, f->a.vel, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st),
-            "fused: load");
-    // membrane-ordered positions for the set-up geometry
-    if (f->ncell > 0) {
-        // gather through the identity order of a fresh load: slot = id
-        GC_CUDA(cudaMemcpyAsync(f->mpos, f->a.pos + f->p.nC, (size_t)f->ncp * sizeof(float4),
-                                cudaMemcpyDeviceToDevice, st), "fused: load");
-        GC_CUDA(cudaMemcpyAsync(f->mnthro, f->a.nthro + f->p.nC, (size_t)f->ncp * sizeof(int4),
-                                cudaMemcpyDeviceToDevice, st), "fused: load");
-    }
-    f->loaded = true;
-    f->setup_done = false;
+    if (!from_device) GC_CUDA(cudaStreamSynchronize(st), "fused_load");   // the staging buffer is reused
+    return GC_OK;
+}
+
+int gc_ensemble_load(GcFused* f, int sys, const float* pos, const float* vel, const float* velhalf, const float* force,
+                     const int* nthro, int from_device) {
+    GC_TRY(check_sys(f, sys, "load"));
+    if (!pos) return gc_fail(GC_EINVAL, "load: NULL positions");
+    const SysInfo& S = f->hsys[sys];
+    GC_TRY(load_range(f, S.id0, (int)(S.end - S.id0), pos, vel, velhalf, force, nthro, from_device));
+    f->sys_loaded[sys] = 1;
+    return GC_OK;
+}
+
+int gc_fused_load(GcFused* f, const float* pos, const float* vel, const float* velhalf, const float* force,
+                  const int* nthro, int from_device) {
+    if (!f || !pos) return gc_fail(GC_EINVAL, "fused_load: NULL argument");
+    GC_TRY(load_range(f, 0, f->n, pos, vel, velhalf, force, nthro, from_device));
+    for (int s = 0; s < f->nsys; ++s) f->sys_loaded[s] = 1;
     return GC_OK;
 }
 
 int gc_fused_setup(GcFused* f) {
-    if (!f || !f->loaded) return gc_fail(GC_ESTATE, "fused_setup: load state first");
+    if (!f) return gc_fail(GC_EINVAL, "fused_setup: NULL handle");
+    for (int s = 0; s < f->nsys; ++s)
+        if (!f->sys_loaded[s]) return gc_fail(GC_ESTATE, "fused_setup: load the state of system %d first", s);
+    if (f->setup_done) return gc_fail(GC_ESTATE, "fused_setup: already set up");
     cudaStream_t st = f->st;
+    GC_TRY(finalize_cells(f));
+    GC_TRY(build_grids(f));   // the aggregation grids exist once the cells are known
+    const int n = f->n;
+    GC_CUDA(cudaMemcpyAsync(f->a.vpred, f->a.vel, (size_t)n * sizeof(float4), cudaMemcpyDeviceToDevice, st),
+            "fused: predicted velocity");
+    if (f->a.sys) {
+        fk_fill_sys<<<gc_blocks(n, 256), 256, 0, st>>>(n, f->dsys, f->nsys, f->a.sys);
+        GC_CHECK_LAUNCH("fused: system of each slot");
+    }
     GcParams p = f->p;
-    p.g = f->lgrid;
     if (f->ncell > 0) {
+        fk_gather_mpos<<<gc_blocks(f->ncp, 256), 256, 0, st>>>(f->ncp, f->dsys, f->msys, f->slot_of, f->a.pos,
+                                                              f->a.nthro, f->mpos, f->mnthro);
+        GC_CHECK_LAUNCH("fused: membrane positions");
         GC_CUDA(cudaMemsetAsync(f->parea, 0, (size_t)f->ncp * sizeof(float), st), "fused: parea");
-        fk_mgeo<<<f->ncell, 256, 0, st>>>(p, f->ncell, f->ntri, f->tri, f->betri, f->mpos, f->mnthro, f->tarea,
-                                         f->tnorm, f->tcen, f->reftarea, f->carea, f->cvol, f->crefarea, f->crefvol,
-                                         f->parea, 1, f->flags);
+        fk_mgeo<<<f->ncell, 256, 0, st>>>(p, f->dsys, f->cellsys, f->ncell, f->ntri, f->tri, f->betri, f->mpos,
+                                         f->mnthro, f->tarea, f->tnorm, f->tcen, f->reftarea, f->carea, f->cvol,
+                                         f->crefarea, f->crefvol, f->parea, 1, f->flags);
         GC_CHECK_LAUNCH("fused: set-up geometry");
         fk_mech_setup<<<gc_blocks(f->nedge, f->block), f->block, 0, st>>>(
-            p, f->nedge, f->edge, f->mpos, f->mnthro, f->shear, f->bend, f->l0, f->lmax, f->perlen, f->hpow,
-            f->hbend, f->refang, f->flags);
+            p, f->dsys, f->msys, f->nedge, f->edge, f->mpos, f->mnthro, f->shear, f->bend, f->l0, f->lmax, f->perlen,
+            f->hpow, f->hbend, f->refang, f->flags);
         GC_CHECK_LAUNCH("fused: set-up mechanics");
     }
+    f->step = -1;
+    GC_TRY(sync_dstep(f));
     GC_TRY(rebuild_lists(f));
     // density and pressure of the loaded state (the reference has them from
     // DenInit until the first step recomputes them)
-    fk_density<<<gc_blocks(f->n, f->block), f->block, 0, st>>>(f->n, p, make_box(f->lgrid), f->a.pos, f->a.vpred,
-                                                               f->a.vh, f->dp, f->nbr, f->cnt, f->cap, nullptr, 0,
-                                                               nullptr);
-    GC_CHECK_LAUNCH("fused: set-up density");
+    GC_TRY(launch_density(f, st, p, false));
     f->setup_done = true;
-    f->step = -1;
     return GC_OK;
 }
 
 int gc_fused_step(GcFused* f, int nsteps, int drive_on) {
     if (!f || !f->setup_done) return gc_fail(GC_ESTATE, "fused_step: call gc_fused_setup first");
-    for (int k = 0; k < nsteps; ++k) GC_TRY(one_step(f, drive_on));
+    if (nsteps < 0) return gc_fail(GC_EINVAL, "fused_step: nsteps < 0");
+    int drive = drive_on ? 1 : 0;
+    if (f->graph && !f->profile) return graph_steps(f, nsteps, drive);
+    for (int k = 0; k < nsteps; ++k) GC_TRY(one_step(f, drive));
     return GC_OK;
 }
 
-int gc_fused_store(GcFused* f, float* pos, float* vel, float* rho, float* press, float* force, float* velhalf,
-                   int* nthro, int to_device) {
-    if (!f) return gc_fail(GC_EINVAL, "fused_store: NULL handle");
-    const int n = f->n;
+static int store_range(GcFused* f, unsigned id_base, int count, float* pos, float* vel, float* rho, float* press,
+                       float* force, float* velhalf, int* nthro, int to_device) {
+    if (count <= 0) return GC_OK;
     cudaStream_t st = f->st;
     float *x = pos, *v = vel, *r = rho, *pr = press, *fo = force, *vh = velhalf;
     int* nt = nthro;
-    size_t b3 = (size_t)n * 12, b1 = (size_t)n * 4;
-    char* s = nullptr;
+    size_t b3 = (size_t)count * 12, b1 = (size_t)count * 4;
     if (!to_device) {
         GC_TRY(stage_bytes(f, 5 * b3 + 2 * b1));
-        s = (char*)f->stage;
+        char* s = (char*)f->stage;
         x = pos ? (float*)(s) : nullptr;
         v = vel ? (float*)(s + b3) : nullptr;
         fo = force ? (float*)(s + 2 * b3) : nullptr;
@@ -1299,8 +2062,9 @@ int gc_fused_store(GcFused* f, float* pos, float* vel, float* rho, float* press,
         r = rho ? (float*)(s + 5 * b3) : nullptr;
         pr = press ? (float*)(s + 5 * b3 + b1) : nullptr;
     }
-    fk_store<<<gc_blocks(n, f->block), f->block, 0, st>>>(n, f->p, f->a.pos, f->a.vel, f->a.vh, f->a.force, f->dp,
-                                                         f->a.nthro, x, v, r, pr, fo, vh, nt);
+    fk_store<<<gc_blocks(count, f->block), f->block, 0, st>>>(count, id_base, f->p, f->slot_of, f->a.pos, f->a.vel,
+                                                              f->a.vh, f->a.force, f->dp, f->a.nthro, x, v, r, pr, fo,
+                                                              vh, nt);
     GC_CHECK_LAUNCH("fused: store");
     if (!to_device) {
         if (pos) GC_CUDA(cudaMemcpyAsync(pos, x, b3, cudaMemcpyDeviceToHost, st), "fused_store");
@@ -1315,47 +2079,90 @@ int gc_fused_store(GcFused* f, float* pos, float* vel, float* rho, float* press,
     return GC_OK;
 }
 
-int gc_fused_store_cells(GcFused* f, float* area, float* vol, float* defforce, float* aggforce, float* trinordir,
-                         float* tricenter, float* pararea, int to_device) {
-    if (!f) return gc_fail(GC_EINVAL, "fused_store_cells: NULL handle");
-    if (f->ncell <= 0) return GC_OK;
+int gc_fused_store(GcFused* f, float* pos, float* vel, float* rho, float* press, float* force, float* velhalf,
+                   int* nthro, int to_device) {
+    if (!f) return gc_fail(GC_EINVAL, "fused_store: NULL handle");
+    return store_range(f, 0, f->n, pos, vel, rho, press, force, velhalf, nthro, to_device);
+}
+
+int gc_ensemble_store(GcFused* f, int sys, float* pos, float* vel, float* rho, float* press, float* force,
+                      float* velhalf, int* nthro, int to_device) {
+    GC_TRY(check_sys(f, sys, "store"));
+    const SysInfo& S = f->hsys[sys];
+    return store_range(f, S.id0, (int)(S.end - S.id0), pos, vel, rho, press, force, velhalf, nthro, to_device);
+}
+
+// Membrane outputs of cells [c0, c0 + nc), vertices [m0, m0 + nv),
+// triangles [t0, t0 + nt).
+static int store_cells_range(GcFused* f, int c0, int nc, int m0, int nv, int t0, int nt, float* area, float* vol,
+                             float* defforce, float* aggforce, float* trinordir, float* tricenter, float* pararea,
+                             int to_device) {
+    if (f->ncell <= 0 || nc <= 0) return GC_OK;
     cudaStream_t st = f->st;
-    size_t nc = f->ncell, ncp = f->ncp, nt = f->ntri;
     float *a = area, *vo = vol, *df = defforce, *ag = aggforce, *tn = trinordir, *tc = tricenter, *pa = pararea;
+    size_t snc = nc, snv = nv, snt = nt;
     if (!to_device) {
-        GC_TRY(stage_bytes(f, 4 * (2 * nc + 3 * ncp + 3 * ncp + 3 * nt + 3 * nt + ncp) + 64));
+        GC_TRY(stage_bytes(f, 4 * (2 * snc + 3 * snv + 3 * snv + 3 * snt + 3 * snt + snv) + 64));
         char* s = (char*)f->stage;
         size_t off = 0;
         auto take = [&](size_t cnt) { float* q = (float*)(s + off); off += 4 * cnt; return q; };
-        a = take(nc); vo = take(nc); df = take(3 * ncp); ag = take(3 * ncp); tn = take(3 * nt); tc = take(3 * nt);
-        pa = take(ncp);
+        a = take(snc); vo = take(snc); df = take(3 * snv); ag = take(3 * snv); tn = take(3 * snt); tc = take(3 * snt);
+        pa = take(snv);
     }
-    fk_cast_cells<<<gc_blocks(nc, 128), 128, 0, st>>>((int)nc, f->carea, f->cvol, a, vo);
+    fk_cast_cells<<<gc_blocks(nc, 128), 128, 0, st>>>(nc, c0, f->carea, f->cvol, a, vo);
     GC_CHECK_LAUNCH("fused: store cells");
-    size_t m = ncp > nt ? ncp : nt;
-    fk_store_cells<<<gc_blocks(m, 128), 128, 0, st>>>((int)ncp, (int)nt, f->mforce, f->magg, f->parea, f->tnorm,
-                                                     f->tcen, df, ag, pa, tn, tc, f->have_agg ? 1 : 0);
+    int m = nv > nt ? nv : nt;
+    fk_store_cells<<<gc_blocks(m, 128), 128, 0, st>>>(nv, m0, nt, t0, f->mforce, f->magg, f->parea, f->tnorm, f->tcen,
+                                                     df, ag, pa, tn, tc, f->have_agg ? 1 : 0);
     GC_CHECK_LAUNCH("fused: store cells");
     if (!to_device) {
-        if (area) GC_CUDA(cudaMemcpyAsync(area, a, 4 * nc, cudaMemcpyDeviceToHost, st), "store cells");
-        if (vol) GC_CUDA(cudaMemcpyAsync(vol, vo, 4 * nc, cudaMemcpyDeviceToHost, st), "store cells");
-        if (defforce) GC_CUDA(cudaMemcpyAsync(defforce, df, 12 * ncp, cudaMemcpyDeviceToHost, st), "store cells");
-        if (aggforce) GC_CUDA(cudaMemcpyAsync(aggforce, ag, 12 * ncp, cudaMemcpyDeviceToHost, st), "store cells");
-        if (trinordir) GC_CUDA(cudaMemcpyAsync(trinordir, tn, 12 * nt, cudaMemcpyDeviceToHost, st), "store cells");
-        if (tricenter) GC_CUDA(cudaMemcpyAsync(tricenter, tc, 12 * nt, cudaMemcpyDeviceToHost, st), "store cells");
-        if (pararea) GC_CUDA(cudaMemcpyAsync(pararea, pa, 4 * ncp, cudaMemcpyDeviceToHost, st), "store cells");
+        if (area) GC_CUDA(cudaMemcpyAsync(area, a, 4 * snc, cudaMemcpyDeviceToHost, st), "store cells");
+        if (vol) GC_CUDA(cudaMemcpyAsync(vol, vo, 4 * snc, cudaMemcpyDeviceToHost, st), "store cells");
+        if (defforce) GC_CUDA(cudaMemcpyAsync(defforce, df, 12 * snv, cudaMemcpyDeviceToHost, st), "store cells");
+        if (aggforce) GC_CUDA(cudaMemcpyAsync(aggforce, ag, 12 * snv, cudaMemcpyDeviceToHost, st), "store cells");
+        if (trinordir) GC_CUDA(cudaMemcpyAsync(trinordir, tn, 12 * snt, cudaMemcpyDeviceToHost, st), "store cells");
+        if (tricenter) GC_CUDA(cudaMemcpyAsync(tricenter, tc, 12 * snt, cudaMemcpyDeviceToHost, st), "store cells");
+        if (pararea) GC_CUDA(cudaMemcpyAsync(pararea, pa, 4 * snv, cudaMemcpyDeviceToHost, st), "store cells");
         GC_CUDA(cudaStreamSynchronize(st), "store cells");
     }
     return GC_OK;
 }
 
-int gc_fused_cell_sums(GcFused* f, double* area, double* vol) {
-    if (!f) return gc_fail(GC_EINVAL, "fused_cell_sums: NULL handle");
-    if (f->ncell <= 0) return GC_OK;
-    GC_CUDA(cudaMemcpyAsync(area, f->carea, 8 * (size_t)f->ncell, cudaMemcpyDeviceToHost, f->st), "cell sums");
-    GC_CUDA(cudaMemcpyAsync(vol, f->cvol, 8 * (size_t)f->ncell, cudaMemcpyDeviceToHost, f->st), "cell sums");
+int gc_fused_store_cells(GcFused* f, float* area, float* vol, float* defforce, float* aggforce, float* trinordir,
+                         float* tricenter, float* pararea, int to_device) {
+    if (!f) return gc_fail(GC_EINVAL, "fused_store_cells: NULL handle");
+    return store_cells_range(f, 0, f->ncell, 0, f->ncp, 0, f->ntri, area, vol, defforce, aggforce, trinordir,
+                             tricenter, pararea, to_device);
+}
+
+int gc_ensemble_store_cells(GcFused* f, int sys, float* area, float* vol, float* defforce, float* aggforce,
+                            float* trinordir, float* tricenter, float* pararea, int to_device) {
+    GC_TRY(check_sys(f, sys, "store_cells"));
+    if (!f->setup_done) return gc_fail(GC_ESTATE, "store_cells: call gc_fused_setup first");
+    const HostCells& h = f->hcells[sys];
+    if (!h.set) return GC_OK;
+    const SysInfo& S = f->hsys[sys];
+    return store_cells_range(f, f->c0[sys], h.ncell, (int)S.m0, (int)(S.end - S.cs), f->t0[sys], h.ntri, area, vol,
+                             defforce, aggforce, trinordir, tricenter, pararea, to_device);
+}
+
+static int cell_sums_range(GcFused* f, int c0, int nc, double* area, double* vol) {
+    if (f->ncell <= 0 || nc <= 0) return GC_OK;
+    if (area) GC_CUDA(cudaMemcpyAsync(area, f->carea + c0, 8 * (size_t)nc, cudaMemcpyDeviceToHost, f->st), "cell sums");
+    if (vol) GC_CUDA(cudaMemcpyAsync(vol, f->cvol + c0, 8 * (size_t)nc, cudaMemcpyDeviceToHost, f->st), "cell sums");
     GC_CUDA(cudaStreamSynchronize(f->st), "cell sums");
     return GC_OK;
+}
+
+int gc_fused_cell_sums(GcFused* f, double* area, double* vol) {
+    if (!f) return gc_fail(GC_EINVAL, "fused_cell_sums: NULL handle");
+    return cell_sums_range(f, 0, f->ncell, area, vol);
+}
+
+int gc_ensemble_cell_sums(GcFused* f, int sys, double* area, double* vol) {
+    GC_TRY(check_sys(f, sys, "cell_sums"));
+    if (!f->setup_done || !f->hcells[sys].set) return GC_OK;
+    return cell_sums_range(f, f->c0[sys], f->hcells[sys].ncell, area, vol);
 }
 
 int gc_fused_stats(GcFused* f, long long* rebuilds, long long* steps, int* list_capacity, double* mean_neighbors,
@@ -1414,20 +2221,200 @@ int gc_fused_profile_read(GcFused* f, double* density_ms, double* force_ms, long
     return GC_OK;
 }
 
+int gc_fused_get_options(GcFused* f, GcFusedOptions* opt) {
+    if (!f || !opt) return gc_fail(GC_EINVAL, "fused_get_options: NULL argument");
+    memset(opt, 0, sizeof(*opt));
+    opt->skin = f->skin_rel;
+    opt->block = f->block;
+    opt->list_capacity = f->cap;
+    opt->compact = f->compact ? 1 : 0;
+    opt->graph = f->graph ? 1 : 0;
+    return GC_OK;
+}
+
+int gc_fused_set_options(GcFused* f, const GcFusedOptions* opt) {
+    if (!f || !opt) return gc_fail(GC_EINVAL, "fused_set_options: NULL argument");
+    float old_skin = f->skin_rel;
+    bool old_compact = f->compact;
+    int old_block = f->block;
+    GC_TRY(apply_options(f, opt));
+    f->skin = f->skin_rel * f->p.rc;
+    f->ens = f->nsys > 1 || f->graph;
+    bool regrid = f->skin_rel != old_skin;
+    if (regrid) GC_TRY(build_grids(f));
+    int cap = f->cap;
+    if (opt->list_capacity > cap) cap = (opt->list_capacity + 7) & ~7;
+    if (regrid) {
+        double grow = pow((f->p.rc + f->skin) / (f->p.rc + old_skin * f->p.rc), 3.0);
+        if (grow > 1.0) cap = ((int)(cap * grow) + 8) & ~7;
+    }
+    GC_TRY(alloc_list(f, cap));
+    if (f->compact != old_compact || f->block != old_block) drop_graphs(f);
+    if (f->setup_done) {
+        GC_TRY(sync_dstep(f));
+        if (regrid || f->compact != old_compact || opt->list_capacity > 0) GC_TRY(refresh(f));
+    }
+    return GC_OK;
+}
+
 int gc_fused_destroy(GcFused* f) {
     if (!f) return GC_OK;
     cudaStreamSynchronize(f->st);
+    for (int d = 0; d < 2; ++d) {
+        if (f->gexec[d]) cudaGraphExecDestroy(f->gexec[d]);
+        if (f->cg[d]) cudaGraphDestroy(f->cg[d]);
+    }
+    if (f->gst) cudaStreamDestroy(f->gst);
+    if (f->gst2) cudaStreamDestroy(f->gst2);
     for (cudaEvent_t e : f->ev) cudaEventDestroy(e);
     for (void* q : f->allocs) cudaFree(q);
     if (f->nbr) cudaFree(f->nbr);
     if (f->cmask) cudaFree(f->cmask);
+    if (f->sortmem) cudaFree(f->sortmem);
     if (f->stage) cudaFree(f->stage);
-    if (f->h_rebuild) cudaFreeHost(f->h_rebuild);
+    if (f->h) cudaFreeHost(f->h);
     delete f;
     return GC_OK;
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Autotuner: times short runs of candidate settings on the handle's own
+// state and keeps the fastest.  Every trial starts from the same saved state
+// and step index with freshly built lists, and the handle returns to that
+// state afterwards, so tuning does not change the trajectory that follows
+// (beyond the summation order the chosen settings imply).  The search is
+// coordinate-wise: skin (the cube size rc + skin of the list grid and the
+// list length), then threads per block, then per-step compaction of the
+// acting entries, then captured steps.  Choices are cached per size class
+// (ensemble or single system, particle count, density, membranes present,
+// noise) for the life of the process.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct TuneKey {
+    int nsys_class, n_class, dens_class, cells, noise;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(nsys_class, n_class, dens_class, cells, noise) <
+               std::tie(o.nsys_class, o.n_class, o.dens_class, o.cells, o.noise);
+    }
+};
+
+std::mutex g_tune_mutex;
+std::map<TuneKey, GcFusedOptions> g_tune_cache;
+
+TuneKey tune_key(GcFused* f) {
+    double vol = 0.0;
+    for (const SysInfo& S : f->hsys) vol += (double)S.g.L[0] * S.g.L[1] * S.g.L[2];
+    double dens = f->n / (vol > 0 ? vol : 1.0);
+    TuneKey k;
+    k.nsys_class = f->nsys > 1 ? (int)lround(log2((double)f->nsys)) + 1 : 0;
+    k.n_class = (int)lround(4.0 * log2((double)f->n));
+    k.dens_class = (int)lround(8.0 * log2(dens * f->p.rc * f->p.rc * f->p.rc + 1e-30));
+    k.cells = f->ncell > 0;
+    k.noise = f->p.noise_pref > 0.f;
+    return k;
+}
+
+// Milliseconds per step of `steps` steps with the given settings, from the
+// saved state (HUGE_VAL if the settings do not run, e.g. out of memory).
+double trial(GcFused* f, const GcFusedOptions& o, int steps, int drive, cudaEvent_t e0, cudaEvent_t e1) {
+    long long step0 = f->step, steps0 = f->steps, reb0 = f->rebuilds;
+    if (gc_fused_set_options(f, &o) != GC_OK) return HUGE_VAL;
+    if (restore_state(f, &f->tsnap) != GC_OK) return HUGE_VAL;
+    f->step = step0;
+    if (refresh(f) != GC_OK) return HUGE_VAL;
+    if (f->graph && (sync_dstep(f) != GC_OK || prepare_graph(f, drive) != GC_OK)) return HUGE_VAL;
+    if (cudaEventRecord(e0, f->st) != cudaSuccess) return HUGE_VAL;
+    int rc = gc_fused_step(f, steps, drive);
+    cudaEventRecord(e1, f->st);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    f->step = step0;
+    f->steps = steps0;
+    f->rebuilds = reb0;
+    return rc == GC_OK ? ms / steps : HUGE_VAL;
+}
+
+}  // namespace
+
+extern "C" int gc_fused_autotune(GcFused* f, int trial_steps, int drive_on, int flags, GcFusedOptions* chosen,
+                                 double* ms_per_step) {
+    if (!f || !f->setup_done) return gc_fail(GC_ESTATE, "fused_autotune: call gc_fused_setup first");
+    if (trial_steps < 1) trial_steps = 30;
+    int drive = drive_on ? 1 : 0;
+    TuneKey key = tune_key(f);
+    GcFusedOptions best;
+    GC_TRY(gc_fused_get_options(f, &best));
+    best.list_capacity = 0;
+    if (flags & GC_TUNE_CACHE) {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            GcFusedOptions o = it->second;
+            int rc = gc_fused_set_options(f, &o);
+            if (rc == GC_OK && chosen) *chosen = o;
+            if (ms_per_step) *ms_per_step = 0.0;
+            return rc;
+        }
+    }
+    bool prof = f->profile;
+    f->profile = false;
+    GC_TRY(save_state(f, &f->tsnap));
+    cudaEvent_t e0, e1;
+    GC_CUDA(cudaEventCreate(&e0), "autotune: events");
+    GC_CUDA(cudaEventCreate(&e1), "autotune: events");
+    double best_ms = trial(f, best, trial_steps, drive, e0, e1);
+    const float skins[] = {0.05f, 0.075f, 0.1f, 0.15f};
+    const int blocks[] = {64, 128, 256};
+    for (float s : skins) {
+        GcFusedOptions o = best;
+        o.skin = s;
+        if (o.skin == best.skin) continue;
+        double ms = trial(f, o, trial_steps, drive, e0, e1);
+        if (ms < best_ms) { best_ms = ms; best = o; }
+    }
+    for (int b : blocks) {
+        GcFusedOptions o = best;
+        o.block = b;
+        if (o.block == best.block) continue;
+        double ms = trial(f, o, trial_steps, drive, e0, e1);
+        if (ms < best_ms) { best_ms = ms; best = o; }
+    }
+    for (int c = 0; c < 2; ++c) {
+        GcFusedOptions o = best;
+        o.compact = c;
+        if (o.compact == best.compact) continue;
+        double ms = trial(f, o, trial_steps, drive, e0, e1);
+        if (ms < best_ms) { best_ms = ms; best = o; }
+    }
+    for (int g = 0; g < 2; ++g) {
+        GcFusedOptions o = best;
+        o.graph = g;
+        if (o.graph == best.graph) continue;
+        double ms = trial(f, o, trial_steps, drive, e0, e1);
+        if (ms < best_ms) { best_ms = ms; best = o; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    long long step0 = f->step;
+    GC_TRY(gc_fused_set_options(f, &best));
+    GC_TRY(restore_state(f, &f->tsnap));
+    f->step = step0;
+    GC_TRY(sync_dstep(f));
+    GC_TRY(refresh(f));
+    f->profile = prof;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tune_cache[key] = best;
+    }
+    if (chosen) *chosen = best;
+    if (ms_per_step) *ms_per_step = best_ms;
+    if (!(best_ms < HUGE_VAL)) return gc_fail(GC_EDEVICE, "fused_autotune: no setting ran");
+    return GC_OK;
+}
 
 // ---------------------------------------------------------------------------
 // The fused engine behind the boundary entry points (GPUCELL_ENGINE=fused).
@@ -1541,29 +2528,8 @@ int engine_cells(GcFused* f, const GcRefPtrs& r) {
         !r.maxrefedgelen || !r.perlen || !r.hpow || !r.hbending || !r.reftriangle || !r.reftriarea ||
         !r.refarea_para || !r.refvol_para)
         return gc_fail(GC_ESTATE, "fused engine: a membrane buffer of the set-up calls was not seen");
-    f->ncell = ncell;
-    f->ntri = ntri;
-    f->nedge = nedge;
-    f->ncp = ncp;
-    GC_TRY(falloc(f, &f->tri, ntri));
-    GC_TRY(falloc(f, &f->edge, nedge));
-    GC_TRY(falloc(f, &f->betri, ncell));
-    GC_TRY(falloc(f, &f->celltab, ncp));
-    float** e1[] = {&f->shear, &f->bend, &f->l0, &f->lmax, &f->perlen, &f->hpow, &f->hbend, &f->refang};
-    for (float** q : e1) GC_TRY(falloc(f, q, nedge));
-    float** t1[] = {&f->hl, &f->hg, &f->hv, &f->tarea, &f->reftarea};
-    for (float** q : t1) GC_TRY(falloc(f, q, ntri));
-    GC_TRY(falloc(f, &f->tnorm, ntri));
-    GC_TRY(falloc(f, &f->tcen, ntri));
-    double** c1[] = {&f->carea, &f->cvol, &f->crefarea, &f->crefvol};
-    for (double** q : c1) GC_TRY(falloc(f, q, ncell));
-    GC_TRY(falloc(f, &f->mpos, ncp));
-    GC_TRY(falloc(f, &f->mforce, ncp));
-    GC_TRY(falloc(f, &f->magg, ncp));
-    GC_TRY(falloc(f, &f->mnthro, ncp));
-    GC_TRY(falloc(f, &f->parea, ncp));
-    GC_TRY(falloc(f, &f->mkeys, ncp));
-    GC_TRY(falloc(f, &f->mvals, ncp));
+    GC_TRY(alloc_cells(f, ncell, ntri, nedge, ncp));
+    f->cells_adopted = true;
     cudaStream_t st = f->st;
     auto d2d = [&](void* dst, const void* src, size_t bytes) -> int {
         if (!src) return GC_OK;
@@ -1586,16 +2552,10 @@ int engine_cells(GcFused* f, const GcRefPtrs& r) {
     GC_TRY(d2d(f->hbend, r.hbending, (size_t)nedge * 4));
     GC_TRY(d2d(f->refang, r.reftriangle, (size_t)nedge * 4));
     GC_TRY(d2d(f->reftarea, r.reftriarea, (size_t)ntri * 4));
-    GC_CUDA(cudaMemsetAsync(f->magg, 0, (size_t)ncp * sizeof(float4), st), "fused engine: magg");
     fk_import_cellrefs<<<gc_blocks(ncell, 128), 128, 0, st>>>(ncell, ntri, f->betri, r.refarea_para, r.refvol_para,
                                                             f->crefarea, f->crefvol);
     GC_CHECK_LAUNCH("fused engine: reference areas and volumes");
-    if (f->p.De != 0.f && f->p.maxcut > 0.f) {
-        float bb[6] = {f->lgrid.lo[0], f->lgrid.hi[0], f->lgrid.lo[1], f->lgrid.hi[1], f->lgrid.lo[2], f->lgrid.hi[2]};
-        GC_TRY(gc_build_grid(bb, f->p.maxcut, f->lgrid.pmask, &f->mgrid));
-        f->have_agg = true;
-    }
-    return GC_OK;
+    return build_grids(f);   // aggregation grid
 }
 
 int engine_start(GcState& s) {
@@ -1606,7 +2566,10 @@ int engine_start(GcState& s) {
     GC_CUDA(cudaMemcpyAsync(bb, r.bbox, sizeof(bb), cudaMemcpyDeviceToHost, s.stream), "fused engine: bbox");
     GC_CUDA(cudaStreamSynchronize(s.stream), "fused engine: bbox");
     GcFused* f = nullptr;
-    GC_TRY(gc_fused_create(&s.c, bb, s.periodic_mask, s.noise_on, nullptr, &f));
+    GcFusedOptions opt;
+    memset(&opt, 0, sizeof(opt));
+    opt.compact = 1;
+    GC_TRY(gc_fused_create(&s.c, bb, s.periodic_mask, s.noise_on, &opt, &f));
     int rc = engine_cells(f, r);
     if (rc == GC_OK) {
         fk_import_ref<<<gc_blocks(f->n, f->block), f->block, 0, f->st>>>(
@@ -1621,7 +2584,7 @@ int engine_start(GcState& s) {
         gc_fused_destroy(f);
         return rc;
     }
-    f->loaded = true;
+    for (int k = 0; k < f->nsys; ++k) f->sys_loaded[k] = 1;
     f->setup_done = true;
     s.engine = f;
     return GC_OK;
@@ -1639,7 +2602,7 @@ int engine_export(GcFused* f, const GcRefPtrs& r) {
                                                      r.triarea, r.trinordir, r.tricenter);
         GC_CHECK_LAUNCH("fused engine: write back cells");
         int m = f->ncp;
-        fk_store_cells<<<gc_blocks(m, 128), 128, 0, st>>>(m, 0, f->mforce, f->magg, f->parea, f->tnorm, f->tcen,
+        fk_store_cells<<<gc_blocks(m, 128), 128, 0, st>>>(m, 0, 0, 0, f->mforce, f->magg, f->parea, f->tnorm, f->tcen,
                                                          r.defforce, r.aggforce, r.pararea, nullptr, nullptr,
                                                          f->have_agg ? 1 : 0);
         GC_CHECK_LAUNCH("fused engine: write back membrane forces");

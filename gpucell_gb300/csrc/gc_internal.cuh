@@ -224,14 +224,18 @@ __device__ __forceinline__ float unit_uniform21(uint32_t u) {
 
 // The noise components xi_ij for the pair (i, j) without the sign of the
 // pair: xi_ij = pair_sign(i, j) * pair_noise_unsigned(i, j).
-__device__ __forceinline__ float3 pair_noise_unsigned(unsigned id_i, unsigned id_j, const GcParams& p) {
+__device__ __forceinline__ float3 pair_noise_unsigned_k(unsigned id_i, unsigned id_j, uint32_t key) {
     unsigned a = id_i < id_j ? id_i : id_j;
     unsigned b = id_i < id_j ? id_j : id_i;
-    Philox2 w = philox2x32_10(a, b, p.noise_key);
+    Philox2 w = philox2x32_10(a, b, key);
     uint32_t u0 = w.w0 & 0x1FFFFFu;
     uint32_t u1 = (w.w0 >> 21) | ((w.w1 & 0x3FFu) << 11);
     uint32_t u2 = (w.w1 >> 10) & 0x1FFFFFu;
     return f3(unit_uniform21(u0), unit_uniform21(u1), unit_uniform21(u2));
+}
+
+__device__ __forceinline__ float3 pair_noise_unsigned(unsigned id_i, unsigned id_j, const GcParams& p) {
+    return pair_noise_unsigned_k(id_i, id_j, p.noise_key);
 }
 
 __device__ __forceinline__ float pair_sign(unsigned id_i, unsigned id_j) { return id_i < id_j ? 1.f : -1.f; }
@@ -334,6 +338,22 @@ int gc_make_params(GcParams* out, bool need_grid);
 int gc_build_grid(const float* bb, float cut, int mask, GcGrid* g);
 // Stable sort of (keys, vals) by key in [0, K), in place (neighbor.cu).
 int gc_counting_sort(int n, int K, int* keys, int* vals, cudaStream_t st);
+// Temporaries of the counting sort.  After a sort, cnt[k] is the first
+// position of key k and cnt[K] = n.
+struct GcSortBufs {
+    unsigned* cnt;    // K + 1
+    unsigned* rank;   // n
+    int *tkey, *tval, *tsrc;   // n each
+    unsigned* bsum;   // K / 4096 + 2
+};
+// Bytes of one allocation that holds the temporaries for n elements and K keys.
+size_t gc_sort_bufs_bytes(int n, int K);
+// Splits such an allocation into the temporaries.
+void gc_sort_bufs_carve(void* base, int n, int K, GcSortBufs* b);
+// The same sort as gc_counting_sort on the given temporaries (no library
+// scratch, so it can be captured into a CUDA graph).
+int gc_counting_sort_bufs(int n, int K, int* keys, int* vals, const GcSortBufs& b, unsigned* flags,
+                          cudaStream_t st);
 // Start of every key's range (K + 1 entries) after the latest counting sort.
 const unsigned* gc_sort_starts();
 // (Re)builds the grid from the caller's device bbox pointer.
@@ -345,6 +365,8 @@ long long gc_noise_step();
 // launch failed.  Written after every <<<...>>> so that
 // gc_launch_count() is exact.
 void gc_count_launch();
+// Adjusts the launch count by k.
+void gc_add_launches(long long k);
 #define GC_CHECK_LAUNCH(what)                                   \
     do {                                                        \
         gc_count_launch();                                      \

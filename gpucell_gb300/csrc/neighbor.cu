@@ -242,12 +242,11 @@ __global__ void k_gather(int n, int* __restrict__ sortpart, const int* __restric
     }
 }
 
-int scan_exclusive(unsigned* buf, int n, cudaStream_t st) {
-    // in-place exclusive scan of buf[0..n), buf[n] = total
+// In-place exclusive scan of buf[0..n) with buf[n] = total; `bsum` holds
+// (n / kScanTile + 1) block sums.
+int scan_exclusive_with(unsigned* buf, int n, unsigned* bsum, cudaStream_t st) {
     int nb = (n + kScanTile - 1) / kScanTile;
     if (nb > kScanTile) return gc_fail(GC_EINVAL, "scan of %d elements exceeds the two-level limit", n);
-    unsigned* bsum = (unsigned*)gc_scratch(SCR_SCAN_BLOCKS, (size_t)(nb + 1) * sizeof(unsigned));
-    if (!bsum) return GC_ENOMEM;
     k_scan_tiles<<<nb, kScanBS, 0, st>>>(n, buf, buf, bsum);
     GC_CHECK_LAUNCH("scan: tiles");
     k_scan_bsums<<<1, kScanBS, 0, st>>>(nb, bsum, buf + n);
@@ -256,6 +255,22 @@ int scan_exclusive(unsigned* buf, int n, cudaStream_t st) {
     GC_CHECK_LAUNCH("scan: add");
     return GC_OK;
 }
+
+// The stable counting sort on caller-provided temporaries.
+int sort_with(int n, int K, int* keys, int* vals, const GcSortBufs& b, unsigned* flags, cudaStream_t st) {
+    if (n <= 0) return GC_OK;
+    GC_CUDA(cudaMemsetAsync(b.cnt, 0, (size_t)(K + 1) * sizeof(unsigned), st), "sort: clear counts");
+    k_sort_count<<<gc_blocks(n, kBS), kBS, 0, st>>>(n, K, keys, b.cnt, b.rank, flags);
+    GC_CHECK_LAUNCH("sort: count");
+    GC_TRY(scan_exclusive_with(b.cnt, K, b.bsum, st));
+    k_sort_scatter<<<gc_blocks(n, kBS), kBS, 0, st>>>(n, K, keys, vals, b.cnt, b.rank, b.tkey, b.tval, b.tsrc);
+    GC_CHECK_LAUNCH("sort: scatter");
+    k_sort_fix<<<gc_blocks((long long)K * 32, kBS), kBS, 0, st>>>(K, b.cnt, b.tkey, b.tval, b.tsrc, keys, vals);
+    GC_CHECK_LAUNCH("sort: fix");
+    return GC_OK;
+}
+
+size_t round256(size_t b) { return (b + 255) / 256 * 256; }
 
 }  // namespace
 
@@ -267,22 +282,41 @@ const unsigned* gc_sort_starts() { return (const unsigned*)gc_state().scratch[SC
 // step.  `keys` and `vals` are sorted in place.
 int gc_counting_sort(int n, int K, int* keys, int* vals, cudaStream_t st) {
     if (n <= 0) return GC_OK;
-    unsigned* cnt = (unsigned*)gc_scratch(SCR_SORT_COUNT, (size_t)(K + 1) * sizeof(unsigned));
-    unsigned* rank = (unsigned*)gc_scratch(SCR_SORT_RANK, (size_t)n * sizeof(unsigned));
-    int* tkey = (int*)gc_scratch(SCR_SORT_KEY, (size_t)n * sizeof(int));
-    int* tval = (int*)gc_scratch(SCR_SORT_VAL, (size_t)n * sizeof(int));
-    int* tsrc = (int*)gc_scratch(SCR_SORT_SRC, (size_t)n * sizeof(int));
-    if (!cnt || !rank || !tkey || !tval || !tsrc) return GC_ENOMEM;
-    unsigned* flags = gc_flags_ptr();
-    GC_CUDA(cudaMemsetAsync(cnt, 0, (size_t)(K + 1) * sizeof(unsigned), st), "sort: clear counts");
-    k_sort_count<<<gc_blocks(n, kBS), kBS, 0, st>>>(n, K, keys, cnt, rank, flags);
-    GC_CHECK_LAUNCH("sort: count");
-    GC_TRY(scan_exclusive(cnt, K, st));
-    k_sort_scatter<<<gc_blocks(n, kBS), kBS, 0, st>>>(n, K, keys, vals, cnt, rank, tkey, tval, tsrc);
-    GC_CHECK_LAUNCH("sort: scatter");
-    k_sort_fix<<<gc_blocks((long long)K * 32, kBS), kBS, 0, st>>>(K, cnt, tkey, tval, tsrc, keys, vals);
-    GC_CHECK_LAUNCH("sort: fix");
-    return GC_OK;
+    GcSortBufs b;
+    b.cnt = (unsigned*)gc_scratch(SCR_SORT_COUNT, (size_t)(K + 1) * sizeof(unsigned));
+    b.rank = (unsigned*)gc_scratch(SCR_SORT_RANK, (size_t)n * sizeof(unsigned));
+    b.tkey = (int*)gc_scratch(SCR_SORT_KEY, (size_t)n * sizeof(int));
+    b.tval = (int*)gc_scratch(SCR_SORT_VAL, (size_t)n * sizeof(int));
+    b.tsrc = (int*)gc_scratch(SCR_SORT_SRC, (size_t)n * sizeof(int));
+    b.bsum = (unsigned*)gc_scratch(SCR_SCAN_BLOCKS, (size_t)(K / kScanTile + 2) * sizeof(unsigned));
+    if (!b.cnt || !b.rank || !b.tkey || !b.tval || !b.tsrc || !b.bsum) return GC_ENOMEM;
+    return sort_with(n, K, keys, vals, b, gc_flags_ptr(), st);
+}
+
+size_t gc_sort_bufs_bytes(int n, int K) {
+    size_t nn = (size_t)(n > 0 ? n : 1), kk = (size_t)(K > 0 ? K : 1);
+    return round256((kk + 1) * 4) + 4 * round256(nn * 4) + round256((kk / kScanTile + 2) * 4);
+}
+
+void gc_sort_bufs_carve(void* base, int n, int K, GcSortBufs* b) {
+    size_t nn = (size_t)(n > 0 ? n : 1), kk = (size_t)(K > 0 ? K : 1);
+    unsigned char* p = (unsigned char*)base;
+    b->cnt = (unsigned*)p;
+    p += round256((kk + 1) * 4);
+    b->rank = (unsigned*)p;
+    p += round256(nn * 4);
+    b->tkey = (int*)p;
+    p += round256(nn * 4);
+    b->tval = (int*)p;
+    p += round256(nn * 4);
+    b->tsrc = (int*)p;
+    p += round256(nn * 4);
+    b->bsum = (unsigned*)p;
+}
+
+int gc_counting_sort_bufs(int n, int K, int* keys, int* vals, const GcSortBufs& b, unsigned* flags,
+                          cudaStream_t st) {
+    return sort_with(n, K, keys, vals, b, flags, st);
 }
 
 extern "C" {
@@ -504,20 +538,13 @@ extern "C" int gc_cudiv_Sort_noalloc(int n, int* keys, int* values) {
     if (K > GC_NOALLOC_SORT_MAX_KEYS)
         return gc_fail(GC_EINVAL, "Sort_noalloc: %d keys exceed the fixed scratch (at most %d)", K,
                        GC_NOALLOC_SORT_MAX_KEYS);
-    // the counts must start at zero; every other region is fully written
-    GC_CUDA(cudaMemsetAsync(cnt, 0, (size_t)(K + 1) * sizeof(unsigned), st), "Sort_noalloc: clear counts");
-    k_sort_count<<<gc_blocks(n, kBS), kBS, 0, st>>>(n, K, keys, cnt, rank, nullptr);
-    GC_CHECK_LAUNCH("Sort_noalloc: count");
-    int nb = (K + kScanTile - 1) / kScanTile;
-    k_scan_tiles<<<nb, kScanBS, 0, st>>>(K, cnt, cnt, bsum);
-    GC_CHECK_LAUNCH("Sort_noalloc: scan tiles");
-    k_scan_bsums<<<1, kScanBS, 0, st>>>(nb, bsum, cnt + K);
-    GC_CHECK_LAUNCH("Sort_noalloc: scan block sums");
-    k_scan_add<<<gc_blocks(K, kBS), kBS, 0, st>>>(K, cnt, bsum);
-    GC_CHECK_LAUNCH("Sort_noalloc: scan add");
-    k_sort_scatter<<<gc_blocks(n, kBS), kBS, 0, st>>>(n, K, keys, values, cnt, rank, tkey, tval, tsrc);
-    GC_CHECK_LAUNCH("Sort_noalloc: scatter");
-    k_sort_fix<<<gc_blocks((long long)K * 32, kBS), kBS, 0, st>>>(K, cnt, tkey, tval, tsrc, keys, values);
-    GC_CHECK_LAUNCH("Sort_noalloc: fix");
+    GcSortBufs b;
+    b.cnt = cnt;
+    b.rank = rank;
+    b.tkey = tkey;
+    b.tval = tval;
+    b.tsrc = tsrc;
+    b.bsum = bsum;
+    GC_TRY(sort_with(n, K, keys, values, b, nullptr, st));
     return GC_OK;
 }

@@ -44,6 +44,10 @@ void init_from_env() {
 
 void gc_count_launch() { ++g_launches; }
 
+// Adjusts the count by k (captured launches that did not run, replays of
+// captured graphs that did).
+void gc_add_launches(long long k) { g_launches += (unsigned long long)k; }
+
 GcState& gc_state() {
     std::call_once(g_once, init_from_env);
     return g_state;

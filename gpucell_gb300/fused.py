@@ -1,12 +1,16 @@
-"""The fused timestep (gc_fused_* in include/gpucell_gb300.h) from Python.
+"""The fused timestep (gc_fused_* / gc_ensemble_* in include/gpucell_gb300.h)
+from Python.
 
 ``FusedSystem`` loads a generated configuration in GPUCell's layouts into a
 library-owned simulation, runs timesteps, and stores the state back in
 original particle order, with host (numpy) or device (torch) buffers.
+``Ensemble`` does the same for many independent configurations stepped by
+the same launches.
 """
 from __future__ import annotations
 
 import ctypes as C
+from typing import Sequence
 
 import numpy as np
 
@@ -22,59 +26,42 @@ def _ptr(a):
     return C.c_void_p(a.data_ptr())
 
 
-class FusedSystem:
-    def __init__(self, cfg: Config, noise=True, skin=0.1, block=128, list_capacity=0, compact=True):
-        self.cfg = cfg
-        self.lib = _lib.load()
-        self.h = C.c_void_p()
-        consts = _lib.Structconst(**cfg.consts())
-        opt = _lib.GcFusedOptions(skin=skin, block=block, list_capacity=list_capacity, compact=1 if compact else 0)
-        bbox = np.ascontiguousarray(cfg.bbox, np.float32)
-        _lib.call("gc_fused_create", C.byref(consts), _ptr(bbox), cfg.pmask, 1 if noise else 0, C.byref(opt),
-                  C.byref(self.h))
-        if cfg.ncell:
-            shear, bend, hl, hg, hv = cfg.edge_params()
-            self._keep = [np.ascontiguousarray(a) for a in (cfg.tri.astype(np.int32), cfg.edge.astype(np.int32),
-                                                           cfg.betri.astype(np.int32), cfg.celltab.astype(np.int32),
-                                                           shear, bend, hl, hg, hv)]
-            _lib.call("gc_fused_set_cells", self.h, cfg.ncell, cfg.ntri, cfg.nedge, *[_ptr(a) for a in self._keep])
-        pos = np.ascontiguousarray(cfg.coor, np.float32)
-        vh = np.ascontiguousarray(cfg.velhalf, np.float32)
-        _lib.call("gc_fused_load", self.h, _ptr(pos), C.c_void_p(0), _ptr(vh), C.c_void_p(0), C.c_void_p(0), 0)
-        _lib.call("gc_fused_setup", self.h)
+def _options(skin, block, list_capacity, compact, graph):
+    return _lib.GcFusedOptions(skin=skin, block=block, list_capacity=list_capacity, compact=1 if compact else 0,
+                               graph=1 if graph else 0)
 
-    def load(self, pos, vel=None, velhalf=None, force=None, nthro=None):
-        arrs = [None if a is None else np.ascontiguousarray(a, np.int32 if k == 4 else np.float32)
-                for k, a in enumerate((pos, vel, velhalf, force, nthro))]
-        _lib.call("gc_fused_load", self.h, *[_ptr(a) for a in arrs], 0)
 
-    def setup(self):
-        _lib.call("gc_fused_setup", self.h)
+def _cell_arrays(cfg: Config):
+    shear, bend, hl, hg, hv = cfg.edge_params()
+    return [np.ascontiguousarray(a) for a in (cfg.tri.astype(np.int32), cfg.edge.astype(np.int32),
+                                              cfg.betri.astype(np.int32), cfg.celltab.astype(np.int32),
+                                              shear, bend, hl, hg, hv)]
+
+
+_PARTICLE_KEYS = ("pos", "vel", "rho", "press", "force", "velhalf", "nthro")
+_CELL_KEYS = ("Area", "Vol", "DefForce", "AggForce", "TriNorDir", "TriCenter", "ParArea")
+
+
+def _particle_out(n):
+    return dict(pos=np.empty((n, 3), np.float32), vel=np.empty((n, 3), np.float32), rho=np.empty(n, np.float32),
+                press=np.empty(n, np.float32), force=np.empty((n, 3), np.float32),
+                velhalf=np.empty((n, 3), np.float32), nthro=np.empty((n, 3), np.int32))
+
+
+def _cell_out(c: Config):
+    return dict(Area=np.empty(c.ncell, np.float32), Vol=np.empty(c.ncell, np.float32),
+                DefForce=np.empty((c.ncp, 3), np.float32), AggForce=np.empty((c.ncp, 3), np.float32),
+                TriNorDir=np.empty((c.ntri, 3), np.float32), TriCenter=np.empty((c.ntri, 3), np.float32),
+                ParArea=np.empty(c.ncp, np.float32))
+
+
+class _Handle:
+    """Calls shared by one simulation and an ensemble."""
+
+    h: C.c_void_p
 
     def step(self, nsteps=1, drive_on=1):
         _lib.call("gc_fused_step", self.h, int(nsteps), int(drive_on))
-
-    def fetch(self) -> dict:
-        n = self.cfg.n
-        out = dict(pos=np.empty((n, 3), np.float32), vel=np.empty((n, 3), np.float32), rho=np.empty(n, np.float32),
-                   press=np.empty(n, np.float32), force=np.empty((n, 3), np.float32),
-                   velhalf=np.empty((n, 3), np.float32), nthro=np.empty((n, 3), np.int32))
-        _lib.call("gc_fused_store", self.h, *[_ptr(out[k]) for k in
-                                             ("pos", "vel", "rho", "press", "force", "velhalf", "nthro")], 0)
-        c = self.cfg
-        if c.ncell:
-            cells = dict(Area=np.empty(c.ncell, np.float32), Vol=np.empty(c.ncell, np.float32),
-                         DefForce=np.empty((c.ncp, 3), np.float32), AggForce=np.empty((c.ncp, 3), np.float32),
-                         TriNorDir=np.empty((c.ntri, 3), np.float32), TriCenter=np.empty((c.ntri, 3), np.float32),
-                         ParArea=np.empty(c.ncp, np.float32))
-            _lib.call("gc_fused_store_cells", self.h, *[_ptr(cells[k]) for k in
-                                                       ("Area", "Vol", "DefForce", "AggForce", "TriNorDir",
-                                                        "TriCenter", "ParArea")], 0)
-            out.update(cells)
-            a, v = np.empty(c.ncell), np.empty(c.ncell)
-            _lib.call("gc_fused_cell_sums", self.h, _ptr(a), _ptr(v))
-            out["Area64"], out["Vol64"] = a, v
-        return out
 
     def stats(self) -> dict:
         r, s, cap, mx = C.c_longlong(), C.c_longlong(), C.c_int(), C.c_int()
@@ -96,8 +83,28 @@ class FusedSystem:
         _lib.call("gc_fused_profile_read", self.h, C.byref(d), C.byref(f), C.byref(k))
         return dict(density_ms=d.value, force_ms=f.value, steps=k.value)
 
+    def options(self) -> dict:
+        o = _lib.GcFusedOptions()
+        _lib.call("gc_fused_get_options", self.h, C.byref(o))
+        return dict(skin=round(float(o.skin), 6), block=o.block, list_capacity=o.list_capacity,
+                    compact=bool(o.compact), graph=bool(o.graph))
+
+    def set_options(self, skin=0.0, block=0, list_capacity=0, compact=None, graph=None):
+        cur = self.options()
+        o = _options(skin, block, list_capacity, cur["compact"] if compact is None else compact,
+                     cur["graph"] if graph is None else graph)
+        _lib.call("gc_fused_set_options", self.h, C.byref(o))
+
+    def autotune(self, trial_steps=30, drive_on=1, use_cache=False) -> dict:
+        o = _lib.GcFusedOptions()
+        ms = C.c_double()
+        _lib.call("gc_fused_autotune", self.h, int(trial_steps), int(drive_on),
+                  _lib.GC_TUNE_CACHE if use_cache else 0, C.byref(o), C.byref(ms))
+        return dict(skin=round(float(o.skin), 6), block=o.block, compact=bool(o.compact), graph=bool(o.graph),
+                    ms_per_step=ms.value)
+
     def close(self):
-        if self.h:
+        if getattr(self, "h", None):
             _lib.call("gc_fused_destroy", self.h)
             self.h = C.c_void_p()
 
@@ -106,3 +113,100 @@ class FusedSystem:
             self.close()
         except Exception:
             pass
+
+
+class FusedSystem(_Handle):
+    def __init__(self, cfg: Config, noise=True, skin=0.1, block=128, list_capacity=0, compact=True, graph=False):
+        self.cfg = cfg
+        self.lib = _lib.load()
+        self.h = C.c_void_p()
+        consts = _lib.Structconst(**cfg.consts())
+        opt = _options(skin, block, list_capacity, compact, graph)
+        bbox = np.ascontiguousarray(cfg.bbox, np.float32)
+        _lib.call("gc_fused_create", C.byref(consts), _ptr(bbox), cfg.pmask, 1 if noise else 0, C.byref(opt),
+                  C.byref(self.h))
+        if cfg.ncell:
+            self._keep = _cell_arrays(cfg)
+            _lib.call("gc_fused_set_cells", self.h, cfg.ncell, cfg.ntri, cfg.nedge, *[_ptr(a) for a in self._keep])
+        pos = np.ascontiguousarray(cfg.coor, np.float32)
+        vh = np.ascontiguousarray(cfg.velhalf, np.float32)
+        _lib.call("gc_fused_load", self.h, _ptr(pos), C.c_void_p(0), _ptr(vh), C.c_void_p(0), C.c_void_p(0), 0)
+        _lib.call("gc_fused_setup", self.h)
+
+    def load(self, pos, vel=None, velhalf=None, force=None, nthro=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.int32 if k == 4 else np.float32)
+                for k, a in enumerate((pos, vel, velhalf, force, nthro))]
+        _lib.call("gc_fused_load", self.h, *[_ptr(a) for a in arrs], 0)
+
+    def setup(self):
+        _lib.call("gc_fused_setup", self.h)
+
+    def fetch(self) -> dict:
+        out = _particle_out(self.cfg.n)
+        _lib.call("gc_fused_store", self.h, *[_ptr(out[k]) for k in _PARTICLE_KEYS], 0)
+        c = self.cfg
+        if c.ncell:
+            cells = _cell_out(c)
+            _lib.call("gc_fused_store_cells", self.h, *[_ptr(cells[k]) for k in _CELL_KEYS], 0)
+            out.update(cells)
+            a, v = np.empty(c.ncell), np.empty(c.ncell)
+            _lib.call("gc_fused_cell_sums", self.h, _ptr(a), _ptr(v))
+            out["Area64"], out["Vol64"] = a, v
+        return out
+
+
+class Ensemble(_Handle):
+    """Independent configurations of uneven size stepped by the same launches.
+
+    The configurations must share their physical constants; particle counts,
+    boxes, membranes, body force (``ConstExtForce``) and noise seed may
+    differ.  ``fetch(s)`` gives system s in its own particle order, exactly as
+    ``FusedSystem.fetch`` would.
+    """
+
+    def __init__(self, cfgs: Sequence[Config], noise=True, skin=0.1, block=128, list_capacity=0, compact=True,
+                 graph=False):
+        self.cfgs = list(cfgs)
+        self.lib = _lib.load()
+        self.h = C.c_void_p()
+        descs = (_lib.GcSystemDesc * len(self.cfgs))()
+        for d, cfg in zip(descs, self.cfgs):
+            d.consts = _lib.Structconst(**cfg.consts())
+            d.bbox[:] = [float(x) for x in cfg.bbox]
+            d.periodic_mask = cfg.pmask
+        opt = _options(skin, block, list_capacity, compact, graph)
+        _lib.call("gc_ensemble_create", len(self.cfgs), descs, 1 if noise else 0, C.byref(opt), C.byref(self.h))
+        self._keep = []
+        for s, cfg in enumerate(self.cfgs):
+            if cfg.ncell:
+                arrs = _cell_arrays(cfg)
+                self._keep.append(arrs)
+                _lib.call("gc_ensemble_set_cells", self.h, s, cfg.ncell, cfg.ntri, cfg.nedge,
+                          *[_ptr(a) for a in arrs])
+            pos = np.ascontiguousarray(cfg.coor, np.float32)
+            vh = np.ascontiguousarray(cfg.velhalf, np.float32)
+            _lib.call("gc_ensemble_load", self.h, s, _ptr(pos), C.c_void_p(0), _ptr(vh), C.c_void_p(0),
+                      C.c_void_p(0), 0)
+        _lib.call("gc_fused_setup", self.h)
+
+    @property
+    def n(self) -> int:
+        return sum(c.n for c in self.cfgs)
+
+    def load(self, s, pos, vel=None, velhalf=None, force=None, nthro=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.int32 if k == 4 else np.float32)
+                for k, a in enumerate((pos, vel, velhalf, force, nthro))]
+        _lib.call("gc_ensemble_load", self.h, int(s), *[_ptr(a) for a in arrs], 0)
+
+    def fetch(self, s) -> dict:
+        c = self.cfgs[s]
+        out = _particle_out(c.n)
+        _lib.call("gc_ensemble_store", self.h, int(s), *[_ptr(out[k]) for k in _PARTICLE_KEYS], 0)
+        if c.ncell:
+            cells = _cell_out(c)
+            _lib.call("gc_ensemble_store_cells", self.h, int(s), *[_ptr(cells[k]) for k in _CELL_KEYS], 0)
+            out.update(cells)
+            a, v = np.empty(c.ncell), np.empty(c.ncell)
+            _lib.call("gc_ensemble_cell_sums", self.h, int(s), _ptr(a), _ptr(v))
+            out["Area64"], out["Vol64"] = a, v
+        return out

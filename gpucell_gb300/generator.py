@@ -79,6 +79,7 @@ class Config:
     betri: Optional[np.ndarray] = None     # (ncell, 2) int32
     celltab: Optional[np.ndarray] = None   # (ncp,) int32
     cell_type: Optional[np.ndarray] = None # (ncell,) 1-based
+    meta: dict = dataclasses.field(default_factory=dict)   # how the configuration was drawn
 
     @property
     def n(self) -> int:
@@ -327,24 +328,31 @@ def rbc_body_points(diameter: float, spacing: float, margin: float) -> np.ndarra
     return np.stack([X[inside], Y[inside], Z[inside]], 1)
 
 
+def unit_cell_volume(subdiv: int) -> float:
+    """Volume of the biconcave cell of unit diameter (divergence theorem)."""
+    v_unit, faces = icosphere(subdiv)
+    shape = biconcave(v_unit, 1.0)
+    a, b, c = (shape[faces[:, k]] for k in range(3))
+    return float(np.einsum("ij,ij->i", a, np.cross(b, c)).sum() / 6.0)
+
+
 def suspension(nx=256, ny=128, nz=128, ncells=200, subdiv=4, hematocrit=0.20, seed=12345,
-               phys: Physics | None = None, name="suspension", max_tries=20000) -> Config:
+               phys: Physics | None = None, name="suspension", max_tries=20000, diameter=None) -> Config:
     """Periodic box of nx*ny*nz particles in total: `ncells` red cells of
     10*4^subdiv+2 vertices at random positions and orientations without
     overlap, the rest fluid on a jittered lattice with the lattice sites
     nearest the membranes removed.  The cell size follows from the
-    hematocrit (cell volume fraction)."""
+    hematocrit (cell volume fraction) unless `diameter` is given."""
     phys = phys or Physics(ext_force=0.0)
     rng = np.random.default_rng(seed)
     dx = 1.0 / 3.0
     L = np.array([nx, ny, nz], float) * dx
     v_unit, faces = icosphere(subdiv)
     unit_shape = biconcave(v_unit, 1.0)
-    # volume of the unit-diameter cell (divergence theorem)
-    a, b, c = (unit_shape[faces[:, k]] for k in range(3))
-    vol1 = float(np.einsum("ij,ij->i", a, np.cross(b, c)).sum() / 6.0)
+    vol1 = unit_cell_volume(subdiv)
     box_vol = float(np.prod(L))
-    diameter = (hematocrit * box_vol / (ncells * vol1)) ** (1.0 / 3.0) if ncells else 0.0
+    if diameter is None:
+        diameter = (hematocrit * box_vol / (ncells * vol1)) ** (1.0 / 3.0) if ncells else 0.0
     cells = []
     if ncells:
         shape = unit_shape * diameter
@@ -376,6 +384,54 @@ def suspension(nx=256, ny=128, nz=128, ncells=200, subdiv=4, hematocrit=0.20, se
         lattice = lattice[np.sort(keep)]
     return _assemble(name, [0.0, L[0], 0.0, L[1], 0.0, L[2]], 7, np.zeros((0, 3)), np.zeros((0, 3)), lattice,
                      cells, phys, dx)
+
+
+def ensemble_suite(nsys=64, seed=2024, n_range=(8000, 200000), max_cells=16, subdiv=3, hct_max=0.30,
+                   force_range=(2.0e-3, 5.0e-2), phys: Physics | None = None) -> list:
+    """Independent periodic suspensions of uneven size for one ensemble: per
+    system a particle count log-uniform in `n_range` (a 2:1:1 box of
+    2 m^3 lattice sites), a hematocrit uniform in [0, hct_max] carried by 0
+    to `max_cells` cells of 10*4^subdiv+2 vertices, a body force log-uniform
+    in `force_range` and its own noise seed.  The cell diameter follows from
+    the hematocrit and the cell count, clipped to [3, 0.55 L_min] so that
+    the cells fit the box; the hematocrit actually built is recorded in
+    `cfg.meta` with the other draws.  Every system shares the remaining
+    physical constants, as an ensemble requires."""
+    base = phys or Physics()
+    rng = np.random.default_rng(seed)
+    dx = 1.0 / 3.0
+    vol1 = unit_cell_volume(subdiv)
+    out = []
+    for s in range(nsys):
+        n_target = float(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1]))))
+        m = max(8, int(round((n_target / 2.0) ** (1.0 / 3.0))))
+        hct = float(rng.uniform(0.0, hct_max))
+        nc = int(rng.integers(0, max_cells + 1))
+        g = float(np.exp(rng.uniform(np.log(force_range[0]), np.log(force_range[1]))))
+        sub_seed = int(rng.integers(1, 2**31 - 1))
+        ph = dataclasses.replace(base, ext_force=g, seed=sub_seed)
+        box_vol = 2.0 * m ** 3 * dx ** 3
+        lmin = m * dx
+        if nc == 0 or hct < 0.01:
+            nc, d = 0, None
+        else:
+            d = (hct * box_vol / (nc * vol1)) ** (1.0 / 3.0)
+            d = float(min(max(d, 3.0), 0.55 * lmin))
+        cfg = None
+        while cfg is None:
+            try:
+                cfg = suspension(nx=2 * m, ny=m, nz=m, ncells=nc, subdiv=subdiv, seed=sub_seed, phys=ph,
+                                 name=f"ensemble{s}", diameter=d, max_tries=4000)
+            except RuntimeError:   # no room left for a cell: make the cells smaller, then fewer
+                if d > 3.0:
+                    d = max(3.0, 0.9 * d)
+                else:
+                    nc -= 1
+        built = nc * vol1 * d ** 3 / box_vol if nc else 0.0
+        cfg.meta = dict(system=s, lattice=(2 * m, m, m), ncells=nc, diameter=d or 0.0, hematocrit=built,
+                        hematocrit_drawn=hct, ext_force=g, seed=sub_seed)
+        out.append(cfg)
+    return out
 
 
 def small_channel(seed=7, with_cell=True, b1_layers=1, nx=24, ny=12, nz=12, subdiv=2, diameter=3.0,

@@ -181,7 +181,9 @@ typedef struct {
     int list_capacity;    /* initial neighbour-list capacity per particle (0: from the density) */
     int compact;          /* 1: the density pass marks the list entries that act this step, and the force
                              pass iterates only those */
-    int reserved[4];
+    int graph;            /* 1: each step runs as one captured CUDA graph; the list rebuild is a conditional
+                             node decided on the device, and gc_fused_step synchronises once per call */
+    int reserved[3];
 } GcFusedOptions;
 /* bbox6 (host) as src/main.cuh:12; periodic_mask as gc_set_periodic. */
 int gc_fused_create(const Structconst* consts, const float* bbox6, int periodic_mask, int noise_on,
@@ -223,7 +225,53 @@ int gc_fused_profile(GcFused* f, int enable);
  * steps timed since gc_fused_profile(f, 1) or the previous read.
  * Synchronises. */
 int gc_fused_profile_read(GcFused* f, double* density_ms, double* force_ms, long long* steps);
+/* Current settings (list_capacity = the current capacity). */
+int gc_fused_get_options(GcFused* f, GcFusedOptions* opt);
+/* Changes the settings of a handle, also after set-up (the lists are rebuilt
+ * when the skin, compaction or capacity change; the state is kept). */
+int gc_fused_set_options(GcFused* f, const GcFusedOptions* opt);
+/* Autotuner: times trial_steps steps (0: 30) of candidate settings -- skin
+ * 0.05/0.075/0.1/0.15 rc (the cube size of the list grid), 64/128/256
+ * threads per block, compaction on/off, captured steps on/off, searched one
+ * after the other -- each from the handle's current state, keeps the fastest
+ * and returns the handle to that state.  With GC_TUNE_CACHE a choice cached
+ * for the same size class (ensemble size, particle count and density to a
+ * quarter octave, membranes, noise) is applied without trials.  Needs
+ * gc_fused_setup; synchronises. */
+#define GC_TUNE_CACHE 1
+int gc_fused_autotune(GcFused* f, int trial_steps, int drive_on, int flags, GcFusedOptions* chosen,
+                      double* ms_per_step);
 int gc_fused_destroy(GcFused* f);
+
+/* ---- ensembles of independent simulations (no counterpart) --------------
+ *
+ * Many independent systems of uneven size stepped by the same launches: the
+ * ids of system s follow those of systems 0..s-1, each system keeps its own
+ * box, grid, body force (ConstExtForce) and noise seed (iSeed, keyed by the
+ * system's own ids, so a system draws the same noise as when run alone);
+ * every other Structconst field must be the same for all systems.  A handle
+ * from gc_ensemble_create takes the gc_fused_* calls too: gc_fused_load,
+ * _store, _store_cells and _cell_sums then cover all systems, concatenated in
+ * system order; gc_ensemble_* cover one system, in that system's own ids. */
+typedef struct {
+    Structconst consts;   /* the system's counts and constants */
+    float bbox[6];        /* as src/main.cuh:12 */
+    int periodic_mask;    /* as gc_set_periodic */
+    int reserved;
+} GcSystemDesc;
+int gc_ensemble_create(int nsys, const GcSystemDesc* systems, int noise_on, const GcFusedOptions* opt,
+                       GcFused** out);
+int gc_ensemble_size(GcFused* f, int* nsys, long long* nparticles);
+int gc_ensemble_set_cells(GcFused* f, int sys, int ncell, int ntri, int nedge, const int* tri, const int* edge,
+                          const int* betri, const int* celltab, const float* shearmod, const float* bendmod,
+                          const float* hlarea, const float* hgarea, const float* hvol);
+int gc_ensemble_load(GcFused* f, int sys, const float* pos, const float* vel, const float* velhalf,
+                     const float* force, const int* nthro, int from_device);
+int gc_ensemble_store(GcFused* f, int sys, float* pos, float* vel, float* rho, float* press, float* force,
+                      float* velhalf, int* nthro, int to_device);
+int gc_ensemble_store_cells(GcFused* f, int sys, float* area, float* vol, float* defforce, float* aggforce,
+                            float* trinordir, float* tricenter, float* pararea, int to_device);
+int gc_ensemble_cell_sums(GcFused* f, int sys, double* area, double* vol);
 
 /* ---- test hooks (no counterpart in the reference) ----------------------- */
 

@@ -30,6 +30,15 @@ def test_structconst_layout():
     assert Structconst.Temp.offset == 88
 
 
+def test_option_and_system_records_match_the_header():
+    from gpucell_gb300._lib import GcFusedOptions, GcSystemDesc
+    assert C.sizeof(GcFusedOptions) == 32 and GcFusedOptions.graph.offset == 16
+    assert C.sizeof(GcSystemDesc) == 128
+    assert GcSystemDesc.bbox.offset == 96 and GcSystemDesc.periodic_mask.offset == 120
+    txt = open(HEADER).read()
+    assert "int graph;" in txt and "int reserved[3];" in txt and "Structconst consts;" in txt
+
+
 def test_library_exports_every_declared_function(built_library):
     lib = C.CDLL(built_library)
     names = declared_c_functions()

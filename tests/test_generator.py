@@ -54,3 +54,24 @@ def test_reference_grid_formula():
     from gpucell_gb300.host import reference_grid
     ncube, outer, invwid, size = reference_grid([0, 20, -10, 10, -10, 10])   # src/main.cuh:12
     assert ncube == [20, 22, 22] and outer == [20.0, 22.0, 22.0] and size == 9680
+
+
+def test_ensemble_suite_draws_within_the_stated_ranges():
+    cfgs = gen.ensemble_suite(nsys=8, seed=3, n_range=(8000, 60000), max_cells=4, subdiv=1)
+    assert len(cfgs) == 8
+    ref = cfgs[0].consts()
+    fixed = [k for k in ref if k not in ("nBound2Start", "nFluidStart", "nCellStart", "nTotalPar", "nCellPar",
+                                         "iSeed", "ConstExtForce")]
+    seeds = set()
+    for c in cfgs:
+        m = c.meta
+        assert 8000 * 0.8 <= c.n <= 60000 * 1.2 and c.pmask == 7
+        assert 0 <= m["ncells"] <= 4 and c.ncell == m["ncells"] and c.ncp == 42 * m["ncells"]
+        assert 0.0 <= m["hematocrit"] <= 0.30 + 1e-9
+        assert 2.0e-3 <= m["ext_force"] <= 5.0e-2
+        k = c.consts()
+        assert all(k[f] == ref[f] for f in fixed)   # one ensemble: same physics
+        seeds.add(k["iSeed"])
+    assert len(seeds) == 8
+    again = gen.ensemble_suite(nsys=8, seed=3, n_range=(8000, 60000), max_cells=4, subdiv=1)
+    assert all(np.array_equal(a.coor, b.coor) for a, b in zip(cfgs, again))
