@@ -50,6 +50,15 @@ def parse():
     ap.add_argument("--small", action="store_true", help="a 1/8-size suspension (for quick checks)")
     ap.add_argument("--no-noise", dest="noise", action="store_false",
                     help="thermal noise off (for cost breakdowns; the reported workload has it on)")
+    ap.add_argument("--graph", action="store_true", help="captured steps (one CUDA graph per step)")
+    ap.add_argument("--tune", action="store_true", help="let the autotuner pick skin, block, compaction, graph")
+    ap.add_argument("--tune-steps", type=int, default=20)
+    ap.add_argument("--profile-steps", type=int, default=10, help="steps of the per-kernel timing pass")
+    ap.add_argument("--no-ensemble", dest="ensemble", action="store_false",
+                    help="skip the 64-suspension ensemble workload")
+    ap.add_argument("--ensemble-only", action="store_true", help="only the ensemble workload")
+    ap.add_argument("--ens-systems", type=int, default=64)
+    ap.add_argument("--ens-steps", type=int, default=20)
     return ap.parse_args()
 
 
@@ -194,19 +203,30 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    if args.ensemble_only:
+        ens = run_ensemble(args, dev, rank, world, barrier, max_over_ranks)
+        if rank == 0:
+            print(json.dumps(ens), flush=True)
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
     cfg, wdesc = workload(args, rank)
     W = max(args.warmup, 3)
     K = args.steps
     plain = measure_plain(cfg, dev, steps=min(K, 10), warmup=3) if args.plain else None
 
-    fs = FusedSystem(cfg, noise=args.noise, skin=args.skin, block=args.block, compact=args.compact)
+    fs = FusedSystem(cfg, noise=args.noise, skin=args.skin, block=args.block, compact=args.compact,
+                     graph=args.graph)
     fs.step(W, 1)
+    tuned = fs.autotune(trial_steps=args.tune_steps) if args.tune else None
+    fs.step(2, 1)   # settle (captures the step graph when one is used)
+    opts = fs.options()
     torch.cuda.synchronize()
     sampler = ClockSampler()
     if rank == 0:
         sampler.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    fs.profile(True)
     barrier()
     torch.cuda.synchronize()
     l0 = _lib.launch_count()
@@ -219,9 +239,13 @@ def run_ours(args):
     launches = _lib.launch_count() - l0
     t_ms = max_over_ranks(ev0.elapsed_time(ev1))
     clocks = sampler.stop(local) if rank == 0 else None
+    st1 = fs.stats()
+    # per-kernel CUDA-event timing on the launching stream (a separate pass,
+    # host-driven, so that the timed steps above run as configured)
+    fs.profile(True)
+    fs.step(max(1, args.profile_steps), 1)
     prof = fs.profile_read()
     fs.profile(False)
-    st1 = fs.stats()
     flags = fs.flags()
 
     # ---- end to end: host state -> device, one step, results -> host ----
@@ -269,6 +293,8 @@ def run_ours(args):
     force_bytes = n * (FORCE_STATE_BYTES + 4 * mean_nb)
     achieved = force_bytes / (force_ms / 1e3) / 1e9
 
+    fs.close()
+    ens = run_ensemble(args, dev, rank, world, barrier, max_over_ranks) if args.ensemble else None
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -292,8 +318,9 @@ def run_ours(args):
         "config": dict(wdesc, particles=n, membrane_vertices=cfg.ncp, triangles=cfg.ntri, edges=cfg.nedge,
                        parallelism=f"replicas x{world}" if world > 1 else "single GPU",
                        l2="working set (>1 GB: state + neighbour lists) is larger than L2; no flush",
-                       noise="on" if args.noise else "off", skin=args.skin, block=args.block,
-                       compact_lists=args.compact),
+                       noise="on" if args.noise else "off", skin=opts["skin"], block=opts["block"],
+                       compact_lists=opts["compact"], captured_steps=opts["graph"],
+                       autotuned=tuned),
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": bi,
                 "d2h_bytes_per_step": bo, "steps": KE,
@@ -321,12 +348,105 @@ def run_ours(args):
     if plain:
         plain["speedup_of_fused"] = plain["ms_per_step"] / (t_ms / K)
         line["plain_fp32"] = plain
+    if ens:
+        line["ensemble"] = ens
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
-    fs.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+ENS_METRIC = "particle-steps/s on a 64-suspension ensemble (8k-200k particles, 0-16 cells of 642 vertices)"
+
+
+def run_ensemble(args, dev, rank, world, barrier, max_over_ranks):
+    """Independent suspensions of uneven size stepped together (one ensemble
+    per GPU, systems shared out by LPT over ranks), against the same systems
+    run one after the other on the FP32 boundary path and on the fused step
+    alone.  Returns the summary on rank 0, None elsewhere."""
+    import torch
+    from gpucell_gb300 import _lib, generator, shard
+    from gpucell_gb300.fused import Ensemble, FusedSystem
+    from gpucell_gb300.host import ParticleSystem
+
+    cfgs = generator.ensemble_suite(nsys=args.ens_systems, seed=2024)
+    mine = shard.shard_for_rank([c.n for c in cfgs], rank, world)
+    sub = [cfgs[i] for i in mine]
+    K = max(1, args.ens_steps)
+    ens = Ensemble(sub, noise=args.noise, skin=0.1, block=128, compact=True, graph=True)
+    ens.step(max(args.warmup, 3), 1)
+    tuned = ens.autotune(trial_steps=10)
+    ens.step(2, 1)
+    opts = ens.options()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    l0 = _lib.launch_count()
+    r0 = ens.stats()["rebuilds"]
+    ev0.record()
+    ens.step(K, 1)
+    ev1.record()
+    torch.cuda.synchronize()
+    barrier()
+    launches = _lib.launch_count() - l0
+    t_ms = max_over_ranks(ev0.elapsed_time(ev1))
+    est = ens.stats()
+    rebuilds = est["rebuilds"] - r0
+    flags = ens.flags()
+    ens.close()
+    if rank != 0:
+        return None
+    n_all = sum(c.n for c in cfgs)
+    out = {"metric": ENS_METRIC, "value": n_all * K / (t_ms / 1e3), "unit": "particle-steps/s",
+           "ms_per_step": t_ms / K, "steps": K, "systems": len(cfgs), "particles": n_all,
+           "membrane_vertices": sum(c.ncp for c in cfgs), "cells": sum(c.ncell for c in cfgs),
+           "particles_min": min(c.n for c in cfgs), "particles_max": max(c.n for c in cfgs),
+           "options": opts, "autotuned": tuned, "gpu_launches": launches,
+           "lists": {"rebuilds_in_timed_steps": rebuilds, "mean_length": est["mean_neighbors"],
+                     "max_length": est["max_neighbors"], "capacity": est["capacity"]},
+           "device_flags": flags, "data": "synthetic (generator.ensemble_suite, seed 2024)",
+           "sharding": f"LPT over {world} ranks, {len(sub)} systems on rank 0" if world > 1 else "one GPU"}
+    if world > 1:
+        return out
+    # the same systems one after the other: FP32 boundary path, fused step
+    seq_plain_ms = seq_fused_ms = 0.0
+    ps_steps, fs_steps = 2, K
+    seq_launches = 0
+    for c in sub:
+        ps = ParticleSystem(c, device=dev, noise=args.noise)
+        ps.update()
+        torch.cuda.synchronize()
+        l1 = _lib.launch_count()
+        ev0.record()
+        for _ in range(ps_steps):
+            ps.update()
+        ev1.record()
+        torch.cuda.synchronize()
+        seq_plain_ms += ev0.elapsed_time(ev1)
+        seq_launches += _lib.launch_count() - l1
+        del ps
+        fs = FusedSystem(c, noise=args.noise, skin=0.1, block=128, compact=True)
+        fs.step(2, 1)
+        torch.cuda.synchronize()
+        ev0.record()
+        fs.step(fs_steps, 1)
+        ev1.record()
+        torch.cuda.synchronize()
+        seq_fused_ms += ev0.elapsed_time(ev1)
+        fs.close()
+    plain_v = n_all * ps_steps / (seq_plain_ms / 1e3)
+    fused_v = n_all * fs_steps / (seq_fused_ms / 1e3)
+    out["sequential_plain_fp32"] = {"value": plain_v, "unit": "particle-steps/s",
+                                    "ms_per_step_all_systems": seq_plain_ms / ps_steps, "steps_each": ps_steps,
+                                    "gpu_launches_per_step": seq_launches / ps_steps,
+                                    "path": "the systems one after the other, boundary entry points, FP32"}
+    out["sequential_fused"] = {"value": fused_v, "unit": "particle-steps/s",
+                               "ms_per_step_all_systems": seq_fused_ms / fs_steps, "steps_each": fs_steps,
+                               "path": "the systems one after the other, fused step, host-driven"}
+    out["speedup_vs_sequential_plain_fp32"] = out["value"] / plain_v
+    out["speedup_vs_sequential_fused"] = out["value"] / fused_v
+    return out
 
 
 def cpu_baseline(cfg, steps):

@@ -43,6 +43,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -113,6 +114,26 @@ __device__ __forceinline__ float3 pair_image(float3 a, float3 b, const Box& B) {
     if (B.pmask & 2) d.y = fmaf(-B.L[1], rintf(d.y * B.invL[1]), d.y);
     if (B.pmask & 4) d.z = fmaf(-B.L[2], rintf(d.z * B.invL[2]), d.z);
     return d;
+}
+
+// Pair difference without the image shift: exact for a particle farther
+// than rc + 2 skin from every periodic face (its listed partners, which have
+// moved at most skin/2 each since the lists were built, are then less than
+// L/2 away along every axis, where rint(d/L) = 0 and pair_image returns the
+// plain difference).
+template <bool WRAP>
+__device__ __forceinline__ float3 pair_diff(float3 a, float3 b, const Box& B) {
+    if constexpr (WRAP) return pair_image(a, b, B);
+    else return f3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+}
+
+// Whether a particle at x is within `margin` of a periodic face of its box.
+__device__ __forceinline__ bool near_face(float3 x, const GcGrid& g, float margin) {
+    bool w = false;
+    if (g.pmask & 1) w |= (x.x - g.lo[0] < margin) || (g.hi[0] - x.x <= margin);
+    if (g.pmask & 2) w |= (x.y - g.lo[1] < margin) || (g.hi[1] - x.y <= margin);
+    if (g.pmask & 4) w |= (x.z - g.lo[2] < margin) || (g.hi[2] - x.z <= margin);
+    return w;
 }
 
 // The per-step kernels exist in two forms.  ENS = false: one system, given
@@ -335,6 +356,9 @@ __global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, const SysInfo* __
         k = cap;
     }
     cnt[i] = k;
+    // pad to a multiple of four with the sentinel slot n (its position is
+    // NaN, so it never passes a cut-off test); the capacity is a multiple of 8
+    for (int q = k; q < ((k + 3) & ~3); ++q) nbr[sell(i, q, cap)] = n;
 }
 
 // ---------------------------------------------------------------------------
@@ -351,13 +375,17 @@ __device__ __forceinline__ size_t mrow(int i, int w, int mw) {
     return ((size_t)(i >> 5) * mw + w) * 32 + (i & 31);
 }
 
+#ifndef GC_DENS_MIN_BLOCKS
+#define GC_DENS_MIN_BLOCKS 5
+#endif
+
 template <bool ENS>
-__global__ void __launch_bounds__(kMaxBS) fk_density(int n, GcParams p, SysInfo s0, const SysInfo* __restrict__ sys,
+__global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, GcParams p, SysInfo s0, const SysInfo* __restrict__ sys,
                                                   const int* __restrict__ sysid, const float4* __restrict__ pos,
                                                   float4* __restrict__ vpred, const float4* __restrict__ vh,
                                                   float2* __restrict__ dp, const int* __restrict__ nbr,
                                                   const int* __restrict__ cnt, int cap, unsigned* __restrict__ cmask,
-                                                  int mw, int* __restrict__ ccnt) {
+                                                  int mw, int* __restrict__ ccnt, float wrap_margin) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 xi4 = pos[i];
@@ -372,31 +400,53 @@ __global__ void __launch_bounds__(kMaxBS) fk_density(int n, GcParams p, SysInfo 
     if (t == PT_FLUID || t == PT_MEMB) {
         float sum = p.w0;
         int kc = 0;
-        unsigned m = 0;
-        int jn = c > 0 ? __ldg(lp) : 0;
-        float4 xn = pos[jn];
-        for (int k = 0; k < c; ++k) {
-            float4 xj = xn;
-            if (k + 1 < c) {
-                jn = __ldg(lp + (size_t)(k + 1) * 32);
-                xn = pos[jn];
+        // The list is padded to a multiple of four entries with the sentinel
+        // slot.  Entries go in groups of four: the indices of the next group
+        // are loaded while the current group is evaluated, so that a thread
+        // keeps four index loads and four position loads in flight; the
+        // acting-entry bits of each 32-entry word are stored once.
+        const int c4 = (c + 3) & ~3;
+        auto run = [&](auto wrap) {
+            constexpr bool W = decltype(wrap)::value;
+            int jq[4];
+            if (c4 > 0) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) jq[u] = __ldg(lp + (size_t)u * 32);
             }
-            float r2 = norm2_rn(pair_image(xi, xyz(xj), B));
-            if (r2 < p.rc2) {
-                if (fid(xj) >= b2) {
-                    float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
-                    sum += wendland_w(r, p);
-                    if (r2 > 0.f) m |= 1u << (k & 31);
-                } else if (r2 < p.rep_r0sq && r2 > 0.f) {
-                    m |= 1u << (k & 31);
+            for (int w0 = 0; w0 < c4; w0 += 32) {
+                unsigned m = 0;
+                const int wend = min(w0 + 32, c4);
+                for (int k0 = w0; k0 < wend; k0 += 4) {
+                    float4 xj[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) xj[u] = pos[jq[u]];
+                    if (k0 + 4 < c4) {
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) jq[u] = __ldg(lp + (size_t)(k0 + 4 + u) * 32);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        float r2 = norm2_rn(pair_diff<W>(xi, xyz(xj[u]), B));
+                        if (r2 < p.rc2) {
+                            unsigned bit = 1u << (k0 - w0 + u);
+                            if (fid(xj[u]) >= b2) {
+                                float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+                                sum += wendland_w(r, p);
+                                if (r2 > 0.f) m |= bit;
+                            } else if (r2 < p.rep_r0sq && r2 > 0.f) {
+                                m |= bit;
+                            }
+                        }
+                    }
+                }
+                if (cmask) {
+                    cmask[mrow(i, w0 >> 5, mw)] = m;
+                    kc += __popc(m);
                 }
             }
-            if (cmask && ((k & 31) == 31 || k + 1 == c)) {
-                cmask[mrow(i, k >> 5, mw)] = m;
-                kc += __popc(m);
-                m = 0;
-            }
-        }
+        };
+        if (near_face(xi, S.g, wrap_margin)) run(std::true_type{});
+        else run(std::false_type{});
         if (ccnt) ccnt[i] = kc;
         float rho = p.mass * sum;
         float c2 = (t == PT_MEMB) ? p.c2sq : p.c1sq;
@@ -431,13 +481,30 @@ __global__ void __launch_bounds__(kMaxBS) fk_density(int n, GcParams p, SysInfo 
 // so the cut-off test is already done.  The pair noise is keyed by the ids
 // local to the system, so a system draws the same noise in an ensemble as
 // alone.
+// Acting entries are taken in groups of kForceGroup: the list indices of the
+// next group are loaded while the current group is evaluated, and a group's
+// position, density and velocity loads are issued together, so that each
+// thread has several independent gathers in flight.
+#ifndef GC_FORCE_GROUP
+#define GC_FORCE_GROUP 1
+#endif
+#ifndef GC_FORCE_AHEAD
+#define GC_FORCE_AHEAD 1
+#endif
+constexpr int kForceGroup = GC_FORCE_GROUP;
+constexpr int kForceAhead = GC_FORCE_AHEAD;   // groups of list indices loaded ahead
+constexpr int force_min_blocks(bool ens) {
+    return (kForceGroup == 1 ? 6 : (kForceGroup == 2 ? 4 : 3)) - (ens ? 1 : 0);
+}
+
 template <bool COMPACT, bool ENS>
-__global__ void __launch_bounds__(kMaxBS, ENS ? 5 : 6)
+__global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
     fk_force(int n, GcParams p, SysInfo s0, const SysInfo* __restrict__ sys, const int* __restrict__ sysid,
              const unsigned* __restrict__ nkey, const float4* __restrict__ pos, const float4* __restrict__ vpred,
              const float4* __restrict__ vh, const float2* __restrict__ dp, float4* __restrict__ force,
              float4* __restrict__ vel, const int* __restrict__ nbr, const int* __restrict__ cnt, int cap,
              const unsigned* __restrict__ cmask, int mw, const float4* __restrict__ mforce, int drive) {
+    constexpr int G = kForceGroup;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 xi4 = pos[i];
@@ -462,7 +529,8 @@ __global__ void __launch_bounds__(kMaxBS, ENS ? 5 : 6)
     const unsigned* mp = COMPACT ? cmask + mrow(i, 0, mw) : nullptr;
     unsigned m = 0;
     int base = -32;
-    // index of the next acting entry (COMPACT) or of the next entry
+    // index of the next acting entry (COMPACT) or of the next entry; called
+    // once per entry, in order
     auto next_k = [&](int k) -> int {
         if constexpr (COMPACT) {
             while (m == 0) {
@@ -476,49 +544,68 @@ __global__ void __launch_bounds__(kMaxBS, ENS ? 5 : 6)
             return k;
         }
     };
-    int jn = 0;
-    float4 xn;
-    if (c > 0) {
-        jn = __ldg(lp + (size_t)next_k(0) * 32);
-        xn = pos[jn];
-    }
-    for (int k = 0; k < c; ++k) {
-        int j = jn;
-        float4 xj4 = xn;
-        if (k + 1 < c) {   // prefetch the next entry while this one is computed
-            jn = __ldg(lp + (size_t)next_k(k + 1) * 32);
-            xn = pos[jn];
+    constexpr int A = kForceAhead;
+    int jq[A][G];
+#pragma unroll
+    for (int a = 0; a < A; ++a)
+#pragma unroll
+        for (int u = 0; u < G; ++u) {
+            int k = a * G + u;
+            jq[a][u] = k < c ? __ldg(lp + (size_t)next_k(k) * 32) : i;
         }
-        float3 d = pair_image(xi, xyz(xj4), B);
-        float r2 = norm2_rn(d);
-        if (!COMPACT && (r2 >= p.rc2 || r2 <= 0.f)) continue;   // coincident pairs exert no force
-        unsigned idj = fid(xj4);
-        float inv_r = rsqrtf(r2);
-        if (idj < b2) {   // Bound1: repulsion only
-            if (r2 < p.rep_r0sq) {
-                float ir2 = inv_r * inv_r;
-                float q2 = p.rep_r0sq * ir2, q4 = q2 * q2, q12 = q4 * q4 * q4;
-                f += (p.rep_D * (q12 - q4) * ir2) * d;
+    for (int k0 = 0; k0 < c; k0 += G) {
+        float4 xg[G], vg[G];
+        float2 dg[G];
+#pragma unroll
+        for (int u = 0; u < G; ++u) {
+            xg[u] = pos[jq[0][u]];
+            dg[u] = dp[jq[0][u]];
+            vg[u] = vpred[jq[0][u]];
+        }
+#pragma unroll
+        for (int a = 0; a + 1 < A; ++a)
+#pragma unroll
+            for (int u = 0; u < G; ++u) jq[a][u] = jq[a + 1][u];
+#pragma unroll
+        for (int u = 0; u < G; ++u) {
+            int k = k0 + A * G + u;
+            jq[A - 1][u] = k < c ? __ldg(lp + (size_t)next_k(k) * 32) : i;
+        }
+#pragma unroll
+        for (int u = 0; u < G; ++u) {
+            if (k0 + u >= c) break;
+            float4 xj4 = xg[u];
+            float3 d = pair_image(xi, xyz(xj4), B);
+            float r2 = norm2_rn(d);
+            if (!COMPACT && (r2 >= p.rc2 || r2 <= 0.f)) continue;   // coincident pairs exert no force
+            unsigned idj = fid(xj4);
+            float inv_r = rsqrtf(r2);
+            if (idj < b2) {   // Bound1: repulsion only
+                if (r2 < p.rep_r0sq) {
+                    float ir2 = inv_r * inv_r;
+                    float q2 = p.rep_r0sq * ir2, q4 = q2 * q2, q12 = q4 * q4 * q4;
+                    f += (p.rep_D * (q12 - q4) * ir2) * d;
+                }
+                continue;
             }
-            continue;
-        }
-        float2 dpj = dp[j];
-        float4 vj = vpred[j];
-        float r = r2 * inv_r;
-        float F = wendland_f(r, p);
-        f += ((dpi.y + dpj.y) * F) * d;
-        float3 e = inv_r * d;
-        float3 vij = f3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z);
-        float ev = dot3(e, vij);
-        float fdd = F * dpi.x * dpj.x;
-        f -= fdd * (p.visA * vij + (p.visB * ev) * e);
-        if (noise) {
-            float qq = p.noise_pref * fdd;
-            float q = qq > 0.f ? qq * rsqrtf(qq) : 0.f;
-            q = id < idj ? q : -q;   // the pair sign of xi_ij
-            float3 xi_ = pair_noise_unsigned_k(id - id0, idj - id0, key);
-            float exi = dot3(e, xi_);
-            f += q * (p.sqrtA * xi_ + ((p.sqrtAB - p.sqrtA) * exi) * e);
+            float2 dpj = dg[u];
+            float4 vj = vg[u];
+            float r = r2 * inv_r;
+            float F = wendland_f(r, p);
+            f += ((dpi.y + dpj.y) * F) * d;
+            float3 e = inv_r * d;
+            float3 vij = f3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z);
+            float ev = dot3(e, vij);
+            float fdd = F * dpi.x * dpj.x;
+            f -= fdd * (p.visA * vij + (p.visB * ev) * e);
+            if (noise) {
+                float qq = p.noise_pref * fdd;
+                float q = qq > 0.f ? qq * rsqrtf(qq) : 0.f;
+                q = id < idj ? q : -q;   // the pair sign of xi_ij
+                float3 xi_ = pair_noise_unsigned_k(id - id0, idj - id0, key);
+                float exi = dot3(e, xi_);
+                f += q * (p.sqrtA * xi_ + ((p.sqrtAB - p.sqrtA) * exi) * e);
+            }
         }
     }
     if (drive) f.x += S.gx;
@@ -1237,6 +1324,11 @@ int sync_dstep(GcFused* f) {
 
 const SysInfo& s0(GcFused* f) { return f->hsys[0]; }
 
+// Distance from a periodic face beyond which a particle's listed pairs need
+// no image shift: rc + 2 skin (each particle moves less than skin/2 between
+// rebuilds), with 1 % of rc to spare.
+float wrap_margin(const GcFused* f) { return 1.01f * f->p.rc + 2.f * f->skin; }
+
 // Re-sort and list build on the host-driven path (swaps the slot arrays;
 // grows the lists and rebuilds when a particle had more neighbours than the
 // lists hold).
@@ -1307,10 +1399,10 @@ int launch_density(GcFused* f, cudaStream_t st, const GcParams& p, bool mark) {
     int* cc = mark && f->compact ? f->ccnt : nullptr;
     if (f->ens)
         fk_density<true><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vpred, f->a.vh,
-                                                   f->dp, f->nbr, f->cnt, f->cap, cm, f->mw, cc);
+                                                   f->dp, f->nbr, f->cnt, f->cap, cm, f->mw, cc, wrap_margin(f));
     else
         fk_density<false><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vpred, f->a.vh,
-                                                    f->dp, f->nbr, f->cnt, f->cap, cm, f->mw, cc);
+                                                    f->dp, f->nbr, f->cnt, f->cap, cm, f->mw, cc, wrap_margin(f));
     GC_CHECK_LAUNCH("fused: density");
     return GC_OK;
 }
@@ -1818,7 +1910,7 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
     int ok = GC_OK;
     SlotArrays* sa[2] = {&f->a, &f->b};
     for (SlotArrays* s : sa) {
-        if (ok == GC_OK) ok = falloc(f, &s->pos, n);
+        if (ok == GC_OK) ok = falloc(f, &s->pos, (size_t)n + 1);   // slot n: the list padding sentinel
         if (ok == GC_OK) ok = falloc(f, &s->vel, n);
         if (ok == GC_OK) ok = falloc(f, &s->vpred, n);
         if (ok == GC_OK) ok = falloc(f, &s->vh, n);
@@ -1862,6 +1954,15 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
         if (opt && opt->list_capacity > 0) capn = opt->list_capacity;
         capn = (capn + 7) & ~7;
         ok = alloc_list(f, capn);
+    }
+    if (ok == GC_OK) {
+        // the sentinel slot that pads the lists: NaN position, fails every cut-off test
+        const uint32_t bits[4] = {0x7fc00000u, 0x7fc00000u, 0x7fc00000u, 0xffffffffu};
+        float4 sentinel;
+        memcpy(&sentinel, bits, sizeof(sentinel));
+        if (cudaMemcpy(f->a.pos + n, &sentinel, sizeof(sentinel), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(f->b.pos + n, &sentinel, sizeof(sentinel), cudaMemcpyHostToDevice) != cudaSuccess)
+            ok = gc_fail(GC_ECUDA, "fused: sentinel slot");
     }
     if (ok == GC_OK) {
         f->h->drebuilds = 0;

@@ -393,10 +393,12 @@ def ensemble_suite(nsys=64, seed=2024, n_range=(8000, 200000), max_cells=16, sub
     2 m^3 lattice sites), a hematocrit uniform in [0, hct_max] carried by 0
     to `max_cells` cells of 10*4^subdiv+2 vertices, a body force log-uniform
     in `force_range` and its own noise seed.  The cell diameter follows from
-    the hematocrit and the cell count, clipped to [3, 0.55 L_min] so that
-    the cells fit the box; the hematocrit actually built is recorded in
-    `cfg.meta` with the other draws.  Every system shares the remaining
-    physical constants, as an ensemble requires."""
+    the hematocrit and the cell count, at least 4.5 (so that the vertices
+    of a 642-vertex membrane are about as far apart as the fluid particles,
+    dx = 1/3) and at most 0.55 L_min (so that the cells fit the box); a box
+    too small for such a cell gets none.  The hematocrit actually built is
+    recorded in `cfg.meta` with the other draws.  Every system shares the
+    remaining physical constants, as an ensemble requires."""
     base = phys or Physics()
     rng = np.random.default_rng(seed)
     dx = 1.0 / 3.0
@@ -412,19 +414,20 @@ def ensemble_suite(nsys=64, seed=2024, n_range=(8000, 200000), max_cells=16, sub
         ph = dataclasses.replace(base, ext_force=g, seed=sub_seed)
         box_vol = 2.0 * m ** 3 * dx ** 3
         lmin = m * dx
-        if nc == 0 or hct < 0.01:
+        d_min, d_max = 4.5, 0.55 * lmin
+        if nc == 0 or hct < 0.01 or d_max < d_min:
             nc, d = 0, None
         else:
             d = (hct * box_vol / (nc * vol1)) ** (1.0 / 3.0)
-            d = float(min(max(d, 3.0), 0.55 * lmin))
+            d = float(min(max(d, d_min), d_max))
         cfg = None
         while cfg is None:
             try:
                 cfg = suspension(nx=2 * m, ny=m, nz=m, ncells=nc, subdiv=subdiv, seed=sub_seed, phys=ph,
                                  name=f"ensemble{s}", diameter=d, max_tries=4000)
             except RuntimeError:   # no room left for a cell: make the cells smaller, then fewer
-                if d > 3.0:
-                    d = max(3.0, 0.9 * d)
+                if d > d_min:
+                    d = max(d_min, 0.9 * d)
                 else:
                     nc -= 1
         built = nc * vol1 * d ** 3 / box_vol if nc else 0.0
