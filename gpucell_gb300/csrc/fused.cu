@@ -292,6 +292,24 @@ __global__ void fk_copy_slots(int n, SlotArrays src, SlotArrays dst) {
     if (dst.sys) dst.sys[q] = src.sys[q];
 }
 
+// Candidates [b, e) of one row of cubes against xs, the image of slot i's
+// position that the row needs; appends the ones within the cut-off to the
+// list of slot i (entry k at lst[32 k]).
+__device__ __forceinline__ void scan_range(const float4* __restrict__ pos, unsigned b, unsigned e, float3 xs, int i,
+                                           float cut2, bool mobile_only, unsigned fl, int cap,
+                                           int* __restrict__ lst, int& k) {
+#pragma unroll 4
+    for (unsigned j = b; j < e; ++j) {
+        float4 xj = pos[j];
+        float dx = xs.x - xj.x, dy = xs.y - xj.y, dz = xs.z - xj.z;
+        float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 >= cut2 || (int)j == i) continue;
+        if (mobile_only && fid(xj) < fl) continue;
+        if (k < cap) lst[(size_t)k * 32] = (int)j;
+        ++k;
+    }
+}
+
 // One thread per slot scans the cubes of its system's list grid around its
 // own.  Fluid and membrane slots list every particle within rc + skin;
 // Bound2 slots list the moving particles (for their wall velocity); Bound1
@@ -313,17 +331,8 @@ __global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, const SysInfo* __
     int k = 0;
     const GcGrid& g = S.g;
     const unsigned fl = S.fl;
-    auto scan = [&](unsigned b, unsigned e, float sx, float sy, float sz) {
-        for (unsigned j = b; j < e; ++j) {
-            float4 xj = pos[j];
-            float dx = (xi.x - xj.x) + sx, dy = (xi.y - xj.y) + sy, dz = (xi.z - xj.z) + sz;
-            float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 >= cut2 || (int)j == i) continue;
-            if (t == PT_B2 && fid(xj) < fl) continue;
-            if (k < cap) nbr[sell(i, k, cap)] = (int)j;
-            ++k;
-        }
-    };
+    int* lst = nbr + sell(i, 0, cap);
+    const bool mobile_only = t == PT_B2;
     if (t != PT_B1) {
         int cx = cube_coord(xi.x, 0, g), cy = cube_coord(xi.y, 1, g), cz = cube_coord(xi.z, 2, g);
         for (int dz = -1; dz <= 1; ++dz) {
@@ -338,14 +347,16 @@ __global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, const SysInfo* __
                 else if (y >= g.n[1]) { if (!(g.pmask & 2)) continue; y -= g.n[1]; sy = -g.L[1]; }
                 int row = S.cube0 + g.n[0] * (y + g.n[1] * z);
                 if (cx >= 1 && cx + 1 < g.n[0]) {
-                    scan(start[row + cx - 1], start[row + cx + 2], 0.f, sy, sz);
+                    scan_range(pos, start[row + cx - 1], start[row + cx + 2], f3(xi.x, xi.y + sy, xi.z + sz), i,
+                               cut2, mobile_only, fl, cap, lst, k);
                 } else {
                     for (int dx = -1; dx <= 1; ++dx) {
                         int x = cx + dx;
                         float sx = 0.f;
                         if (x < 0) { if (!(g.pmask & 1)) continue; x += g.n[0]; sx = g.L[0]; }
                         else if (x >= g.n[0]) { if (!(g.pmask & 1)) continue; x -= g.n[0]; sx = -g.L[0]; }
-                        scan(start[row + x], start[row + x + 1], sx, sy, sz);
+                        scan_range(pos, start[row + x], start[row + x + 1], f3(xi.x + sx, xi.y + sy, xi.z + sz), i,
+                                   cut2, mobile_only, fl, cap, lst, k);
                     }
                 }
             }
@@ -493,9 +504,10 @@ __global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, 
 #endif
 constexpr int kForceGroup = GC_FORCE_GROUP;
 constexpr int kForceAhead = GC_FORCE_AHEAD;   // groups of list indices loaded ahead
-constexpr int force_min_blocks(bool ens) {
-    return (kForceGroup == 1 ? 6 : (kForceGroup == 2 ? 4 : 3)) - (ens ? 1 : 0);
-}
+#ifndef GC_FORCE_MIN_BLOCKS
+#define GC_FORCE_MIN_BLOCKS (kForceGroup == 1 ? 6 : (kForceGroup == 2 ? 4 : 3))
+#endif
+constexpr int force_min_blocks(bool ens) { return GC_FORCE_MIN_BLOCKS - (ens ? 1 : 0); }
 
 template <bool COMPACT, bool ENS>
 __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
