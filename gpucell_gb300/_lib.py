@@ -129,6 +129,8 @@ _SIGS = {
     "gc_fused_get_options": [_P, _P],
     "gc_fused_set_options": [_P, _P],
     "gc_fused_autotune": [_P, _I, _I, _I, _P, _P],
+    "gc_fused_checkpoint": [_P, C.c_char_p],
+    "gc_fused_restore": [_P, C.c_char_p],
     "gc_fused_destroy": [_P],
     "gc_ensemble_create": [_I, _P, _I, _P, _P],
     "gc_ensemble_size": [_P, _P, _P],

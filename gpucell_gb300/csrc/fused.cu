@@ -37,6 +37,7 @@
 #include "gc_internal.cuh"
 
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -703,7 +704,7 @@ __global__ void fk_mgeo(GcParams p, const SysInfo* __restrict__ sys, const int* 
                         const float4* __restrict__ mpos, const int4* __restrict__ mnt, float* __restrict__ tarea,
                         float4* __restrict__ tnorm, float4* __restrict__ tcen, float* __restrict__ reftarea,
                         double* __restrict__ carea, double* __restrict__ cvol, double* __restrict__ crefarea,
-                        double* __restrict__ crefvol, float* __restrict__ parea, int setup, unsigned* flags) {
+                        double* __restrict__ crefvol, int setup, unsigned* flags) {
     __shared__ double sh[32];
     int c = blockIdx.x;
     int2 be = betri[c];
@@ -730,6 +731,7 @@ __global__ void fk_mgeo(GcParams p, const SysInfo* __restrict__ sys, const int* 
         int a = v.x - 1, b = v.y - 1, cc = v.z - 1;
         if (a < 0 || b < 0 || cc < 0 || a >= ncp || b >= ncp || cc >= ncp) {
             raise_flag(flags, GC_FLAG_BAD_INDEX);
+            tarea[t] = 0.f;
             continue;
         }
         float3 u1 = mdiff(mpos, mnt, a, r, g);
@@ -749,10 +751,6 @@ __global__ void fk_mgeo(GcParams p, const SysInfo* __restrict__ sys, const int* 
         double v1x = u1.x, v1y = u1.y, v1z = u1.z, v2x = u2.x, v2y = u2.y, v2z = u2.z, v3x = u3.x, v3y = u3.y,
                v3z = u3.z;
         accV += (v1x * (v2y * v3z - v2z * v3y) + v1y * (v2z * v3x - v2x * v3z) + v1z * (v2x * v3y - v2y * v3x)) / 6.0;
-        float a3 = A * (1.f / 3.f);
-        atomicAdd(&parea[a], a3);
-        atomicAdd(&parea[b], a3);
-        atomicAdd(&parea[cc], a3);
     }
     double Ac = block_sum_d(accA, sh);
     double Vc = block_sum_d(accV, sh);
@@ -829,22 +827,25 @@ __global__ void fk_mech_setup(GcParams p, const SysInfo* __restrict__ sys, const
     refang[e] = atan2f(D.s, D.c);
 }
 
-__device__ __forceinline__ void add4(float4* o, float3 f) {
-    atomicAdd(&o->x, f.x);
-    atomicAdd(&o->y, f.y);
-    atomicAdd(&o->z, f.z);
-}
+// The edge and triangle kernels write the force on each of their vertices
+// into a slot of their own (edge e, vertex r of p1..p4: part 4e + r;
+// triangle t, vertex r: part 4 nedge + 3t + r); fk_mgather then sums each
+// vertex's parts in a fixed order.  No float atomics, so the membrane forces
+// -- and with them the whole step -- are the same from run to run.
+__device__ __forceinline__ float4 part(float3 f) { return make_float4(f.x, f.y, f.z, 0.f); }
 
 __global__ void fk_medge(GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ msys, int nedge,
                          const int6* __restrict__ edge, const float4* __restrict__ mpos, const int4* __restrict__ mnt,
                          const float* __restrict__ lmax, const float* __restrict__ perlen,
                          const float* __restrict__ hpow, const float* __restrict__ refang,
-                         const float* __restrict__ hbend, float4* __restrict__ mforce, unsigned* flags) {
+                         const float* __restrict__ hbend, float4* __restrict__ parts, unsigned* flags) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nedge) return;
     int a, b, c, d;
+    float4* out = parts + 4 * (size_t)e;
     if (!edge_ok(edge[e], (int)p.nCP, &a, &b, &c, &d)) {
         raise_flag(flags, GC_FLAG_BAD_INDEX);
+        out[0] = out[1] = out[2] = out[3] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
     const GcGrid& g = sys[msys ? msys[a] : 0].g;
@@ -876,10 +877,10 @@ __global__ void fk_medge(GcParams p, const SysInfo* __restrict__ sys, const int*
         f2 -= dE * D.gk;
         f4 -= dE * D.gl;
     }
-    add4(&mforce[a], f1);
-    add4(&mforce[b], f2);
-    add4(&mforce[c], f3v);
-    add4(&mforce[d], f4);
+    out[0] = part(f1);
+    out[1] = part(f2);
+    out[2] = part(f3v);
+    out[3] = part(f4);
 }
 
 __global__ void fk_mtri(GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ cellsys, int ncell,
@@ -888,7 +889,7 @@ __global__ void fk_mtri(GcParams p, const SysInfo* __restrict__ sys, const int* 
                         const float* __restrict__ hl, const float* __restrict__ hg, const float* __restrict__ hv,
                         const double* __restrict__ carea, const double* __restrict__ cvol,
                         const double* __restrict__ crefarea, const double* __restrict__ crefvol,
-                        float4* __restrict__ mforce, int ntri) {
+                        float4* __restrict__ parts, int ntri) {
     // one block per cell: the cell's coefficients are read once
     int c = blockIdx.x;
     int2 be = betri[c];
@@ -900,6 +901,8 @@ __global__ void fk_mtri(GcParams p, const SysInfo* __restrict__ sys, const int* 
     for (int t = be.x + threadIdx.x; t <= be.y; t += blockDim.x) {
         int3 v = tri[t];
         int a = v.x - 1, b = v.y - 1, cc = v.z - 1;
+        float4* out = parts + 3 * (size_t)t;
+        out[0] = out[1] = out[2] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (a < 0 || b < 0 || cc < 0 || a >= ncp || b >= ncp || cc >= ncp) continue;
         float3 x2 = mdiff(mpos, mnt, b, a, g), x3 = mdiff(mpos, mnt, cc, a, g);
         float3 xi = cross3(x2, x3);
@@ -912,10 +915,31 @@ __global__ void fk_mtri(GcParams p, const SysInfo* __restrict__ sys, const int* 
         float cV = hv[t] * dV * (1.f / 6.f);
         float3 g1 = 0.5f * cross3(nh, x3 - x2), g2 = 0.5f * cross3(nh, -x3), g3 = 0.5f * cross3(nh, x2);
         float3 fv = -cV * xi;
-        add4(&mforce[a], fv - cA * g1);
-        add4(&mforce[b], fv - cA * g2);
-        add4(&mforce[cc], fv - cA * g3);
+        out[0] = part(fv - cA * g1);
+        out[1] = part(fv - cA * g2);
+        out[2] = part(fv - cA * g3);
     }
+}
+
+// Per vertex: the sum of its edge and triangle parts (in the fixed order of
+// the incidence list: its edges, then its triangles, each by index) and its
+// area, a third of each incident triangle.
+__global__ void fk_mgather(int ncp, int nedge, const int* __restrict__ inc_ptr, const int* __restrict__ inc,
+                           const float4* __restrict__ parts, const float* __restrict__ tarea,
+                           float4* __restrict__ mforce, float* __restrict__ parea) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= ncp) return;
+    float3 f = f3(0.f, 0.f, 0.f);
+    float a = 0.f;
+    const int tri0 = 4 * nedge;
+    for (int q = inc_ptr[v]; q < inc_ptr[v + 1]; ++q) {
+        int k = inc[q];
+        float4 x = parts[k];
+        f += f3(x.x, x.y, x.z);
+        if (k >= tri0) a += tarea[(k - tri0) / 3] * (1.f / 3.f);
+    }
+    mforce[v] = make_float4(f.x, f.y, f.z, 0.f);
+    parea[v] = a;
 }
 
 // Morse aggregation on membrane-only grids (cubes at least MaxCut wide).
@@ -1097,6 +1121,23 @@ __global__ void fk_count_stats(int n, const int* __restrict__ cnt, unsigned long
     }
 }
 
+// slot of every id from the ids carried in the positions (restore)
+__global__ void fk_slot_of(int n, const float4* __restrict__ pos, int* __restrict__ slot_of, unsigned* flags) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    unsigned id = fid(pos[q]);
+    if (id >= (unsigned)n) {
+        raise_flag(flags, GC_FLAG_BAD_INDEX);
+        return;
+    }
+    slot_of[id] = q;
+}
+
+__global__ void fk_iota(int n, int* __restrict__ v) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) v[q] = q;
+}
+
 // system index of the slots (set-up, slot = id)
 __global__ void fk_fill_sys(int n, const SysInfo* __restrict__ sys, int nsys, int* __restrict__ sysid) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1199,6 +1240,8 @@ struct GcFused {
     int4* mnthro = nullptr;
     float* parea = nullptr;
     int *mkeys = nullptr, *mvals = nullptr;
+    float4* mparts = nullptr;    // per-edge and per-triangle vertex forces (4 per edge, then 3 per triangle)
+    int *inc_ptr = nullptr, *inc = nullptr;   // vertex -> its parts (CSR)
     bool cells_adopted = false;   // membranes taken from the boundary entry points' buffers
     bool have_agg = false;
     bool setup_done = false;
@@ -1421,20 +1464,21 @@ int launch_density(GcFused* f, cudaStream_t st, const GcParams& p, bool mark) {
 
 int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p) {
     if (f->ncell <= 0) return GC_OK;
-    GC_CUDA(cudaMemsetAsync(f->mforce, 0, (size_t)f->ncp * sizeof(float4), st), "fused: clear mforce");
-    GC_CUDA(cudaMemsetAsync(f->parea, 0, (size_t)f->ncp * sizeof(float), st), "fused: clear parea");
     fk_mgeo<<<f->ncell, 256, 0, st>>>(p, f->dsys, f->cellsys, f->ncell, f->ntri, f->tri, f->betri, f->mpos, f->mnthro,
                                      f->tarea, f->tnorm, f->tcen, f->reftarea, f->carea, f->cvol, f->crefarea,
-                                     f->crefvol, f->parea, 0, f->flags);
+                                     f->crefvol, 0, f->flags);
     GC_CHECK_LAUNCH("fused: membrane geometry");
     fk_medge<<<gc_blocks(f->nedge, f->block), f->block, 0, st>>>(p, f->dsys, f->msys, f->nedge, f->edge, f->mpos,
                                                                  f->mnthro, f->lmax, f->perlen, f->hpow, f->refang,
-                                                                 f->hbend, f->mforce, f->flags);
+                                                                 f->hbend, f->mparts, f->flags);
     GC_CHECK_LAUNCH("fused: membrane edges");
     fk_mtri<<<f->ncell, 256, 0, st>>>(p, f->dsys, f->cellsys, f->ncell, f->betri, f->tri, f->mpos, f->mnthro,
                                      f->reftarea, f->hl, f->hg, f->hv, f->carea, f->cvol, f->crefarea, f->crefvol,
-                                     f->mforce, f->ntri);
+                                     f->mparts + 4 * (size_t)f->nedge, f->ntri);
     GC_CHECK_LAUNCH("fused: membrane triangles");
+    fk_mgather<<<gc_blocks(f->ncp, f->block), f->block, 0, st>>>(f->ncp, f->nedge, f->inc_ptr, f->inc, f->mparts,
+                                                                 f->tarea, f->mforce, f->parea);
+    GC_CHECK_LAUNCH("fused: membrane forces per vertex");
     if (f->have_agg) {
         fk_mkey<<<gc_blocks(f->ncp, f->block), f->block, 0, st>>>(f->ncp, f->dsys, f->msys, f->mpos, f->mkeys,
                                                                   f->mvals);
@@ -1756,8 +1800,43 @@ int alloc_cells(GcFused* f, int ncell, int ntri, int nedge, int ncp) {
     GC_TRY(falloc(f, &f->parea, ncp));
     GC_TRY(falloc(f, &f->mkeys, ncp));
     GC_TRY(falloc(f, &f->mvals, ncp));
+    GC_TRY(falloc(f, &f->mparts, 4 * (size_t)nedge + 3 * (size_t)ntri));
+    GC_TRY(falloc(f, &f->inc_ptr, (size_t)ncp + 1));
+    GC_TRY(falloc(f, &f->inc, 4 * (size_t)nedge + 3 * (size_t)ntri));
     GC_CUDA(cudaMemsetAsync(f->magg, 0, (size_t)ncp * sizeof(float4), f->st), "fused: magg");
     f->have_agg = f->p.De != 0.f && f->p.maxcut > 0.f;
+    return GC_OK;
+}
+
+// Vertex -> part incidence (CSR) from the global 1-based topology (host
+// arrays): for every vertex its edge parts in edge order, then its triangle
+// parts in triangle order.  Out-of-range indices contribute nothing.
+int build_incidence(GcFused* f, const int* tri, const int* edge) {
+    const int ncp = f->ncp, ne = f->nedge, nt = f->ntri;
+    std::vector<int> cnt((size_t)ncp + 1, 0);
+    auto ok = [&](int v) { return v >= 1 && v <= ncp; };
+    for (int e = 0; e < ne; ++e)
+        for (int r = 0; r < 4; ++r)
+            if (ok(edge[6 * (size_t)e + r])) ++cnt[edge[6 * (size_t)e + r]];
+    for (int t = 0; t < nt; ++t)
+        for (int r = 0; r < 3; ++r)
+            if (ok(tri[3 * (size_t)t + r])) ++cnt[tri[3 * (size_t)t + r]];
+    std::vector<int> ptr((size_t)ncp + 1, 0);
+    for (int v = 0; v < ncp; ++v) ptr[v + 1] = ptr[v] + cnt[v + 1];
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1), inc((size_t)ptr[ncp]);
+    for (int e = 0; e < ne; ++e)
+        for (int r = 0; r < 4; ++r) {
+            int v = edge[6 * (size_t)e + r];
+            if (ok(v)) inc[fill[v - 1]++] = 4 * e + r;
+        }
+    for (int t = 0; t < nt; ++t)
+        for (int r = 0; r < 3; ++r) {
+            int v = tri[3 * (size_t)t + r];
+            if (ok(v)) inc[fill[v - 1]++] = 4 * ne + 3 * t + r;
+        }
+    GC_CUDA(cudaMemcpyAsync(f->inc_ptr, ptr.data(), ptr.size() * 4, cudaMemcpyHostToDevice, f->st), "fused: incidence");
+    GC_CUDA(cudaMemcpyAsync(f->inc, inc.data(), inc.size() * 4, cudaMemcpyHostToDevice, f->st), "fused: incidence");
+    GC_CUDA(cudaStreamSynchronize(f->st), "fused: incidence");
     return GC_OK;
 }
 
@@ -1823,6 +1902,7 @@ int finalize_cells(GcFused* f) {
     GC_TRY(up(f->hl, hl.data(), hl.size() * 4));
     GC_TRY(up(f->hg, hg.data(), hg.size() * 4));
     GC_TRY(up(f->hv, hv.data(), hv.size() * 4));
+    GC_TRY(build_incidence(f, tri.data(), edge.data()));
     if (f->nsys > 1) {
         GC_TRY(falloc(f, &f->msys, f->ncp));
         GC_TRY(falloc(f, &f->cellsys, ncell));
@@ -2128,15 +2208,15 @@ int gc_fused_setup(GcFused* f) {
         fk_gather_mpos<<<gc_blocks(f->ncp, 256), 256, 0, st>>>(f->ncp, f->dsys, f->msys, f->slot_of, f->a.pos,
                                                               f->a.nthro, f->mpos, f->mnthro);
         GC_CHECK_LAUNCH("fused: membrane positions");
-        GC_CUDA(cudaMemsetAsync(f->parea, 0, (size_t)f->ncp * sizeof(float), st), "fused: parea");
         fk_mgeo<<<f->ncell, 256, 0, st>>>(p, f->dsys, f->cellsys, f->ncell, f->ntri, f->tri, f->betri, f->mpos,
                                          f->mnthro, f->tarea, f->tnorm, f->tcen, f->reftarea, f->carea, f->cvol,
-                                         f->crefarea, f->crefvol, f->parea, 1, f->flags);
+                                         f->crefarea, f->crefvol, 1, f->flags);
         GC_CHECK_LAUNCH("fused: set-up geometry");
         fk_mech_setup<<<gc_blocks(f->nedge, f->block), f->block, 0, st>>>(
             p, f->dsys, f->msys, f->nedge, f->edge, f->mpos, f->mnthro, f->shear, f->bend, f->l0, f->lmax, f->perlen,
             f->hpow, f->hbend, f->refang, f->flags);
         GC_CHECK_LAUNCH("fused: set-up mechanics");
+        GC_TRY(launch_membranes(f, st, p));   // membrane outputs of the loaded state
     }
     f->step = -1;
     GC_TRY(sync_dstep(f));
@@ -2391,6 +2471,202 @@ int gc_fused_destroy(GcFused* f) {
 }
 
 }  // extern "C"
+
+
+// ---------------------------------------------------------------------------
+// Checkpoint and restart.
+//
+// The file holds what the next steps depend on: the slot-ordered state (with
+// the slot order itself, through the ids in the positions), the positions
+// and cube keys the current neighbour lists were built from, the density
+// and pressure, the step index that keys the noise, and the membrane
+// reference geometry recorded at set-up.  A restore rebuilds the lists from
+// those positions and keys without re-sorting, which reproduces them entry
+// for entry, so that a restored run continues bit for bit as the original
+// would have (host-driven steps; captured steps rebuild their lists when
+// they are captured).  Layout, little-endian: a 128-byte header, one
+// 16-byte record per system (particles, membrane vertices, seed), then the
+// arrays in the order of ckpt_arrays.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct CkptHeader {
+    char magic[8];
+    uint32_t version, nsys;
+    uint64_t n, ncp, ncell, ntri, nedge;
+    int64_t step;
+    float skin_rel;
+    int32_t K;
+    uint32_t has_sys, has_cells;
+    uint8_t reserved[128 - 8 - 8 - 40 - 8 - 4 - 4 - 8];
+};
+static_assert(sizeof(CkptHeader) == 128, "checkpoint header is 128 bytes");
+
+struct CkptSys {
+    uint32_t n, ncp;
+    uint64_t seed;
+};
+
+struct CkptArray {
+    void* dev;
+    size_t bytes;
+};
+
+std::vector<CkptArray> ckpt_arrays(GcFused* f) {
+    size_t n = f->n;
+    std::vector<CkptArray> v = {
+        {f->a.pos, n * 16}, {f->a.vel, n * 16}, {f->a.vpred, n * 16}, {f->a.vh, n * 16}, {f->a.force, n * 16},
+        {f->a.nthro, n * 16}, {f->refpos, n * 16}, {f->keys, n * 4}, {f->dp, n * 8}};
+    if (f->a.sys) v.push_back({f->a.sys, n * 4});
+    if (f->ncell > 0) {
+        size_t nt = f->ntri, nc = f->ncell, ne = f->nedge;
+        v.push_back({f->reftarea, nt * 4});
+        v.push_back({f->crefarea, nc * 8});
+        v.push_back({f->crefvol, nc * 8});
+        for (float* q : {f->l0, f->lmax, f->perlen, f->hpow, f->hbend, f->refang}) v.push_back({q, ne * 4});
+    }
+    return v;
+}
+
+void ckpt_header(GcFused* f, CkptHeader* h) {
+    memset(h, 0, sizeof(*h));
+    memcpy(h->magic, "GCFCKPT1", 8);
+    h->version = 1;
+    h->nsys = f->nsys;
+    h->n = f->n;
+    h->ncp = f->ncp;
+    h->ncell = f->ncell;
+    h->ntri = f->ntri;
+    h->nedge = f->nedge;
+    h->step = f->step;
+    h->skin_rel = f->skin_rel;
+    h->K = f->K;
+    h->has_sys = f->a.sys ? 1 : 0;
+    h->has_cells = f->ncell > 0 ? 1 : 0;
+}
+
+// The lists exactly as the last rebuild made them: the cube starts from the
+// saved (sorted) keys and the scan over the saved build positions.
+int rebuild_from_ref(GcFused* f) {
+    const int n = f->n, nb = gc_blocks(n, f->block);
+    cudaStream_t st = f->st;
+    fk_iota<<<nb, f->block, 0, st>>>(n, f->vals);
+    GC_CHECK_LAUNCH("restore: identity");
+    GC_TRY(gc_counting_sort_bufs(n, f->K, f->keys, f->vals, f->sb, f->flags, st));
+    float cut = f->p.rc + f->skin;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        GC_CUDA(cudaMemsetAsync(f->oflag, 0, sizeof(unsigned), st), "restore: flags");
+        fk_build_list<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->refpos, f->sb.cnt, f->nbr, f->cnt, f->cap,
+                                              cut * cut, f->oflag);
+        GC_CHECK_LAUNCH("restore: build lists");
+        GC_CUDA(cudaMemcpyAsync(&f->h->oflag, f->oflag, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "restore");
+        GC_CUDA(cudaStreamSynchronize(st), "restore");
+        if (!(f->h->oflag & GC_FLAG_CELL_OVERFLOW)) return GC_OK;
+        GC_TRY(alloc_list(f, f->cap * 2));
+    }
+    return gc_fail(GC_EDEVICE, "restore: neighbour lists overflow %d entries", f->cap);
+}
+
+}  // namespace
+
+extern "C" int gc_fused_checkpoint(GcFused* f, const char* path) {
+    if (!f || !path) return gc_fail(GC_EINVAL, "checkpoint: NULL argument");
+    if (!f->setup_done) return gc_fail(GC_ESTATE, "checkpoint: call gc_fused_setup first");
+    FILE* fp = fopen(path, "wb");
+    if (!fp) return gc_fail(GC_EINVAL, "checkpoint: cannot open %s for writing", path);
+    CkptHeader h;
+    ckpt_header(f, &h);
+    std::vector<CkptSys> sys(f->nsys);
+    for (int s = 0; s < f->nsys; ++s) {
+        sys[s].n = f->hsys[s].end - f->hsys[s].id0;
+        sys[s].ncp = f->hsys[s].end - f->hsys[s].cs;
+        sys[s].seed = f->hsys[s].seed;
+    }
+    bool ok = fwrite(&h, sizeof(h), 1, fp) == 1 && fwrite(sys.data(), sizeof(CkptSys), sys.size(), fp) == sys.size();
+    std::vector<char> buf;
+    int rc = GC_OK;
+    for (const CkptArray& a : ckpt_arrays(f)) {
+        if (!ok) break;
+        buf.resize(a.bytes);
+        cudaError_t e = cudaMemcpyAsync(buf.data(), a.dev, a.bytes, cudaMemcpyDeviceToHost, f->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(f->st);
+        if (e != cudaSuccess) {
+            rc = gc_cuda_fail(e, "checkpoint: read state");
+            break;
+        }
+        ok = fwrite(buf.data(), 1, a.bytes, fp) == a.bytes;
+    }
+    if (fclose(fp) != 0) ok = false;
+    if (rc != GC_OK) return rc;
+    if (!ok) return gc_fail(GC_EINVAL, "checkpoint: write to %s failed", path);
+    return GC_OK;
+}
+
+extern "C" int gc_fused_restore(GcFused* f, const char* path) {
+    if (!f || !path) return gc_fail(GC_EINVAL, "restore: NULL argument");
+    if (!f->setup_done) return gc_fail(GC_ESTATE, "restore: set the handle up as for the original run first");
+    FILE* fp = fopen(path, "rb");
+    if (!fp) return gc_fail(GC_EINVAL, "restore: cannot open %s", path);
+    CkptHeader h;
+    int rc = GC_OK;
+    std::vector<CkptSys> sys;
+    if (fread(&h, sizeof(h), 1, fp) != 1 || memcmp(h.magic, "GCFCKPT1", 8) != 0 || h.version != 1) {
+        rc = gc_fail(GC_EINVAL, "restore: %s is not a checkpoint of this library", path);
+    } else if (h.nsys != (uint32_t)f->nsys || h.n != (uint64_t)f->n || h.ncp != (uint64_t)f->ncp ||
+               h.ncell != (uint64_t)f->ncell || h.ntri != (uint64_t)f->ntri || h.nedge != (uint64_t)f->nedge ||
+               h.has_sys != (f->a.sys ? 1u : 0u)) {
+        rc = gc_fail(GC_EINVAL, "restore: the checkpoint holds another configuration (%llu particles in %u systems, "
+                                "%llu cells; this handle: %d in %d, %d)",
+                     (unsigned long long)h.n, h.nsys, (unsigned long long)h.ncell, f->n, f->nsys, f->ncell);
+    } else {
+        sys.resize(h.nsys);
+        if (fread(sys.data(), sizeof(CkptSys), sys.size(), fp) != sys.size()) {
+            rc = gc_fail(GC_EINVAL, "restore: %s is truncated", path);
+        } else {
+            for (int s = 0; s < f->nsys && rc == GC_OK; ++s)
+                if (sys[s].n != f->hsys[s].end - f->hsys[s].id0 || sys[s].ncp != f->hsys[s].end - f->hsys[s].cs ||
+                    sys[s].seed != f->hsys[s].seed)
+                    rc = gc_fail(GC_EINVAL, "restore: system %d differs from the checkpoint's", s);
+        }
+    }
+    if (rc == GC_OK && h.skin_rel != f->skin_rel) {   // the lists were built at the checkpoint's skin
+        f->skin_rel = h.skin_rel;
+        f->skin = f->skin_rel * f->p.rc;
+        rc = build_grids(f);
+    }
+    if (rc == GC_OK && h.K != f->K) rc = gc_fail(GC_EINVAL, "restore: the cube grids differ from the checkpoint's");
+    std::vector<char> buf;
+    for (const CkptArray& a : ckpt_arrays(f)) {
+        if (rc != GC_OK) break;
+        buf.resize(a.bytes);
+        if (fread(buf.data(), 1, a.bytes, fp) != a.bytes) {
+            rc = gc_fail(GC_EINVAL, "restore: %s is truncated", path);
+            break;
+        }
+        cudaError_t e = cudaMemcpyAsync(a.dev, buf.data(), a.bytes, cudaMemcpyHostToDevice, f->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(f->st);   // the host buffer is reused
+        if (e != cudaSuccess) rc = gc_cuda_fail(e, "restore: write state");
+    }
+    fclose(fp);
+    if (rc != GC_OK) return rc;
+    const int n = f->n;
+    cudaStream_t st = f->st;
+    fk_slot_of<<<gc_blocks(n, 256), 256, 0, st>>>(n, f->a.pos, f->slot_of, f->flags);
+    GC_CHECK_LAUNCH("restore: slots");
+    if (f->ncell > 0) {
+        fk_gather_mpos<<<gc_blocks(f->ncp, 256), 256, 0, st>>>(f->ncp, f->dsys, f->msys, f->slot_of, f->a.pos,
+                                                              f->a.nthro, f->mpos, f->mnthro);
+        GC_CHECK_LAUNCH("restore: membrane positions");
+    }
+    GC_TRY(rebuild_from_ref(f));
+    f->step = h.step;
+    GC_TRY(sync_dstep(f));
+    drop_graphs(f);
+    GcParams p = f->p;
+    GC_TRY(launch_membranes(f, st, p));   // membrane outputs of the restored state
+    GC_CUDA(cudaStreamSynchronize(st), "restore");
+    return GC_OK;
+}
 
 // ---------------------------------------------------------------------------
 // Autotuner: times short runs of candidate settings on the handle's own
@@ -2668,6 +2944,11 @@ int engine_cells(GcFused* f, const GcRefPtrs& r) {
     fk_import_cellrefs<<<gc_blocks(ncell, 128), 128, 0, st>>>(ncell, ntri, f->betri, r.refarea_para, r.refvol_para,
                                                             f->crefarea, f->crefvol);
     GC_CHECK_LAUNCH("fused engine: reference areas and volumes");
+    std::vector<int> htri(3 * (size_t)ntri), hedge(6 * (size_t)nedge);
+    GC_CUDA(cudaMemcpyAsync(htri.data(), f->tri, htri.size() * 4, cudaMemcpyDeviceToHost, st), "fused engine: topology");
+    GC_CUDA(cudaMemcpyAsync(hedge.data(), f->edge, hedge.size() * 4, cudaMemcpyDeviceToHost, st), "fused engine: topology");
+    GC_CUDA(cudaStreamSynchronize(st), "fused engine: topology");
+    GC_TRY(build_incidence(f, htri.data(), hedge.data()));
     return build_grids(f);   // aggregation grid
 }
 

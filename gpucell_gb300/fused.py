@@ -103,6 +103,12 @@ class _Handle:
         return dict(skin=round(float(o.skin), 6), block=o.block, compact=bool(o.compact), graph=bool(o.graph),
                     ms_per_step=ms.value)
 
+    def checkpoint(self, path):
+        _lib.call("gc_fused_checkpoint", self.h, str(path).encode())
+
+    def restore(self, path):
+        _lib.call("gc_fused_restore", self.h, str(path).encode())
+
     def close(self):
         if getattr(self, "h", None):
             _lib.call("gc_fused_destroy", self.h)

@@ -314,6 +314,83 @@ def channel(nx=64, ny=32, nz=32, wall_layers=3, b1_layers=0, cell_subdiv=3, cell
     return _assemble(name, bbox, 1 | 4, b1a, np.concatenate(b2), fluid, cells, phys, dx, wall_vel=wv)
 
 
+def couette(nx=64, ny=32, nz=32, wall_layers=3, ncells=4, subdiv=3, cell_diameter=None, shear_rate=0.5,
+            seed=12345, phys: Physics | None = None, name="couette") -> Config:
+    """Couette flow for aggregation: the walls of `channel` move in -x and +x
+    at -+U with U = shear_rate * Ly / 2 (prescribed through their VelHalf;
+    the shear rate is in reduced units, 1/time), no body force, and `ncells`
+    red cells stacked face to face across the channel (a rouleau: disc
+    normals along y, centres 0.42 d apart), so that neighbouring membranes
+    are within the Morse range.  The physics default turns aggregation on:
+    De = 3e-3, beta = 1.5, r0 = 0.3, cut-off 2.5."""
+    phys = phys or Physics(ext_force=0.0, sur_energy=3.0e-3, sca_fac=1.5, zero_len=0.3, max_cut=2.5)
+    dx = 1.0 / 3.0
+    Ly = ny * dx
+    d = cell_diameter if cell_diameter is not None else min(8.0 / 1.5, 0.45 * ny * dx)
+    u = shear_rate * Ly / 2.0
+    pitch = 0.42 * d
+    ys = (np.arange(ncells) - 0.5 * (ncells - 1)) * pitch
+    centers = [(0.0, float(y), 0.0) for y in ys]
+    if ncells and ((ncells - 1) * pitch + 0.35 * d > Ly - 2 * dx or d > min(nx, nz) * dx):
+        raise ValueError("channel too small for the cells")
+    return channel(nx=nx, ny=ny, nz=nz, wall_layers=wall_layers, b1_layers=0,
+                   cell_subdiv=subdiv if ncells else -1, cell_diameter=d, seed=seed, phys=phys,
+                   wall_vel=((-u, 0.0, 0.0), (u, 0.0, 0.0)), name=name,
+                   cell_centers=centers if ncells else None)
+
+
+def constriction(nx=96, ny=36, nz=24, wall_layers=3, b1_layers=1, ratio=2.0, ncells=2, subdiv=3,
+                 cell_diameter=None, seed=12345, phys: Physics | None = None, name="constriction") -> Config:
+    """Channel with a smooth 2:1 constriction of frozen wall particles: the
+    walls y = +-h(x) follow the signed-distance profile
+    h(x) = H - (H - H/ratio) (1 + cos(2 pi (x - Lx/2)/w))/2 for |x - Lx/2| < w/2
+    (w = Lx/3) and H elsewhere, H = Ly/2.  Every lattice site of the box
+    [0, Lx) x [-H - t, H + t) x [-Lz/2, Lz/2) (t = the wall thickness) with
+    |y| < h(x) is fluid, h(x) <= |y| < h(x) + wall_layers dx is Bound2 and the
+    next b1_layers dx is Bound1; the rest is empty.  Periodic in x and z;
+    the body force drives the flow through the throat (the pressure drop of a
+    driven inflow in a periodic channel).  Cells sit in the wide part,
+    upstream of the throat."""
+    phys = phys or Physics()
+    rng = np.random.default_rng(seed)
+    dx = 1.0 / 3.0
+    Lx, Ly, Lz = nx * dx, ny * dx, nz * dx
+    H = Ly / 2
+    t = (wall_layers + b1_layers) * dx
+    w = Lx / 3.0
+
+    def h(x):
+        s = np.abs(x - Lx / 2)
+        bump = 0.5 * (1 + np.cos(2 * np.pi * (x - Lx / 2) / w))
+        return np.where(s < w / 2, H - (H - H / ratio) * bump, H)
+
+    nyt = ny + 2 * (wall_layers + b1_layers)
+    lat = _lattice(nx, nyt, nz, dx, (0.0, -H - t, -Lz / 2), rng)
+    hx = h(lat[:, 0])
+    ay = np.abs(lat[:, 1])
+    fluid = lat[ay < hx]
+    b2 = lat[(ay >= hx) & (ay < hx + wall_layers * dx)]
+    b1 = lat[(ay >= hx + wall_layers * dx) & (ay < hx + t)]
+    cells = []
+    if ncells:
+        d = cell_diameter if cell_diameter is not None else 0.5 * H
+        v, f = icosphere(subdiv)
+        shape = biconcave(v, d)
+        rot = np.array([[0.0, 0, 1.0], [0, 1.0, 0], [-1.0, 0, 0]])   # disc normal along x (facing the flow)
+        zs = (np.arange(ncells) - 0.5 * (ncells - 1)) * (1.1 * d)
+        for z in zs:
+            if abs(z) + 0.55 * d > Lz / 2:
+                raise ValueError("box too thin for the cells")
+            cells.append((shape @ rot.T + np.array([Lx / 6, 0.0, z]), f))
+        mv = np.concatenate([c[0] for c in cells])
+        from scipy.spatial import cKDTree
+        tree = cKDTree(mv)
+        dist, _ = tree.query(fluid, k=1)
+        fluid = fluid[dist > 0.6 * dx]   # room for the membranes
+    bbox = [0.0, Lx, -H - t, H + t, -Lz / 2, Lz / 2]
+    return _assemble(name, bbox, 1 | 4, b1, b2, fluid, cells, phys, dx)
+
+
 def rbc_body_points(diameter: float, spacing: float, margin: float) -> np.ndarray:
     """Grid points inside the biconcave shape dilated by `margin` (body frame)."""
     R = 0.5 * diameter + margin

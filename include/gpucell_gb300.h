@@ -241,6 +241,16 @@ int gc_fused_set_options(GcFused* f, const GcFusedOptions* opt);
 #define GC_TUNE_CACHE 1
 int gc_fused_autotune(GcFused* f, int trial_steps, int drive_on, int flags, GcFusedOptions* chosen,
                       double* ms_per_step);
+/* Checkpoint and restart (no counterpart in the reference): writes the
+ * complete dynamic state to a binary file -- slot-ordered state, the
+ * positions and cube keys the neighbour lists were built from, density and
+ * pressure, the step index that keys the noise, the membrane reference
+ * geometry.  gc_fused_restore reads it into a handle created and set up as
+ * for the original run (same systems, constants, boxes and membranes) and
+ * rebuilds the lists exactly, so that host-driven steps continue bit for bit
+ * as the original run would have.  Synchronise. */
+int gc_fused_checkpoint(GcFused* f, const char* path);
+int gc_fused_restore(GcFused* f, const char* path);
 int gc_fused_destroy(GcFused* f);
 
 /* ---- ensembles of independent simulations (no counterpart) --------------

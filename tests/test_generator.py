@@ -75,3 +75,32 @@ def test_ensemble_suite_draws_within_the_stated_ranges():
     assert len(seeds) == 8
     again = gen.ensemble_suite(nsys=8, seed=3, n_range=(8000, 60000), max_cells=4, subdiv=1)
     assert all(np.array_equal(a.coor, b.coor) for a, b in zip(cfgs, again))
+
+
+def test_couette_walls_move_and_cells_touch():
+    cfg = gen.couette(nx=36, ny=18, nz=18, ncells=2, subdiv=2, cell_diameter=3.0, shear_rate=0.5)
+    u = 0.5 * (18 / 3.0) / 2
+    b2 = cfg.velhalf[cfg.n_b1:cfg.n_b1 + cfg.n_b2]
+    y = cfg.coor[cfg.n_b1:cfg.n_b1 + cfg.n_b2, 1]
+    assert np.allclose(b2[y < 0, 0], -u) and np.allclose(b2[y > 0, 0], u)
+    assert np.all(cfg.velhalf[cfg.n_b1 + cfg.n_b2:] == 0)
+    c = cfg.consts()
+    assert c["ConstExtForce"] == 0 and c["surEnergy"] > 0 and c["MaxCut"] == 2.5
+    m = cfg.coor[cfg.n_cell_start:].astype(np.float64)
+    a, b = m[:162], m[162:]
+    gap = np.sqrt(((a[:, None, :] - b[None, :, :]) ** 2).sum(-1)).min()
+    assert 0.0 < gap < c["MaxCut"]
+
+
+def test_constriction_walls_follow_the_profile():
+    cfg = gen.constriction(nx=48, ny=24, nz=18, ncells=2, subdiv=2, cell_diameter=2.4)
+    H = 24 / 3.0 / 2
+    fl = cfg.coor[cfg.n_b1 + cfg.n_b2:cfg.n_cell_start]
+    x, y = fl[:, 0], np.abs(fl[:, 1])
+    Lx = 48 / 3.0
+    throat = np.abs(x - Lx / 2) < 0.2
+    wide = x < Lx / 6 - 1.5
+    assert y[throat].max() < 0.52 * H and y[wide].max() > 0.9 * H   # 2:1
+    b2 = cfg.coor[cfg.n_b1:cfg.n_b1 + cfg.n_b2]
+    assert np.abs(b2[np.abs(b2[:, 0] - Lx / 2) < 0.2, 1]).min() >= 0.49 * H
+    assert cfg.n_b1 > 0 and cfg.ncell == 2 and cfg.pmask == 5
