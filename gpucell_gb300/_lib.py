@@ -71,6 +71,17 @@ assert C.sizeof(GcSystemDesc) == 128
 
 GC_TUNE_CACHE = 1
 
+
+class GcOutputFrame(C.Structure):
+    """ctypes mirror of GcOutputFrame (include/gpucell_gb300.h)."""
+
+    _fields_ = [("n", C.c_longlong), ("n_b1", C.c_longlong), ("n_b2", C.c_longlong), ("n_cell_start", C.c_longlong),
+                ("pos", C.c_void_p), ("vel", C.c_void_p), ("rho", C.c_void_p), ("press", C.c_void_p),
+                ("ncell", C.c_int), ("ntri", C.c_int), ("cell_verts", C.c_void_p), ("tri", C.c_void_p),
+                ("betri", C.c_void_p), ("defforce", C.c_void_p), ("aggforce", C.c_void_p),
+                ("tricenter", C.c_void_p), ("trinordir", C.c_void_p), ("cell_stats", C.c_void_p),
+                ("threads", C.c_int), ("reserved", C.c_int)]
+
 _P = C.c_void_p
 _I = C.c_int
 _U = C.c_uint
@@ -139,6 +150,10 @@ _SIGS = {
     "gc_ensemble_store": [_P, _I] + [_P] * 7 + [_I],
     "gc_ensemble_store_cells": [_P, _I] + [_P] * 7 + [_I],
     "gc_ensemble_cell_sums": [_P, _I, _P, _P],
+    "gc_ensemble_cell_stats": [_P, _I, _P],
+    "gc_ensemble_write_output": [_P, _I, C.c_char_p, C.c_longlong, C.c_double, _I, _I],
+    "gc_fused_write_output": [_P, C.c_char_p, C.c_longlong, C.c_double, _I, _I],
+    "gc_output_write": [_P, C.c_char_p, C.c_longlong, C.c_double, _I],
 }
 _RESTYPES = {"gc_last_error": C.c_char_p, "gc_get_step": C.c_longlong, "gc_launch_count": C.c_ulonglong}
 

@@ -75,7 +75,7 @@ def build_library(verbose: bool = False, extra_flags=None, force: bool = False) 
                     print(o)
     if jobs or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < _newest(objs):
         tmp = LIB_PATH + ".tmp"
-        _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs)
+        _run([nvcc] + ARCH + ["-shared", "-Xcompiler", "-pthread", "-o", tmp] + objs)
         os.replace(tmp, LIB_PATH)
     return LIB_PATH
 

@@ -41,6 +41,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -1138,6 +1139,40 @@ __global__ void fk_iota(int n, int* __restrict__ v) {
     if (q < n) v[q] = q;
 }
 
+// Per-cell statistics for GPUCell's per-cell time series: mean deformation
+// and aggregation force and mean velocity over the cell's vertices, the
+// magnitude of the mean velocity, area and volume; FP64 sums, one block per
+// cell.
+__global__ void fk_cell_stats(int c0, const int2* __restrict__ cell_verts, const SysInfo* __restrict__ sys,
+                              const int* __restrict__ cellsys, const int* __restrict__ slot_of,
+                              const float4* __restrict__ vel, const float4* __restrict__ mforce,
+                              const float4* __restrict__ magg, int have_agg, const double* __restrict__ carea,
+                              const double* __restrict__ cvol, double* __restrict__ out) {
+    __shared__ double sh[32];
+    const int c = c0 + blockIdx.x;
+    const int2 vr = cell_verts[c];
+    const SysInfo& S = sys[cellsys ? cellsys[c] : 0];
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int v = vr.x + threadIdx.x; v <= vr.y; v += blockDim.x) {
+        float4 m = mforce[v];
+        float4 a = have_agg ? magg[v] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 u = vel[slot_of[S.cs + (unsigned)(v - (int)S.m0)]];
+        acc[0] += (double)(m.x - a.x); acc[1] += (double)(m.y - a.y); acc[2] += (double)(m.z - a.z);
+        acc[3] += a.x; acc[4] += a.y; acc[5] += a.z;
+        acc[6] += u.x; acc[7] += u.y; acc[8] += u.z;
+    }
+    const double inv = 1.0 / (double)(vr.y - vr.x + 1);
+    double r[9];
+    for (int k = 0; k < 9; ++k) r[k] = block_sum_d(acc[k], sh) * inv;
+    if (threadIdx.x == 0) {
+        double* o = out + 12 * (size_t)blockIdx.x;
+        for (int k = 0; k < 9; ++k) o[k] = r[k];
+        o[9] = sqrt(r[6] * r[6] + r[7] * r[7] + r[8] * r[8]);
+        o[10] = carea[c];
+        o[11] = cvol[c];
+    }
+}
+
 // system index of the slots (set-up, slot = id)
 __global__ void fk_fill_sys(int n, const SysInfo* __restrict__ sys, int nsys, int* __restrict__ sysid) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1157,6 +1192,7 @@ struct HostCells {
     bool set = false;
     int ncell = 0, ntri = 0, nedge = 0;
     std::vector<int> tri, edge, betri, celltab;
+    std::vector<int> verts;   // first and last vertex of each cell (0-based), from its triangles
     std::vector<float> shear, bend, hl, hg, hv;
 };
 
@@ -1242,6 +1278,8 @@ struct GcFused {
     int *mkeys = nullptr, *mvals = nullptr;
     float4* mparts = nullptr;    // per-edge and per-triangle vertex forces (4 per edge, then 3 per triangle)
     int *inc_ptr = nullptr, *inc = nullptr;   // vertex -> its parts (CSR)
+    int2* cell_verts = nullptr;  // first and last membrane vertex of each cell (global, inclusive)
+    double* cell_stats = nullptr;   // ncell x 12, see gc_ensemble_cell_stats
     bool cells_adopted = false;   // membranes taken from the boundary entry points' buffers
     bool have_agg = false;
     bool setup_done = false;
@@ -1903,6 +1941,19 @@ int finalize_cells(GcFused* f) {
     GC_TRY(up(f->hg, hg.data(), hg.size() * 4));
     GC_TRY(up(f->hv, hv.data(), hv.size() * 4));
     GC_TRY(build_incidence(f, tri.data(), edge.data()));
+    {
+        std::vector<int> cv(2 * (size_t)ncell);
+        size_t oc2 = 0;
+        for (int s = 0; s < f->nsys; ++s) {
+            const HostCells& h = f->hcells[s];
+            if (!h.set) continue;
+            for (int k = 0; k < 2 * h.ncell; ++k) cv[2 * oc2 + k] = h.verts[k] + (int)f->hsys[s].m0;
+            oc2 += h.ncell;
+        }
+        GC_TRY(falloc(f, &f->cell_verts, ncell));
+        GC_TRY(falloc(f, &f->cell_stats, 12 * (size_t)ncell));
+        GC_TRY(up(f->cell_verts, cv.data(), cv.size() * 4));
+    }
     if (f->nsys > 1) {
         GC_TRY(falloc(f, &f->msys, f->ncp));
         GC_TRY(falloc(f, &f->cellsys, ncell));
@@ -2123,6 +2174,17 @@ int gc_ensemble_set_cells(GcFused* f, int sys, int ncell, int ntri, int nedge, c
     h.hl.assign(hlarea, hlarea + ntri);
     h.hg.assign(hgarea, hgarea + ntri);
     h.hv.assign(hvol, hvol + ntri);
+    h.verts.assign(2 * (size_t)ncell, 0);
+    for (int k = 0; k < ncell; ++k) {
+        int lo = ncp, hi = -1;
+        for (int t = betri[2 * k]; t <= betri[2 * k + 1]; ++t)
+            for (int q = 0; q < 3; ++q) {
+                lo = std::min(lo, tri[3 * t + q] - 1);
+                hi = std::max(hi, tri[3 * t + q] - 1);
+            }
+        h.verts[2 * k] = lo;
+        h.verts[2 * k + 1] = hi;
+    }
     return GC_OK;
 }
 
@@ -2356,6 +2418,74 @@ int gc_ensemble_cell_sums(GcFused* f, int sys, double* area, double* vol) {
     GC_TRY(check_sys(f, sys, "cell_sums"));
     if (!f->setup_done || !f->hcells[sys].set) return GC_OK;
     return cell_sums_range(f, f->c0[sys], f->hcells[sys].ncell, area, vol);
+}
+
+int gc_ensemble_cell_stats(GcFused* f, int sys, double* out) {
+    GC_TRY(check_sys(f, sys, "cell_stats"));
+    if (!out) return gc_fail(GC_EINVAL, "cell_stats: NULL output");
+    if (!f->setup_done) return gc_fail(GC_ESTATE, "cell_stats: call gc_fused_setup first");
+    const HostCells& h = f->hcells[sys];
+    if (!h.set || h.ncell <= 0) return GC_OK;
+    fk_cell_stats<<<h.ncell, 256, 0, f->st>>>(f->c0[sys], f->cell_verts, f->dsys, f->cellsys, f->slot_of, f->a.vel,
+                                             f->mforce, f->magg, f->have_agg ? 1 : 0, f->carea, f->cvol,
+                                             f->cell_stats);
+    GC_CHECK_LAUNCH("fused: cell statistics");
+    GC_CUDA(cudaMemcpyAsync(out, f->cell_stats, 12 * sizeof(double) * h.ncell, cudaMemcpyDeviceToHost, f->st),
+            "cell_stats");
+    GC_CUDA(cudaStreamSynchronize(f->st), "cell_stats");
+    return GC_OK;
+}
+
+int gc_ensemble_write_output(GcFused* f, int sys, const char* dir, long long step_data, double time, int first,
+                             int threads) {
+    GC_TRY(check_sys(f, sys, "write_output"));
+    if (!dir) return gc_fail(GC_EINVAL, "write_output: NULL directory");
+    if (!f->setup_done) return gc_fail(GC_ESTATE, "write_output: call gc_fused_setup first");
+    const SysInfo& S = f->hsys[sys];
+    const HostCells& h = f->hcells[sys];
+    const int n = (int)(S.end - S.id0), ncp = (int)(S.end - S.cs);
+    std::vector<float> pos(3 * (size_t)n), vel(3 * (size_t)n), rho(n), press(n);
+    GC_TRY(store_range(f, S.id0, n, pos.data(), vel.data(), rho.data(), press.data(), nullptr, nullptr, nullptr, 0));
+    GcOutputFrame fr;
+    memset(&fr, 0, sizeof(fr));
+    fr.n = n;
+    fr.n_b1 = S.b2 - S.id0;
+    fr.n_b2 = S.fl - S.b2;
+    fr.n_cell_start = S.cs - S.id0;
+    fr.pos = pos.data();
+    fr.vel = vel.data();
+    fr.rho = rho.data();
+    fr.press = press.data();
+    fr.threads = threads;
+    std::vector<float> def, agg, cen, nor;
+    std::vector<double> stats;
+    if (h.set && h.ncell > 0) {
+        def.resize(3 * (size_t)ncp);
+        agg.resize(3 * (size_t)ncp);
+        cen.resize(3 * (size_t)h.ntri);
+        nor.resize(3 * (size_t)h.ntri);
+        stats.resize(12 * (size_t)h.ncell);
+        GC_TRY(gc_ensemble_store_cells(f, sys, nullptr, nullptr, def.data(), agg.data(), nor.data(), cen.data(),
+                                       nullptr, 0));
+        GC_TRY(gc_ensemble_cell_stats(f, sys, stats.data()));
+        fr.ncell = h.ncell;
+        fr.ntri = h.ntri;
+        fr.cell_verts = h.verts.data();
+        fr.tri = h.tri.data();
+        fr.betri = h.betri.data();
+        fr.defforce = def.data();
+        fr.aggforce = agg.data();
+        fr.tricenter = cen.data();
+        fr.trinordir = nor.data();
+        fr.cell_stats = stats.data();
+    }
+    return gc_output_write(&fr, dir, step_data, time, first);
+}
+
+int gc_fused_write_output(GcFused* f, const char* dir, long long step_data, double time, int first, int threads) {
+    if (!f) return gc_fail(GC_EINVAL, "write_output: NULL handle");
+    if (f->nsys != 1) return gc_fail(GC_EINVAL, "write_output: an ensemble writes one system at a time");
+    return gc_ensemble_write_output(f, 0, dir, step_data, time, first, threads);
 }
 
 int gc_fused_stats(GcFused* f, long long* rebuilds, long long* steps, int* list_capacity, double* mean_neighbors,

@@ -1,0 +1,297 @@
+// output.cu -- GPUCell's output files, written from host arrays.
+//
+// The reference writes, per output step (Particle::OutputPar,
+// src/Particle.cu:681-691), six Tecplot text files and appends one line per
+// cell to two time series:
+//
+//   FluidCoor/<step>.plt   zones Bound1, Bound2, fluid, membrane: x y z id
+//                          (OutputCoor, src/Particle.cu:712-790)
+//   FluidField/<step>.plt  walls and fluid: x y z Den Press Vx Vy Vz
+//                          (OutputField, src/Particle.cu:887-928)
+//   CellCoor/<step>.plt    per cell an FE triangle zone: vertices x y z, then
+//                          triangles as zone-local vertex numbers
+//                          (OutPutCellCoor, src/Particle.cu:930-1005)
+//   CellForce/<step>.plt   the same zones with DefForce and AggForce per
+//                          vertex (OutPutCellForce, src/Particle.cu:1007-1081)
+//   CellForce/TF_Cell<i>.plt  time, mean DefForce, mean AggForce of cell i
+//                          (src/Particle.cu:1083-1133)
+//   CellGeo/Geo_Cell<i>.plt   time, |mean velocity|, area, volume of cell i
+//                          (OutPutCellGeo, src/Particle.cu:1139-1220)
+//   CellNorDir/<step>.plt  per cell: triangle centre, normal, index
+//                          (OutPutTriNorDir, src/Particle.cu:1222-1275)
+//
+// with the reference's layout: left-aligned fields, 20 characters wide (15
+// in the two time series), floating point in scientific notation with five
+// digits after the point.  The reference finds each cell's vertices by
+// scanning all particles for every cell (O(cells x particles)) and sums the
+// per-cell means on the host; here particles are written in original id
+// order, each cell's vertices in membrane order (its zone-local numbering
+// follows), the per-cell means arrive precomputed (the fused step reduces
+// them on the GPU in FP64), and the text is formatted by several threads.
+#include <errno.h>
+#include <stdio.h>
+#include <string.h>
+#include <sys/stat.h>
+#include <sys/types.h>
+
+#include <algorithm>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "gc_internal.cuh"
+
+namespace {
+
+int mkdirs(const std::string& path) {
+    std::string cur;
+    for (size_t i = 0; i <= path.size(); ++i) {
+        if (i == path.size() || path[i] == '/') {
+            if (!cur.empty() && mkdir(cur.c_str(), 0755) != 0 && errno != EEXIST)
+                return gc_fail(GC_EINVAL, "output: cannot create directory %s", cur.c_str());
+        }
+        if (i < path.size()) cur.push_back(path[i]);
+    }
+    return GC_OK;
+}
+
+inline void put_e(std::string& s, float v, int width) {
+    char b[64];
+    int k = snprintf(b, sizeof b, "%-*.5e", width, (double)v);
+    s.append(b, (size_t)k);
+}
+
+inline void put_d(std::string& s, long long v, int width) {
+    char b[64];
+    int k = snprintf(b, sizeof b, "%-*lld", width, v);
+    s.append(b, (size_t)k);
+}
+
+inline void put_padded(std::string& s, const char* text, int width) {
+    char b[256];
+    int k = snprintf(b, sizeof b, "%-*s", width, text);
+    s.append(b, (size_t)k);
+}
+
+// Formats lines [0, count) with `line(i, out)` on several threads and
+// returns the text in order.
+template <class F>
+std::string format_lines(long long count, int threads, F line) {
+    if (count <= 0) return std::string();
+    int t = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+    if (t < 1) t = 1;
+    if (count < 20000) t = 1;
+    std::vector<std::string> parts(t);
+    auto work = [&](int w) {
+        long long b = count * w / t, e = count * (w + 1) / t;
+        std::string& s = parts[w];
+        s.reserve((size_t)(e - b) * 96);
+        for (long long i = b; i < e; ++i) line(i, s);
+    };
+    std::vector<std::thread> pool;
+    for (int w = 1; w < t; ++w) pool.emplace_back(work, w);
+    work(0);
+    for (auto& th : pool) th.join();
+    size_t total = 0;
+    for (auto& p : parts) total += p.size();
+    std::string out;
+    out.reserve(total);
+    for (auto& p : parts) out += p;
+    return out;
+}
+
+struct File {
+    FILE* fp = nullptr;
+    bool ok = true;
+    File(const std::string& path, const char* mode) { fp = fopen(path.c_str(), mode); ok = fp != nullptr; }
+    ~File() { if (fp) fclose(fp); }
+    void put(const std::string& s) {
+        if (ok && !s.empty() && fwrite(s.data(), 1, s.size(), fp) != s.size()) ok = false;
+    }
+    bool close() {
+        if (!fp) return false;
+        bool r = fclose(fp) == 0 && ok;
+        fp = nullptr;
+        return r;
+    }
+};
+
+int fail_write(const std::string& path) { return gc_fail(GC_EINVAL, "output: cannot write %s", path.c_str()); }
+
+std::string step_file(const std::string& dir, const char* sub, long long step) {
+    return dir + "/" + sub + "/" + std::to_string(step) + ".plt";
+}
+
+int write_coor(const GcOutputFrame& fr, const std::string& dir, long long step, int threads) {
+    std::string path = step_file(dir, "FluidCoor", step);
+    File f(path, "w");
+    if (!f.ok) return fail_write(path);
+    f.put("Title=\"Particle Coordinate\"\n");
+    f.put("Variables=\"x\",\"y\",\"z\",\"SP\"\n");
+    const long long b12 = fr.n_b1 + fr.n_b2;
+    const long long lo[4] = {0, fr.n_b1, b12, fr.n_cell_start};
+    const long long hi[4] = {fr.n_b1, b12, fr.n_cell_start, fr.n};
+    for (int z = 0; z < 4; ++z) {
+        if (hi[z] <= lo[z]) continue;
+        std::string zone;
+        put_padded(zone, "Zone", 20);
+        zone += '\n';
+        f.put(zone);
+        const long long base = lo[z];
+        f.put(format_lines(hi[z] - lo[z], threads, [&](long long k, std::string& s) {
+            long long i = base + k;
+            put_e(s, fr.pos[3 * i], 20);
+            put_e(s, fr.pos[3 * i + 1], 20);
+            put_e(s, fr.pos[3 * i + 2], 20);
+            put_d(s, i, 20);
+            s += '\n';
+        }));
+    }
+    return f.close() ? GC_OK : fail_write(path);
+}
+
+int write_field(const GcOutputFrame& fr, const std::string& dir, long long step, int threads) {
+    std::string path = step_file(dir, "FluidField", step);
+    File f(path, "w");
+    if (!f.ok) return fail_write(path);
+    f.put("Title=\"Particle Fluid\"\n");
+    f.put("Variables=\"x\",\"y\",\"z\",\"Den\",\"Press\",\"Vx\",\"Vy\",\"Vz\"\n");
+    f.put(format_lines(fr.n_cell_start, threads, [&](long long i, std::string& s) {
+        put_e(s, fr.pos[3 * i], 20);
+        put_e(s, fr.pos[3 * i + 1], 20);
+        put_e(s, fr.pos[3 * i + 2], 20);
+        put_e(s, fr.rho[i], 20);
+        put_e(s, fr.press[i], 20);
+        put_e(s, fr.vel[3 * i], 20);
+        put_e(s, fr.vel[3 * i + 1], 20);
+        put_e(s, fr.vel[3 * i + 2], 20);
+        s += '\n';
+    }));
+    return f.close() ? GC_OK : fail_write(path);
+}
+
+// CellCoor (forces = false) or CellForce (forces = true).
+int write_cells(const GcOutputFrame& fr, const std::string& dir, long long step, int threads, bool forces) {
+    std::string path = step_file(dir, forces ? "CellForce" : "CellCoor", step);
+    File f(path, "w");
+    if (!f.ok) return fail_write(path);
+    f.put(forces ? "Title=\"Particle Force\"\n" : "Title=\"Particle Coordinate\"\n");
+    f.put(forces ? "Variables=\"x\",\"y\",\"z\", \"DFx\",\"DFy\",\"DFz\",\"AFx\",\"AFy\",\"AFz\"\n"
+                 : "Variables=\"x\",\"y\",\"z\"\n");
+    for (int c = 0; c < fr.ncell; ++c) {
+        const int v0 = fr.cell_verts[2 * c], v1 = fr.cell_verts[2 * c + 1] + 1;
+        const int t0 = fr.betri[2 * c], t1 = fr.betri[2 * c + 1];
+        char head[160];
+        snprintf(head, sizeof head, "Zone N=%d, E=%d, F=FEPOINT, ET=TRIANGLE\n", v1 - v0, t1 - t0 + 1);
+        f.put(head);
+        f.put(format_lines(v1 - v0, threads, [&](long long k, std::string& s) {
+            long long m = v0 + k, i = fr.n_cell_start + m;
+            put_e(s, fr.pos[3 * i], 20);
+            put_e(s, fr.pos[3 * i + 1], 20);
+            put_e(s, fr.pos[3 * i + 2], 20);
+            if (forces) {
+                for (int a = 0; a < 3; ++a) put_e(s, fr.defforce[3 * m + a], 20);
+                for (int a = 0; a < 3; ++a) put_e(s, fr.aggforce[3 * m + a], 20);
+            }
+            s += '\n';
+        }));
+        f.put(format_lines(t1 - t0 + 1, threads, [&](long long k, std::string& s) {
+            long long t = t0 + k;
+            for (int a = 0; a < 3; ++a) put_d(s, (long long)fr.tri[3 * t + a] - 1 - v0 + 1, 20);
+            s += '\n';
+        }));
+    }
+    return f.close() ? GC_OK : fail_write(path);
+}
+
+int write_nordir(const GcOutputFrame& fr, const std::string& dir, long long step, int threads) {
+    std::string path = step_file(dir, "CellNorDir", step);
+    File f(path, "w");
+    if (!f.ok) return fail_write(path);
+    f.put("Title=\"Triangle information\"\n");
+    f.put("Variables=\"Cenx\",\"Ceny\",\"Cenz\",\"Norx\",\"Nory\",\"Norz\",\"ID\"\n");
+    for (int c = 0; c < fr.ncell; ++c) {
+        const int t0 = fr.betri[2 * c], t1 = fr.betri[2 * c + 1];
+        std::string zone;
+        put_padded(zone, "Zone", 20);
+        zone += '\n';
+        f.put(zone);
+        f.put(format_lines(t1 - t0 + 1, threads, [&](long long k, std::string& s) {
+            long long t = t0 + k;
+            for (int a = 0; a < 3; ++a) put_e(s, fr.tricenter[3 * t + a], 20);
+            for (int a = 0; a < 3; ++a) put_e(s, fr.trinordir[3 * t + a], 20);
+            put_d(s, t, 20);
+            s += '\n';
+        }));
+    }
+    return f.close() ? GC_OK : fail_write(path);
+}
+
+// One line per cell appended to TF_Cell<i>.plt and Geo_Cell<i>.plt.
+int write_series(const GcOutputFrame& fr, const std::string& dir, double time, int first) {
+    for (int c = 0; c < fr.ncell; ++c) {
+        const double* st = fr.cell_stats + 12 * (size_t)c;
+        std::string tf, geo;
+        put_e(tf, (float)time, 15);
+        for (int a = 0; a < 6; ++a) put_e(tf, (float)st[a], 15);
+        tf += '\n';
+        put_e(geo, (float)time, 15);
+        put_e(geo, (float)st[9], 15);
+        put_e(geo, (float)st[10], 15);
+        put_e(geo, (float)st[11], 15);
+        geo += '\n';
+        std::string p1 = dir + "/CellForce/TF_Cell" + std::to_string(c) + ".plt";
+        std::string p2 = dir + "/CellGeo/Geo_Cell" + std::to_string(c) + ".plt";
+        File a(p1, first ? "w" : "a");
+        a.put(tf);
+        if (!a.close()) return fail_write(p1);
+        File b(p2, first ? "w" : "a");
+        b.put(geo);
+        if (!b.close()) return fail_write(p2);
+    }
+    return GC_OK;
+}
+
+}  // namespace
+
+extern "C" int gc_output_write(const GcOutputFrame* fr, const char* dir, long long step_data, double time,
+                               int first) {
+    if (!fr || !dir) return gc_fail(GC_EINVAL, "output_write: NULL argument");
+    if (fr->n < 0 || fr->n_b1 < 0 || fr->n_b2 < 0 || fr->n_b1 + fr->n_b2 > fr->n_cell_start ||
+        fr->n_cell_start > fr->n)
+        return gc_fail(GC_EINVAL, "output_write: inconsistent particle counts");
+    if (fr->n > 0 && (!fr->pos || !fr->vel || !fr->rho || !fr->press))
+        return gc_fail(GC_EINVAL, "output_write: NULL particle array");
+    const long long ncp = fr->n - fr->n_cell_start;
+    if (fr->ncell > 0) {
+        if (!fr->cell_verts || !fr->tri || !fr->betri || !fr->defforce || !fr->aggforce || !fr->tricenter ||
+            !fr->trinordir || !fr->cell_stats)
+            return gc_fail(GC_EINVAL, "output_write: NULL membrane array");
+        for (int c = 0; c < fr->ncell; ++c) {
+            int v0 = fr->cell_verts[2 * c], v1 = fr->cell_verts[2 * c + 1] + 1;
+            int t0 = fr->betri[2 * c], t1 = fr->betri[2 * c + 1];
+            if (v0 < 0 || v1 < v0 || v1 > ncp || t0 < 0 || t1 < t0 || t1 >= fr->ntri)
+                return gc_fail(GC_EINVAL, "output_write: bad vertex or triangle range of cell %d", c);
+            for (int t = t0; t <= t1; ++t)
+                for (int a = 0; a < 3; ++a) {
+                    int v = fr->tri[3 * (size_t)t + a] - 1;
+                    if (v < v0 || v >= v1)
+                        return gc_fail(GC_EINVAL, "output_write: triangle %d of cell %d has a vertex of another cell",
+                                       t, c);
+                }
+        }
+    }
+    std::string d(dir);
+    for (const char* sub : {"FluidCoor", "FluidField", "CellCoor", "CellForce", "CellGeo", "CellNorDir"})
+        GC_TRY(mkdirs(d + "/" + sub));
+    const int th = fr->threads;
+    GC_TRY(write_coor(*fr, d, step_data, th));
+    GC_TRY(write_field(*fr, d, step_data, th));
+    if (fr->ncell > 0) {
+        GC_TRY(write_cells(*fr, d, step_data, th, false));
+        GC_TRY(write_cells(*fr, d, step_data, th, true));
+        GC_TRY(write_series(*fr, d, time, first));
+        GC_TRY(write_nordir(*fr, d, step_data, th));
+    }
+    return GC_OK;
+}

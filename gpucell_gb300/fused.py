@@ -103,6 +103,20 @@ class _Handle:
         return dict(skin=round(float(o.skin), 6), block=o.block, compact=bool(o.compact), graph=bool(o.graph),
                     ms_per_step=ms.value)
 
+    def write_output(self, directory, step_data, time, first=False, sys=0, threads=0):
+        """GPUCell's output files for one output step (see gpucell_gb300.output)."""
+        _lib.call("gc_ensemble_write_output", self.h, int(sys), str(directory).encode(), int(step_data), float(time),
+                  1 if first else 0, int(threads))
+
+    def cell_stats(self, sys=0) -> np.ndarray:
+        """Per-cell mean DefForce, mean AggForce, mean velocity (x, y, z each),
+        |mean velocity|, area, volume: ncell x 12, reduced on the GPU in FP64."""
+        cfg = self.cfgs[sys] if hasattr(self, "cfgs") else self.cfg
+        out = np.zeros((max(cfg.ncell, 0), 12))
+        if cfg.ncell:
+            _lib.call("gc_ensemble_cell_stats", self.h, int(sys), _ptr(out))
+        return out
+
     def checkpoint(self, path):
         _lib.call("gc_fused_checkpoint", self.h, str(path).encode())
 

@@ -283,6 +283,45 @@ int gc_ensemble_store_cells(GcFused* f, int sys, float* area, float* vol, float*
                             float* trinordir, float* tricenter, float* pararea, int to_device);
 int gc_ensemble_cell_sums(GcFused* f, int sys, double* area, double* vol);
 
+/* ---- output files (GPUCell's OutputPar, src/Particle.cu:681-1300) --------
+ *
+ * One output step in the reference's text formats: FluidCoor/<step>.plt,
+ * FluidField/<step>.plt, CellCoor/<step>.plt, CellForce/<step>.plt,
+ * CellNorDir/<step>.plt under `dir`, and one line per cell appended to
+ * CellForce/TF_Cell<i>.plt and CellGeo/Geo_Cell<i>.plt (truncated first
+ * when `first` is set, as the reference does at StepCount 0).  Particles are
+ * written in original id order and each cell's vertices in membrane order
+ * (the zone-local numbering of the triangles follows). */
+typedef struct {
+    long long n;              /* particles */
+    long long n_b1, n_b2;     /* Bound1 ids [0, n_b1), Bound2 ids [n_b1, n_b1 + n_b2) */
+    long long n_cell_start;   /* fluid ids up to here, membrane vertices from here to n */
+    const float* pos;         /* n x 3, original order */
+    const float* vel;         /* n x 3 */
+    const float* rho;         /* n */
+    const float* press;       /* n */
+    int ncell, ntri;
+    const int* cell_verts;    /* ncell x 2: first and last membrane vertex of each cell (0-based, inclusive) */
+    const int* tri;           /* ntri x 3: 1-based membrane vertex indices */
+    const int* betri;         /* ncell x 2: first and last triangle of each cell */
+    const float* defforce;    /* ncp x 3 */
+    const float* aggforce;    /* ncp x 3 */
+    const float* tricenter;   /* ntri x 3 */
+    const float* trinordir;   /* ntri x 3 */
+    const double* cell_stats; /* ncell x 12: mean DefForce, mean AggForce, mean velocity (x, y, z each),
+                                 |mean velocity|, area, volume */
+    int threads;              /* formatting threads (0: all cores) */
+    int reserved;
+} GcOutputFrame;
+int gc_output_write(const GcOutputFrame* frame, const char* dir, long long step_data, double time, int first);
+/* Per-cell statistics of one system of a fused handle, reduced on the GPU in
+ * FP64: ncell x 12 doubles as GcOutputFrame.cell_stats (host pointer). */
+int gc_ensemble_cell_stats(GcFused* f, int sys, double* out);
+/* Stores one system of a fused handle and writes its output files. */
+int gc_ensemble_write_output(GcFused* f, int sys, const char* dir, long long step_data, double time, int first,
+                             int threads);
+int gc_fused_write_output(GcFused* f, const char* dir, long long step_data, double time, int first, int threads);
+
 /* ---- test hooks (no counterpart in the reference) ----------------------- */
 
 /* Runs the production neighbour traversal of CalFluidDen over the current
