@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--ensemble-only", action="store_true", help="only the ensemble workload")
     ap.add_argument("--ens-systems", type=int, default=64)
     ap.add_argument("--ens-steps", type=int, default=20)
+    ap.add_argument("--no-output", dest="output", action="store_false",
+                    help="skip timing one output step (GPUCell's output files)")
     return ap.parse_args()
 
 
@@ -282,6 +284,21 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
 
+    out_info = None
+    if args.output and rank == 0:
+        import shutil
+        tmp = tempfile.mkdtemp(prefix="gc_output_")
+        try:
+            t0 = time.perf_counter()
+            fs.write_output(os.path.join(tmp, "Result"), 1, 1e-3, first=True)
+            dt = time.perf_counter() - t0
+            size = sum(os.path.getsize(os.path.join(r, f)) for r, _, fl in os.walk(tmp) for f in fl)
+            out_info = {"seconds": dt, "bytes": size, "threads": os.cpu_count(),
+                        "what": "one output step: store, per-cell GPU reductions, FluidCoor, FluidField, CellCoor, "
+                                "CellForce, CellNorDir, TF_Cell/Geo_Cell lines (gc_fused_write_output)"}
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+
     n_all = n * world
     value = n_all * K / (t_ms / 1e3)
     e2e_value = n_all * KE / e2e_s
@@ -341,6 +358,7 @@ def run_ours(args):
                     "the pair physics is FP32-issue bound",
         },
         "kernels_ms_per_step": {"fk_force": force_ms, "fk_density": dens_ms},
+        "output_step": out_info,
         "lists": {"rebuilds_in_timed_steps": st1["rebuilds"] - st0["rebuilds"], "mean_length": mean_nb,
                   "max_length": st1["max_neighbors"], "capacity": st1["capacity"]},
         "device_flags": flags,

@@ -20,8 +20,11 @@ from gpucell_gb300.output import read_plt
 pytestmark = pytest.mark.gpu
 
 
+PHYS = gen.Physics(sur_energy=5.0, max_cut=1.2, zero_len=0.3, sca_fac=4.0)
+
+
 def _cfg():
-    phys = gen.Physics(sur_energy=5.0, max_cut=1.2, zero_len=0.3, sca_fac=4.0)
+    phys = PHYS
     return gen.channel(nx=24, ny=12, nz=18, wall_layers=3, b1_layers=1, cell_subdiv=2, cell_diameter=3.0,
                        phys=phys, cell_centers=[(0.0, -0.55, 0.0), (0.0, 0.55, 0.0)], seed=11)
 
@@ -85,7 +88,7 @@ def test_cell_stats_and_files(cuda_device, tmp_path):
 
 def test_ensemble_system_writes_its_own_files(cuda_device, tmp_path):
     from gpucell_gb300.fused import Ensemble
-    a = gen.suspension(nx=16, ny=16, nz=16, ncells=0, seed=5)
+    a = gen.suspension(nx=16, ny=16, nz=16, ncells=0, seed=5, phys=PHYS)
     b = _cfg()
     ens = Ensemble([a, b], noise=False)
     ens.step(3, 1)
