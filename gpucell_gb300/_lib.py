@@ -72,6 +72,22 @@ assert C.sizeof(GcSystemDesc) == 128
 GC_TUNE_CACHE = 1
 
 
+class GcInputSet(C.Structure):
+    """ctypes mirror of GcInputSet (include/gpucell_gb300.h)."""
+
+    _FP = C.POINTER(C.c_float)
+    _IP = C.POINTER(C.c_int)
+    _fields_ = [("n_b1", C.c_longlong), ("n_b2", C.c_longlong), ("n_fluid", C.c_longlong), ("sdpd_coor", _FP),
+                ("sound1", C.c_float), ("sound2", C.c_float), ("shear_vis", C.c_float), ("bulk_vis", C.c_float),
+                ("den_init", C.c_float), ("ext_force", C.c_float), ("ncell", C.c_int), ("ntype", C.c_int),
+                ("ncp", C.c_longlong), ("ntri", C.c_longlong), ("nedge", C.c_longlong), ("cell_type", _IP),
+                ("npar", _IP), ("ntri_cell", _IP), ("cell_coor", _FP), ("tri", _IP), ("edge", _IP),
+                ("betri", _IP), ("celltab", _IP), ("shear_mod", _FP), ("bending_mod", _FP), ("hgarea", _FP),
+                ("hlarea", _FP), ("hvol", _FP), ("max_cut", C.c_float), ("zero_len", C.c_float),
+                ("sca_fac", C.c_float), ("sur_energy", C.c_float), ("shear_e", _FP), ("bend_e", _FP),
+                ("hl_t", _FP), ("hg_t", _FP), ("hv_t", _FP)]
+
+
 class GcOutputFrame(C.Structure):
     """ctypes mirror of GcOutputFrame (include/gpucell_gb300.h)."""
 
@@ -154,6 +170,10 @@ _SIGS = {
     "gc_ensemble_write_output": [_P, _I, C.c_char_p, C.c_longlong, C.c_double, _I, _I],
     "gc_fused_write_output": [_P, C.c_char_p, C.c_longlong, C.c_double, _I, _I],
     "gc_output_write": [_P, C.c_char_p, C.c_longlong, C.c_double, _I],
+    "gc_input_read": [C.c_char_p, _P],
+    "gc_input_write_binary": [C.c_char_p, _P],
+    "gc_input_read_binary": [C.c_char_p, _P],
+    "gc_input_free": [_P],
 }
 _RESTYPES = {"gc_last_error": C.c_char_p, "gc_get_step": C.c_longlong, "gc_launch_count": C.c_ulonglong}
 

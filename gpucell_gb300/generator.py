@@ -80,6 +80,7 @@ class Config:
     celltab: Optional[np.ndarray] = None   # (ncp,) int32
     cell_type: Optional[np.ndarray] = None # (ncell,) 1-based
     meta: dict = dataclasses.field(default_factory=dict)   # how the configuration was drawn
+    moduli: Optional[tuple] = None         # per-edge shear, bending; per-triangle hl, hg, hv (else from phys)
 
     @property
     def n(self) -> int:
@@ -131,6 +132,8 @@ class Config:
 
     def edge_params(self):
         """Per-edge shear and bending moduli, per-triangle area/volume constants."""
+        if self.moduli is not None:
+            return tuple(np.ascontiguousarray(a, np.float32) for a in self.moduli)
         p = self.phys
         return (np.full(self.nedge, p.shear_mod, np.float32), np.full(self.nedge, p.bending_mod, np.float32),
                 np.full(self.ntri, p.hlarea, np.float32), np.full(self.ntri, p.hgarea, np.float32),

@@ -322,6 +322,41 @@ int gc_ensemble_write_output(GcFused* f, int sys, const char* dir, long long ste
                              int threads);
 int gc_fused_write_output(GcFused* f, const char* dir, long long step_data, double time, int first, int threads);
 
+/* ---- input files (GPUCell's loaders, src/Particle.cu:45-380) -------------
+ *
+ * The four input files (SDPDParCoor.txt, SDPDPhyPara.txt, CELLParStruct.txt,
+ * CELLPhyPara.txt) parsed with the reference's rules -- 20-character
+ * columns, atof conversion, one header line before every block, the
+ * per-cell vertex and triangle offsets added to the topology, the per-type
+ * moduli spread over edges and triangles -- but without its fixed array
+ * sizes (2,000,000 wall + fluid particles, 4,000,000 membrane vertices,
+ * src/Particle.cu:31-32, 200-202).  The set owns its arrays (malloc);
+ * gc_input_free releases them.  The binary form holds the same set for fast
+ * reloading. */
+typedef struct {
+    long long n_b1, n_b2, n_fluid;   /* SDPDParCoor.txt */
+    float* sdpd_coor;                /* (n_b1 + n_b2 + n_fluid) x 3: Bound1, Bound2, fluid */
+    float sound1, sound2, shear_vis, bulk_vis, den_init, ext_force;   /* SDPDPhyPara.txt (force per mass) */
+    int ncell, ntype;                /* CELLParStruct.txt, CELLPhyPara.txt */
+    long long ncp, ntri, nedge;
+    int* cell_type;                  /* ncell: 1-based type */
+    int* npar;                       /* ncell: vertices per cell */
+    int* ntri_cell;                  /* ncell: triangles per cell */
+    float* cell_coor;                /* ncp x 3 */
+    int* tri;                        /* ntri x 3: 1-based membrane vertex indices */
+    int* edge;                       /* nedge x 6: p1..p4 1-based vertices, t1 t2 1-based triangles */
+    int* betri;                      /* ncell x 2: first and last triangle of each cell */
+    int* celltab;                    /* ncp: 0-based cell of each vertex */
+    float *shear_mod, *bending_mod, *hgarea, *hlarea, *hvol;   /* ntype each */
+    float max_cut, zero_len, sca_fac, sur_energy;
+    float *shear_e, *bend_e;         /* nedge: moduli of each edge's cell type */
+    float *hl_t, *hg_t, *hv_t;       /* ntri */
+} GcInputSet;
+int gc_input_read(const char* dir, GcInputSet* out);
+int gc_input_write_binary(const char* path, const GcInputSet* set);
+int gc_input_read_binary(const char* path, GcInputSet* out);
+int gc_input_free(GcInputSet* set);
+
 /* ---- test hooks (no counterpart in the reference) ----------------------- */
 
 /* Runs the production neighbour traversal of CalFluidDen over the current
