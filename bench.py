@@ -145,6 +145,10 @@ def plain_bytes_per_step(cfg):
 # (1/d, P/d^2) (8 B) read, force and velocity (16 B each) written, the list
 # length (4 B) and its neighbour-list entries (4 B each) read.
 FORCE_STATE_BYTES = 16 * 3 + 8 + 16 * 2 + 4
+# DRAM bytes (read + write) of one fk_force launch on the 4.2M-particle
+# suspension, from ncu at full size (profiles/fused_step_rbc_suspension_4M_launches.md):
+# 2.845e9 read + 0.128e9 written, with 143.6 list entries per particle.
+FORCE_TRAFFIC_4M = 2.845227264e9 + 0.127872512e9
 
 
 def measure_plain(cfg, dev, steps, warmup):
@@ -351,7 +355,8 @@ def run_ours(args):
             "unit": "GB/s",
             "frac": achieved / hbm,
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": None,
+            "traffic": FORCE_TRAFFIC_4M if (not args.small and n == 4194304) else None,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one fk_force launch, full size",
             "bytes_per_launch": force_bytes,
             "launch_ms": force_ms,
             "note": f"bytes = {FORCE_STATE_BYTES} per particle + 4 per list entry (mean list {mean_nb:.1f}); "
