@@ -1260,6 +1260,14 @@ struct GcFused {
     size_t sortmem_bytes = 0;
     int sort_n = 0, sort_K = 0;
     GcSortBufs sb{};
+    void* sortmem_agg = nullptr;   // the aggregation sort's own temporaries: it runs beside the list rebuild
+    int sort_agg_n = 0, sort_agg_K = 0;
+    GcSortBufs sb_agg{};
+    // The membrane kernels depend only on the integrated membrane positions:
+    // they run on their own stream from the end of the integration to the
+    // force pass, beside the rebuild check, the list rebuild and the density.
+    cudaStream_t mst = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // membranes (global indices over the ensemble)
     int ncell = 0, ntri = 0, nedge = 0, ncp = 0;
     int3* tri = nullptr;
@@ -1284,7 +1292,7 @@ struct GcFused {
     bool have_agg = false;
     bool setup_done = false;
     // captured steps
-    cudaStream_t gst = nullptr, gst2 = nullptr;
+    cudaStream_t gst = nullptr, gst2 = nullptr, gst3 = nullptr;
     cudaGraph_t cg[2] = {};
     cudaGraphExec_t gexec[2] = {};
     bool graph_dirty = true;
@@ -1378,6 +1386,19 @@ int ensure_sort_bufs(GcFused* f) {
     return GC_OK;
 }
 
+int ensure_agg_sort_bufs(GcFused* f) {
+    if (!f->have_agg || f->ncp <= 0) return GC_OK;
+    if (f->sortmem_agg && f->ncp <= f->sort_agg_n && f->Kagg <= f->sort_agg_K) return GC_OK;
+    if (f->sortmem_agg) cudaFree(f->sortmem_agg);
+    f->sortmem_agg = nullptr;
+    GC_CUDA(cudaMalloc(&f->sortmem_agg, gc_sort_bufs_bytes(f->ncp, f->Kagg)), "fused: aggregation sort");
+    f->sort_agg_n = f->ncp;
+    f->sort_agg_K = f->Kagg;
+    gc_sort_bufs_carve(f->sortmem_agg, f->ncp, f->Kagg, &f->sb_agg);
+    drop_graphs(f);
+    return GC_OK;
+}
+
 // Per-system list grids (cubes at least rc + skin wide) and aggregation
 // grids, their global cube offsets, and the device copy of the table.
 int build_grids(GcFused* f) {
@@ -1404,6 +1425,7 @@ int build_grids(GcFused* f) {
         GC_CUDA(cudaMemcpyAsync(f->dsys, f->hsys.data(), sizeof(SysInfo) * f->nsys, cudaMemcpyHostToDevice, f->st),
                 "fused: system table");
     GC_TRY(ensure_sort_bufs(f));
+    GC_TRY(ensure_agg_sort_bufs(f));
     drop_graphs(f);
     return GC_OK;
 }
@@ -1521,8 +1543,8 @@ int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p) {
         fk_mkey<<<gc_blocks(f->ncp, f->block), f->block, 0, st>>>(f->ncp, f->dsys, f->msys, f->mpos, f->mkeys,
                                                                   f->mvals);
         GC_CHECK_LAUNCH("fused: aggregation keys");
-        GC_TRY(gc_counting_sort_bufs(f->ncp, f->Kagg, f->mkeys, f->mvals, f->sb, f->flags, st));
-        fk_magg<<<gc_blocks(f->ncp, f->block), f->block, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mvals, f->sb.cnt,
+        GC_TRY(gc_counting_sort_bufs(f->ncp, f->Kagg, f->mkeys, f->mvals, f->sb_agg, f->flags, st));
+        fk_magg<<<gc_blocks(f->ncp, f->block), f->block, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mvals, f->sb_agg.cnt,
                                                                   f->mpos, f->celltab, f->parea, f->magg, f->mforce);
         GC_CHECK_LAUNCH("fused: aggregation");
     }
@@ -1577,6 +1599,23 @@ int launch_step_begin(GcFused* f, cudaStream_t st) {
     return GC_OK;
 }
 
+// The membrane kernels of a step on stream `ms`, after the integration that
+// `st` has queued; join_membranes makes `st` wait for them.
+int fork_membranes(GcFused* f, cudaStream_t st, cudaStream_t ms, const GcParams& p) {
+    if (f->ncell <= 0) return GC_OK;
+    GC_CUDA(cudaEventRecord(f->ev_fork, st), "fused: fork");
+    GC_CUDA(cudaStreamWaitEvent(ms, f->ev_fork, 0), "fused: fork");
+    GC_TRY(launch_membranes(f, ms, p));
+    GC_CUDA(cudaEventRecord(f->ev_join, ms), "fused: join");
+    return GC_OK;
+}
+
+int join_membranes(GcFused* f, cudaStream_t st) {
+    if (f->ncell <= 0) return GC_OK;
+    GC_CUDA(cudaStreamWaitEvent(st, f->ev_join, 0), "fused: join");
+    return GC_OK;
+}
+
 // One step on the host-driven path: the host reads the rebuild flag.
 int one_step(GcFused* f, int drive) {
     cudaStream_t st = f->st;
@@ -1586,13 +1625,14 @@ int one_step(GcFused* f, int drive) {
     if (f->ens) GC_TRY(launch_step_begin(f, st));
     else GC_CUDA(cudaMemsetAsync(f->rebuild, 0, sizeof(int), st), "fused: flag");
     GC_TRY(launch_integrate(f, st, p));
+    GC_TRY(fork_membranes(f, st, f->mst, p));
     GC_CUDA(cudaMemcpyAsync(&f->h->rebuild, f->rebuild, sizeof(int), cudaMemcpyDeviceToHost, st), "fused: flag");
     GC_CUDA(cudaStreamSynchronize(st), "fused: flag");
     if (f->h->rebuild) GC_TRY(rebuild_lists(f));
     prof_mark(f, st);
     GC_TRY(launch_density(f, st, p, true));
     prof_mark(f, st);
-    GC_TRY(launch_membranes(f, st, p));
+    GC_TRY(join_membranes(f, st));
     prof_mark(f, st);
     GC_TRY(launch_force(f, st, p, drive));
     prof_mark(f, st);
@@ -1626,6 +1666,7 @@ int launch_rebuild_body(GcFused* f, cudaStream_t st) {
 int capture_step(GcFused* f, int drive) {
     if (!f->gst) GC_CUDA(cudaStreamCreateWithFlags(&f->gst, cudaStreamNonBlocking), "fused: capture stream");
     if (!f->gst2) GC_CUDA(cudaStreamCreateWithFlags(&f->gst2, cudaStreamNonBlocking), "fused: capture stream");
+    if (!f->gst3) GC_CUDA(cudaStreamCreateWithFlags(&f->gst3, cudaStreamNonBlocking), "fused: capture stream");
     cudaStream_t st = f->gst;
     GcParams p = f->p;
     unsigned long long l0 = gc_launch_count();
@@ -1644,6 +1685,7 @@ int capture_step(GcFused* f, int drive) {
         if (e != cudaSuccess) { rc = gc_cuda_fail(e, "fused: conditional handle"); break; }
         if ((rc = launch_step_begin(f, st)) != GC_OK) break;
         if ((rc = launch_integrate(f, st, p)) != GC_OK) break;
+        if ((rc = fork_membranes(f, st, f->gst3, p)) != GC_OK) break;
         fk_set_cond<<<1, 1, 0, st>>>(hcond, f->rebuild, f->drebuilds);
         gc_count_launch();
         if ((e = cudaGetLastError()) != cudaSuccess) { rc = gc_cuda_fail(e, "fused: set condition"); break; }
@@ -1670,7 +1712,7 @@ int capture_step(GcFused* f, int drive) {
         if (e != cudaSuccess) { rc = gc_cuda_fail(e, "fused: end rebuild capture"); break; }
         body_kernels = (long long)(gc_launch_count() - lb);
         if ((rc = launch_density(f, st, p, true)) != GC_OK) break;
-        if ((rc = launch_membranes(f, st, p)) != GC_OK) break;
+        if ((rc = join_membranes(f, st)) != GC_OK) break;
         if ((rc = launch_force(f, st, p, drive)) != GC_OK) break;
         if ((rc = launch_wallvel(f, st, p)) != GC_OK) break;
     } while (0);
@@ -2081,6 +2123,10 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
     if (ok == GC_OK && f->ncp > 0) ok = falloc(f, &f->mnthro, f->ncp);
     if (ok == GC_OK && cudaMallocHost(&f->h, sizeof(GcFused::Pinned)) != cudaSuccess)
         ok = gc_fail(GC_ENOMEM, "fused: pinned words");
+    if (ok == GC_OK && (cudaStreamCreateWithFlags(&f->mst, cudaStreamNonBlocking) != cudaSuccess ||
+                        cudaEventCreateWithFlags(&f->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+                        cudaEventCreateWithFlags(&f->ev_join, cudaEventDisableTiming) != cudaSuccess))
+        ok = gc_fail(GC_ECUDA, "fused: membrane stream");
     if (ok == GC_OK) ok = build_grids(f);
     if (ok == GC_OK) {
         // list capacity: expected neighbours within rc + skin at the largest
@@ -2587,8 +2633,14 @@ int gc_fused_destroy(GcFused* f) {
         if (f->gexec[d]) cudaGraphExecDestroy(f->gexec[d]);
         if (f->cg[d]) cudaGraphDestroy(f->cg[d]);
     }
+    if (f->mst) cudaStreamSynchronize(f->mst);
     if (f->gst) cudaStreamDestroy(f->gst);
     if (f->gst2) cudaStreamDestroy(f->gst2);
+    if (f->gst3) cudaStreamDestroy(f->gst3);
+    if (f->mst) cudaStreamDestroy(f->mst);
+    if (f->ev_fork) cudaEventDestroy(f->ev_fork);
+    if (f->ev_join) cudaEventDestroy(f->ev_join);
+    if (f->sortmem_agg) cudaFree(f->sortmem_agg);
     for (cudaEvent_t e : f->ev) cudaEventDestroy(e);
     for (void* q : f->allocs) cudaFree(q);
     if (f->nbr) cudaFree(f->nbr);
