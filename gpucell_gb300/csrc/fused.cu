@@ -70,7 +70,8 @@ struct SysInfo {
     int mcube0;                      // first global cube of the aggregation grid
     float gx;                        // body force in x (ConstExtForce)
     float invL[3];
-    GcGrid g;                        // list grid: the box, cubes at least rc + skin wide
+    int lr;                          // list-grid stencil radius: 2 for cells >= (rc + skin)/2, 1 for cubes >= rc + skin
+    GcGrid g;                        // list grid over the box
     GcGrid mg;                       // aggregation grid: cubes at least MaxCut wide
 };
 
@@ -312,13 +313,15 @@ __device__ __forceinline__ void scan_range(const float4* __restrict__ pos, unsig
     }
 }
 
-// One thread per slot scans the cubes of its system's list grid around its
-// own.  Fluid and membrane slots list every particle within rc + skin;
-// Bound2 slots list the moving particles (for their wall velocity); Bound1
-// slots list nothing.  Positions are inside the box on periodic axes (the
-// permutation wraps them), so each neighbouring row of cubes has one image
-// shift, and the three cubes of a row that do not wrap are one contiguous
-// range of slots.
+// One thread per slot scans the cells of its system's list grid within the
+// stencil radius R around its own (R = 2 for cells at least (rc + skin)/2
+// wide, R = 1 for cubes at least rc + skin wide; either way every pair
+// within rc + skin is found).  Fluid and membrane slots list every particle
+// within rc + skin; Bound2 slots list the moving particles (for their wall
+// velocity); Bound1 slots list nothing.  Positions are inside the box on
+// periodic axes (the permutation wraps them), so each neighbouring row of
+// cells has one image shift, and the 2R + 1 cells of a row that do not wrap
+// are one contiguous range of slots.
 __global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, const SysInfo* __restrict__ sys,
                                                      const int* __restrict__ sysid, const float4* __restrict__ pos,
                                                      const unsigned* __restrict__ start, int* __restrict__ nbr,
@@ -336,23 +339,24 @@ __global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, const SysInfo* __
     int* lst = nbr + sell(i, 0, cap);
     const bool mobile_only = t == PT_B2;
     if (t != PT_B1) {
+        const int R = S.lr;
         int cx = cube_coord(xi.x, 0, g), cy = cube_coord(xi.y, 1, g), cz = cube_coord(xi.z, 2, g);
-        for (int dz = -1; dz <= 1; ++dz) {
+        for (int dz = -R; dz <= R; ++dz) {
             int z = cz + dz;
             float sz = 0.f;
             if (z < 0) { if (!(g.pmask & 4)) continue; z += g.n[2]; sz = g.L[2]; }
             else if (z >= g.n[2]) { if (!(g.pmask & 4)) continue; z -= g.n[2]; sz = -g.L[2]; }
-            for (int dy = -1; dy <= 1; ++dy) {
+            for (int dy = -R; dy <= R; ++dy) {
                 int y = cy + dy;
                 float sy = 0.f;
                 if (y < 0) { if (!(g.pmask & 2)) continue; y += g.n[1]; sy = g.L[1]; }
                 else if (y >= g.n[1]) { if (!(g.pmask & 2)) continue; y -= g.n[1]; sy = -g.L[1]; }
                 int row = S.cube0 + g.n[0] * (y + g.n[1] * z);
-                if (cx >= 1 && cx + 1 < g.n[0]) {
-                    scan_range(pos, start[row + cx - 1], start[row + cx + 2], f3(xi.x, xi.y + sy, xi.z + sz), i,
+                if (cx >= R && cx + R < g.n[0]) {
+                    scan_range(pos, start[row + cx - R], start[row + cx + R + 1], f3(xi.x, xi.y + sy, xi.z + sz), i,
                                cut2, mobile_only, fl, cap, lst, k);
                 } else {
-                    for (int dx = -1; dx <= 1; ++dx) {
+                    for (int dx = -R; dx <= R; ++dx) {
                         int x = cx + dx;
                         float sx = 0.f;
                         if (x < 0) { if (!(g.pmask & 1)) continue; x += g.n[0]; sx = g.L[0]; }
@@ -1406,7 +1410,16 @@ int build_grids(GcFused* f) {
     for (int s = 0; s < f->nsys; ++s) {
         SysInfo& S = f->hsys[s];
         const GcSystemDesc& d = f->desc[s];
-        GC_TRY(gc_build_grid(d.bbox, d.consts.CutRadius + f->skin, d.periodic_mask, &S.g));
+        // half-width cells (a 5x5x5 stencil scans ~40 % fewer candidates than
+        // 3x3x3 cubes) wherever every periodic axis has at least 5 of them
+        const float cut = d.consts.CutRadius + f->skin;
+        S.lr = 2;
+        if (gc_build_grid(d.bbox, 0.5f * cut, d.periodic_mask, &S.g) != GC_OK ||
+            ((d.periodic_mask & 1) && S.g.n[0] < 5) || ((d.periodic_mask & 2) && S.g.n[1] < 5) ||
+            ((d.periodic_mask & 4) && S.g.n[2] < 5)) {
+            S.lr = 1;
+            GC_TRY(gc_build_grid(d.bbox, cut, d.periodic_mask, &S.g));
+        }
         for (int a = 0; a < 3; ++a) S.invL[a] = 1.f / S.g.L[a];
         S.cube0 = K;
         K += S.g.ncells;
