@@ -210,7 +210,8 @@ __global__ void k_sdpd(int n, GcParams p, const float3* __restrict__ coor, const
         float fdd = F / (di * dj);
         f -= fdd * (p.visA * vij + (p.visB * ev) * e);
         if (noise) {
-            float q = sqrtf(p.noise_pref * fdd);
+            // a pair at the cut-off can give F a rounding-sized negative value: no noise then
+            float q = fdd > 0.f ? sqrtf(p.noise_pref * fdd) : 0.f;
             float3 xi_ = pair_noise(id, idj, p);
             float exi = dot3(e, xi_);
             f += q * (p.sqrtA * xi_ + ((p.sqrtAB - p.sqrtA) * exi) * e);

@@ -501,7 +501,10 @@ int or_sdpd_force(or_state* s) {
                 double xi[3];
                 or_pair_noise(s, (unsigned)i, (unsigned)j, xi);
                 v3 x = mk(xi[0], xi[1], xi[2]);
-                double q = sqrt(pref * fdd);
+                /* The pair passed the FP32 cut-off test (the GPU's predicate) but r is
+                 * evaluated in FP64: at the cut-off, F can be a rounding-sized negative
+                 * number.  Such a pair gets no noise, as on the GPU. */
+                double q = fdd > 0.0 ? sqrt(pref * fdd) : 0.0;
                 f = add(f, scl(q, add(scl(sA, x), scl((sAB - sA) * dot(e, x), e))));
             }
         });

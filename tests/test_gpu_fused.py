@@ -130,3 +130,23 @@ def test_fused_store_load_round_trip(cuda_device):
         assert np.array_equal(a[k], b[k]), k
     fs.step(1, 1)      # continues from the reloaded state
     assert np.isfinite(fs.fetch()["pos"]).all()
+
+
+def test_fused_tracks_oracle_noise_on(cuda_device):
+    """With the thermal noise on: the GPU and the oracle draw the same
+    Philox pair noise (same key schedule, same 21-bit variates), so the
+    trajectories agree to FP32 rounding: positions within 1e-5 and
+    velocities within 1e-4 of their largest magnitude after 4 steps."""
+    from gpucell_gb300.fused import FusedSystem
+    cfg = gen.small_channel()
+    fs = FusedSystem(cfg, noise=True)
+    o = _oracle(cfg, True)
+    for _ in range(4):
+        o.step()
+    fs.step(4, 1)
+    g = fs.fetch()
+    assert np.isfinite(o.vel).all()
+    assert np.abs(o.vel).max() > 0.1     # the noise acts
+    np.testing.assert_allclose(g["pos"], o.pos, atol=1e-5)
+    _close_rel(g["vel"], o.vel, 1e-4)
+    np.testing.assert_allclose(g["Area64"], o.area, rtol=1e-5)

@@ -217,3 +217,20 @@ def test_full_step_is_stable(oracle_lib):
         o.step()
     assert np.all(np.isfinite(o.pos)) and np.all(np.isfinite(o.vel))
     assert abs(o.area[0] / a0[0] - 1) < 0.1 and abs(o.vol[0] / v0[0] - 1) < 0.1
+
+
+def test_noise_on_steps_stay_finite_and_hot():
+    """Regression: a pair that passes the FP32 cut-off test while its FP64
+    distance is a rounding error above rc gets a tiny negative F; its noise
+    amplitude must be zero, not sqrt of a negative number (which turned the
+    whole state into NaN within a few steps)."""
+    import os
+    from oracle.binding import Oracle
+    from gpucell_gb300 import generator as gen
+    cfg = gen.suspension(nx=24, ny=16, nz=16, ncells=0, seed=12345)
+    o = Oracle(cfg, noise=True, nthreads=os.cpu_count() or 1)
+    o.setup()
+    for _ in range(6):
+        o.step()
+        assert np.isfinite(o.pos).all() and np.isfinite(o.vel).all() and np.isfinite(o.force).all()
+    assert (o.vel ** 2).sum(axis=1).mean() > 0.1   # the noise heats the fluid
