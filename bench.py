@@ -149,6 +149,13 @@ FORCE_STATE_BYTES = 16 * 3 + 8 + 16 * 2 + 4
 # suspension, from ncu at full size (profiles/fused_step_rbc_suspension_4M_launches.md):
 # 2.845e9 read + 0.128e9 written, with 143.6 list entries per particle.
 FORCE_TRAFFIC_4M = 2.845227264e9 + 0.127872512e9
+# Warp instructions fk_force issues per particle (ncu smsp__inst_executed.sum
+# of one launch on the 524,288-particle suspension / particles, mean list
+# 143.7; profiles/fk_force_fk_density_rbc_suspension_524k.md), and the SM
+# schedulers of a GB300 (152 SMs x 4), each issuing one warp instruction
+# per cycle.
+FORCE_WARP_INST_PER_PARTICLE = 345528243 / 524288
+GB300_SCHEDULERS = 152 * 4
 
 
 def measure_plain(cfg, dev, steps, warmup):
@@ -361,6 +368,17 @@ def run_ours(args):
             "launch_ms": force_ms,
             "note": f"bytes = {FORCE_STATE_BYTES} per particle + 4 per list entry (mean list {mean_nb:.1f}); "
                     "the pair physics is FP32-issue bound",
+        },
+        "issue_roofline": {
+            "kernel": "fk_force",
+            "bound": "instruction issue",
+            "achieved": FORCE_WARP_INST_PER_PARTICLE * n / (force_ms / 1e3),
+            "peak": GB300_SCHEDULERS * (clocks["sm_mhz"] if clocks else 2070.0) * 1e6,
+            "unit": "warp instructions/s",
+            "frac": FORCE_WARP_INST_PER_PARTICLE * n / (force_ms / 1e3)
+                    / (GB300_SCHEDULERS * (clocks["sm_mhz"] if clocks else 2070.0) * 1e6),
+            "note": "instructions per particle from ncu on the 524k-particle suspension; peak = 608 schedulers x "
+                    "the sampled SM clock x 1 warp instruction per cycle",
         },
         "kernels_ms_per_step": {"fk_force": force_ms, "fk_density": dens_ms},
         "output_step": out_info,
