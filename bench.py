@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--ensemble-only", action="store_true", help="only the ensemble workload")
     ap.add_argument("--ens-systems", type=int, default=64)
     ap.add_argument("--ens-steps", type=int, default=20)
+    ap.add_argument("--no-parity", dest="parity", action="store_false",
+                    help="skip the parity check against the FP64 oracle on a small channel")
     ap.add_argument("--no-output", dest="output", action="store_false",
                     help="skip timing one output step (GPUCell's output files)")
     return ap.parse_args()
@@ -253,6 +255,7 @@ def run_ours(args):
     t_ms = max_over_ranks(ev0.elapsed_time(ev1))
     clocks = sampler.stop(local) if rank == 0 else None
     st1 = fs.stats()
+    diag = fs.diagnostics()
     # per-kernel CUDA-event timing on the launching stream (a separate pass,
     # host-driven, so that the timed steps above run as configured)
     fs.profile(True)
@@ -323,6 +326,7 @@ def run_ours(args):
 
     fs.close()
     ens = run_ensemble(args, dev, rank, world, barrier, max_over_ranks) if args.ensemble else None
+    parity = parity_check() if (args.parity and rank == 0) else None
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -382,6 +386,11 @@ def run_ours(args):
         },
         "kernels_ms_per_step": {"fk_force": force_ms, "fk_density": dens_ms},
         "output_step": out_info,
+        "diagnostics_fp64": {"momentum": [float(x) for x in diag["momentum"]],
+                             "kinetic_energy": diag["kinetic_energy"], "kT": diag["temperature"],
+                             "max_speed": diag["max_speed"], "mean_fluid_density": diag["mean_fluid_density"],
+                             "note": "after the timed steps, reduced on the GPU in FP64 (gc_ensemble_diagnostics)"},
+        "parity": parity,
         "lists": {"rebuilds_in_timed_steps": st1["rebuilds"] - st0["rebuilds"], "mean_length": mean_nb,
                   "max_length": st1["max_neighbors"], "capacity": st1["capacity"]},
         "device_flags": flags,
@@ -488,6 +497,44 @@ def run_ensemble(args, dev, rank, world, barrier, max_over_ranks):
     out["speedup_vs_sequential_plain_fp32"] = out["value"] / plain_v
     out["speedup_vs_sequential_fused"] = out["value"] / fused_v
     return out
+
+
+def parity_check(steps=100):
+    """The fused step against the FP64 oracle on a walled channel with one
+    red cell (Bound1 and Bound2 walls, 5.9k particles, noise off): largest
+    position error, velocity-profile error (8 bins across the channel,
+    relative to the largest bin velocity) and membrane area/volume errors
+    after `steps` steps."""
+    import numpy as np
+    from gpucell_gb300 import generator
+    from gpucell_gb300.build import build_oracle
+    from gpucell_gb300.fused import FusedSystem
+    build_oracle()
+    from oracle.binding import Oracle
+    cfg = generator.small_channel()
+    fs = FusedSystem(cfg, noise=False)
+    o = Oracle(cfg, noise=False, nthreads=os.cpu_count() or 1)
+    o.setup()
+    fs.step(steps, 1)
+    for _ in range(steps):
+        o.step()
+    g = fs.fetch()
+    fs.close()
+    fl = slice(cfg.n_b1 + cfg.n_b2, cfg.n_cell_start)
+    lo, hi = float(cfg.bbox[2]), float(cfg.bbox[3])
+
+    def profile(pos, vel):
+        b = np.clip(((pos[fl, 1] - lo) / (hi - lo) * 8).astype(int), 0, 7)
+        return np.array([vel[fl, 0][b == k].mean() for k in range(8)])
+
+    pg, po = profile(g["pos"].astype(np.float64), g["vel"].astype(np.float64)), profile(o.pos, o.vel)
+    return {"workload": f"walled channel, {cfg.n} particles, one {cfg.ncp}-vertex cell, noise off",
+            "steps": steps,
+            "max_position_error": float(np.abs(g["pos"] - o.pos).max()),
+            "velocity_profile_error": float(np.abs(pg - po).max() / np.abs(po).max()),
+            "area_error": float(abs(g["Area64"][0] / o.area[0] - 1)),
+            "volume_error": float(abs(g["Vol64"][0] / o.vol[0] - 1)),
+            "reference": "FP64 CPU oracle (oracle/oracle.c)"}
 
 
 def cpu_baseline(cfg, steps):

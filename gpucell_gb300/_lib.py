@@ -167,6 +167,7 @@ _SIGS = {
     "gc_ensemble_store_cells": [_P, _I] + [_P] * 7 + [_I],
     "gc_ensemble_cell_sums": [_P, _I, _P, _P],
     "gc_ensemble_cell_stats": [_P, _I, _P],
+    "gc_ensemble_diagnostics": [_P, _I, _P],
     "gc_ensemble_write_output": [_P, _I, C.c_char_p, C.c_longlong, C.c_double, _I, _I],
     "gc_fused_write_output": [_P, C.c_char_p, C.c_longlong, C.c_double, _I, _I],
     "gc_output_write": [_P, C.c_char_p, C.c_longlong, C.c_double, _I],

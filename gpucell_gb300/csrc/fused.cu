@@ -1177,6 +1177,69 @@ __global__ void fk_cell_stats(int c0, const int2* __restrict__ cell_verts, const
     }
 }
 
+// Diagnostics of the ids [id0, id0 + count): per block, FP64 partial sums of
+// the momentum and kinetic energy of the moving particles (fluid and
+// membrane), their count, the largest speed, and the density sum and count
+// of the fluid particles; fk_diag_final adds the blocks in order.
+constexpr int kDiagBS = 256;
+constexpr int kDiagVals = 9;   // px py pz  2 E_kin  n_mobile  max|v|  sum rho  n_fluid  (unused)
+
+__global__ void __launch_bounds__(kDiagBS) fk_diag_partial(int count, unsigned id0, unsigned fl, unsigned cs,
+                                                          float mass, const int* __restrict__ slot_of,
+                                                          const float4* __restrict__ vel,
+                                                          const float2* __restrict__ dp,
+                                                          double* __restrict__ partial) {
+    __shared__ double sh[32];
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[kDiagVals] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (k < count) {
+        unsigned id = id0 + k;
+        int i = slot_of[id];
+        if (id >= fl) {
+            float4 u = vel[i];
+            v[0] = (double)mass * u.x;
+            v[1] = (double)mass * u.y;
+            v[2] = (double)mass * u.z;
+            v[3] = (double)mass * ((double)u.x * u.x + (double)u.y * u.y + (double)u.z * u.z);
+            v[4] = 1.0;
+            v[5] = sqrt((double)u.x * u.x + (double)u.y * u.y + (double)u.z * u.z);
+        }
+        if (id >= fl && id < cs) {
+            v[6] = (double)mass / (double)dp[i].x;
+            v[7] = 1.0;
+        }
+    }
+    for (int q = 0; q < kDiagVals; ++q) {
+        double x = v[q];
+        if (q == 5) {   // maximum
+#pragma unroll
+            for (int o = 16; o; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+            if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = x;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double m = 0.0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, sh[w]);
+                partial[(size_t)blockIdx.x * kDiagVals + q] = m;
+            }
+            __syncthreads();
+        } else {
+            double t = block_sum_d(x, sh);
+            if (threadIdx.x == 0) partial[(size_t)blockIdx.x * kDiagVals + q] = t;
+        }
+    }
+}
+
+__global__ void fk_diag_final(int nblocks, const double* __restrict__ partial, double* __restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double acc[kDiagVals] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int b = 0; b < nblocks; ++b)
+        for (int q = 0; q < kDiagVals; ++q) {
+            double x = partial[(size_t)b * kDiagVals + q];
+            acc[q] = q == 5 ? fmax(acc[q], x) : acc[q] + x;
+        }
+    for (int q = 0; q < kDiagVals; ++q) out[q] = acc[q];
+}
+
 // system index of the slots (set-up, slot = id)
 __global__ void fk_fill_sys(int n, const SysInfo* __restrict__ sys, int nsys, int* __restrict__ sysid) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1292,6 +1355,7 @@ struct GcFused {
     int *inc_ptr = nullptr, *inc = nullptr;   // vertex -> its parts (CSR)
     int2* cell_verts = nullptr;  // first and last membrane vertex of each cell (global, inclusive)
     double* cell_stats = nullptr;   // ncell x 12, see gc_ensemble_cell_stats
+    double* diag = nullptr;         // diagnostics partial sums and result
     bool cells_adopted = false;   // membranes taken from the boundary entry points' buffers
     bool have_agg = false;
     bool setup_done = false;
@@ -2492,6 +2556,40 @@ int gc_ensemble_cell_stats(GcFused* f, int sys, double* out) {
     GC_CUDA(cudaMemcpyAsync(out, f->cell_stats, 12 * sizeof(double) * h.ncell, cudaMemcpyDeviceToHost, f->st),
             "cell_stats");
     GC_CUDA(cudaStreamSynchronize(f->st), "cell_stats");
+    return GC_OK;
+}
+
+int gc_ensemble_diagnostics(GcFused* f, int sys, double* out) {
+    GC_TRY(check_sys(f, sys, "diagnostics"));
+    if (!out) return gc_fail(GC_EINVAL, "diagnostics: NULL output");
+    if (!f->setup_done) return gc_fail(GC_ESTATE, "diagnostics: call gc_fused_setup first");
+    const SysInfo& S = f->hsys[sys];
+    const int count = (int)(S.end - S.id0);
+    const int nb = gc_blocks(count, kDiagBS);
+    if (!f->diag) {
+        int most = 0;
+        for (const SysInfo& T : f->hsys) most = std::max(most, gc_blocks((int)(T.end - T.id0), kDiagBS));
+        GC_TRY(falloc(f, &f->diag, (size_t)(most + 1) * kDiagVals));
+    }
+    fk_diag_partial<<<nb, kDiagBS, 0, f->st>>>(count, S.id0, S.fl, S.cs, f->p.mass, f->slot_of, f->a.vel, f->dp,
+                                              f->diag);
+    GC_CHECK_LAUNCH("fused: diagnostics");
+    double* res = f->diag + (size_t)nb * kDiagVals;
+    fk_diag_final<<<1, 32, 0, f->st>>>(nb, f->diag, res);
+    GC_CHECK_LAUNCH("fused: diagnostics");
+    double r[kDiagVals];
+    GC_CUDA(cudaMemcpyAsync(r, res, sizeof(r), cudaMemcpyDeviceToHost, f->st), "diagnostics");
+    GC_CUDA(cudaStreamSynchronize(f->st), "diagnostics");
+    const double nm = r[4] > 0 ? r[4] : 1.0;
+    out[0] = r[0];
+    out[1] = r[1];
+    out[2] = r[2];
+    out[3] = 0.5 * r[3];                                        // kinetic energy
+    // temperature from the peculiar velocities: (2 E_kin - |P|^2 / M) / (3 N)
+    out[4] = (r[3] - (r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) / (f->p.mass * nm)) / (3.0 * nm);
+    out[5] = r[5];                                              // largest speed
+    out[6] = r[7] > 0 ? r[6] / r[7] : 0.0;                      // mean fluid density
+    out[7] = r[4];                                              // moving particles
     return GC_OK;
 }
 

@@ -117,6 +117,15 @@ class _Handle:
             _lib.call("gc_ensemble_cell_stats", self.h, int(sys), _ptr(out))
         return out
 
+    def diagnostics(self, sys=0) -> dict:
+        """FP64 diagnostics reduced on the GPU: total momentum, kinetic energy,
+        k_B T of the peculiar velocities, largest speed, mean fluid density,
+        moving particles."""
+        out = np.zeros(8)
+        _lib.call("gc_ensemble_diagnostics", self.h, int(sys), _ptr(out))
+        return dict(momentum=out[0:3].copy(), kinetic_energy=float(out[3]), temperature=float(out[4]),
+                    max_speed=float(out[5]), mean_fluid_density=float(out[6]), moving=int(out[7]))
+
     def checkpoint(self, path):
         _lib.call("gc_fused_checkpoint", self.h, str(path).encode())
 

@@ -317,6 +317,12 @@ int gc_output_write(const GcOutputFrame* frame, const char* dir, long long step_
 /* Per-cell statistics of one system of a fused handle, reduced on the GPU in
  * FP64: ncell x 12 doubles as GcOutputFrame.cell_stats (host pointer). */
 int gc_ensemble_cell_stats(GcFused* f, int sys, double* out);
+/* Diagnostics of one system, reduced on the GPU in FP64 in a fixed order:
+ * out[0..2] total momentum of the moving (fluid and membrane) particles,
+ * out[3] their kinetic energy, out[4] k_B T from their peculiar velocities
+ * ((2 E_kin - |P|^2/M) / 3N), out[5] the largest speed, out[6] the mean fluid
+ * density, out[7] the number of moving particles.  Host pointer, 8 doubles. */
+int gc_ensemble_diagnostics(GcFused* f, int sys, double* out);
 /* Stores one system of a fused handle and writes its output files. */
 int gc_ensemble_write_output(GcFused* f, int sys, const char* dir, long long step_data, double time, int first,
                              int threads);

@@ -130,3 +130,27 @@ def test_trajectory_drift_1000_steps(cuda_device):
         drift.append(np.abs(d).max())
     print("\ndrift per 100 steps: " + " ".join(f"{x:.1e}" for x in drift))
     assert drift[-1] < 5e-4
+
+
+def test_gpu_diagnostics_match_the_stored_state(cuda_device):
+    """gc_ensemble_diagnostics (FP64 on the GPU) equals the same sums taken
+    in FP64 on the host from the stored state, and the momentum of a
+    periodic fluid without body force stays at zero."""
+    from gpucell_gb300.fused import FusedSystem
+    cfg = gen.suspension(nx=24, ny=24, nz=24, ncells=0, seed=5)
+    fs = FusedSystem(cfg, noise=True)
+    fs.step(50, 1)
+    g = fs.fetch()
+    d = fs.diagnostics()
+    m = cfg.phys.mass
+    v = g["vel"].astype(np.float64)[cfg.n_b1 + cfg.n_b2:]
+    P = m * v.sum(axis=0)
+    E = 0.5 * m * (v * v).sum()
+    T = (2 * E - (P * P).sum() / (m * v.shape[0])) / (3 * v.shape[0])
+    np.testing.assert_allclose(d["momentum"], P, rtol=1e-9, atol=1e-9)
+    assert abs(d["kinetic_energy"] / E - 1) < 1e-12 and abs(d["temperature"] / T - 1) < 1e-12
+    assert d["max_speed"] == pytest.approx(np.sqrt((v * v).sum(axis=1)).max(), rel=1e-12)
+    rho = g["rho"].astype(np.float64)[cfg.n_b1 + cfg.n_b2:cfg.n_cell_start]
+    assert d["mean_fluid_density"] == pytest.approx(rho.mean(), rel=1e-6)
+    assert d["moving"] == v.shape[0]
+    assert np.abs(d["momentum"]).max() < 1e-6 * np.sqrt(2 * E * m * v.shape[0])   # pairwise forces, no drive
