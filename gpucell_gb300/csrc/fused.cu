@@ -34,7 +34,7 @@
 //     build only when some particle moved more than skin/2), the noise key of
 //     the step is derived on the device from a step counter, and the host
 //     synchronises once per gc_fused_step call instead of once per step.
-#include "gc_internal.cuh"
+#include "fused_internal.cuh"
 
 #include <math.h>
 #include <stdio.h>
@@ -49,31 +49,11 @@
 #include <utility>
 #include <vector>
 
-namespace {
+namespace gcf {
 
-constexpr int kBS = 128;      // default threads per block
-constexpr int kMaxBS = 256;   // largest block the particle kernels accept
 
-__device__ __forceinline__ unsigned fid(float4 x) { return __float_as_uint(x.w); }
-__device__ __forceinline__ float3 xyz(float4 a) { return f3(a.x, a.y, a.z); }
 
-__device__ __forceinline__ size_t sell(int i, int k, int cap) {
-    return ((size_t)(i >> 5) * cap + k) * 32 + (i & 31);
-}
 
-// One system of an ensemble: global id ranges, grids, body force, seed.
-struct SysInfo {
-    uint64_t seed;                   // iSeed of the system (pair noise)
-    unsigned id0, b2, fl, cs, end;   // first id; first Bound2, fluid and membrane id; one past the last
-    unsigned m0;                     // first membrane index (membrane-ordered arrays)
-    int cube0;                       // first global cube of the list grid
-    int mcube0;                      // first global cube of the aggregation grid
-    float gx;                        // body force in x (ConstExtForce)
-    float invL[3];
-    int lr;                          // list-grid stencil radius: 2 for cells >= (rc + skin)/2, 1 for cubes >= rc + skin
-    GcGrid g;                        // list grid over the box
-    GcGrid mg;                       // aggregation grid: cubes at least MaxCut wide
-};
 
 __device__ __forceinline__ int stype(unsigned id, const SysInfo& S) {
     return id < S.b2 ? PT_B1 : (id < S.fl ? PT_B2 : (id < S.cs ? PT_FLUID : PT_MEMB));
@@ -236,11 +216,6 @@ __global__ void fk_cellkey(int n, const SysInfo* __restrict__ sys, const int* __
     vals[i] = i;
 }
 
-struct SlotArrays {
-    float4 *pos, *vel, *vpred, *vh, *force;
-    int4* nthro;
-    int* sys;   // system of each slot (nullptr for one system)
-};
 
 // Gathers the slot arrays into the new order and wraps every position into
 // its box on periodic axes (counting the crossings), so that the list build
@@ -388,9 +363,6 @@ __global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, const SysInfo* __
 // interleaved like the lists (word w of slot i at ((i/32)*mw + w)*32 + i%32),
 // and the number of set bits in ccnt.  The force pass then iterates only the
 // set bits, so no lane idles on an entry that does not act.
-__device__ __forceinline__ size_t mrow(int i, int w, int mw) {
-    return ((size_t)(i >> 5) * mw + w) * 32 + (i & 31);
-}
 
 #ifndef GC_DENS_MIN_BLOCKS
 #define GC_DENS_MIN_BLOCKS 5
@@ -685,23 +657,6 @@ __device__ __forceinline__ float3 mdiff(const float4* mpos, const int4* mnt, int
     return d;
 }
 
-__device__ double block_sum_d(double v, double* sh) {
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[wid] = v;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
-#pragma unroll
-        for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (threadIdx.x == 0) sh[0] = t;
-    }
-    __syncthreads();
-    double t = sh[0];
-    __syncthreads();
-    return t;
-}
 
 // Triangle geometry and per-cell area/volume (FP64 sums), one block per cell.
 __global__ void fk_mgeo(GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ cellsys, int ncell,
@@ -1126,119 +1081,8 @@ __global__ void fk_count_stats(int n, const int* __restrict__ cnt, unsigned long
     }
 }
 
-// slot of every id from the ids carried in the positions (restore)
-__global__ void fk_slot_of(int n, const float4* __restrict__ pos, int* __restrict__ slot_of, unsigned* flags) {
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    unsigned id = fid(pos[q]);
-    if (id >= (unsigned)n) {
-        raise_flag(flags, GC_FLAG_BAD_INDEX);
-        return;
-    }
-    slot_of[id] = q;
-}
 
-__global__ void fk_iota(int n, int* __restrict__ v) {
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < n) v[q] = q;
-}
 
-// Per-cell statistics for GPUCell's per-cell time series: mean deformation
-// and aggregation force and mean velocity over the cell's vertices, the
-// magnitude of the mean velocity, area and volume; FP64 sums, one block per
-// cell.
-__global__ void fk_cell_stats(int c0, const int2* __restrict__ cell_verts, const SysInfo* __restrict__ sys,
-                              const int* __restrict__ cellsys, const int* __restrict__ slot_of,
-                              const float4* __restrict__ vel, const float4* __restrict__ mforce,
-                              const float4* __restrict__ magg, int have_agg, const double* __restrict__ carea,
-                              const double* __restrict__ cvol, double* __restrict__ out) {
-    __shared__ double sh[32];
-    const int c = c0 + blockIdx.x;
-    const int2 vr = cell_verts[c];
-    const SysInfo& S = sys[cellsys ? cellsys[c] : 0];
-    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int v = vr.x + threadIdx.x; v <= vr.y; v += blockDim.x) {
-        float4 m = mforce[v];
-        float4 a = have_agg ? magg[v] : make_float4(0.f, 0.f, 0.f, 0.f);
-        float4 u = vel[slot_of[S.cs + (unsigned)(v - (int)S.m0)]];
-        acc[0] += (double)(m.x - a.x); acc[1] += (double)(m.y - a.y); acc[2] += (double)(m.z - a.z);
-        acc[3] += a.x; acc[4] += a.y; acc[5] += a.z;
-        acc[6] += u.x; acc[7] += u.y; acc[8] += u.z;
-    }
-    const double inv = 1.0 / (double)(vr.y - vr.x + 1);
-    double r[9];
-    for (int k = 0; k < 9; ++k) r[k] = block_sum_d(acc[k], sh) * inv;
-    if (threadIdx.x == 0) {
-        double* o = out + 12 * (size_t)blockIdx.x;
-        for (int k = 0; k < 9; ++k) o[k] = r[k];
-        o[9] = sqrt(r[6] * r[6] + r[7] * r[7] + r[8] * r[8]);
-        o[10] = carea[c];
-        o[11] = cvol[c];
-    }
-}
-
-// Diagnostics of the ids [id0, id0 + count): per block, FP64 partial sums of
-// the momentum and kinetic energy of the moving particles (fluid and
-// membrane), their count, the largest speed, and the density sum and count
-// of the fluid particles; fk_diag_final adds the blocks in order.
-constexpr int kDiagBS = 256;
-constexpr int kDiagVals = 9;   // px py pz  2 E_kin  n_mobile  max|v|  sum rho  n_fluid  (unused)
-
-__global__ void __launch_bounds__(kDiagBS) fk_diag_partial(int count, unsigned id0, unsigned fl, unsigned cs,
-                                                          float mass, const int* __restrict__ slot_of,
-                                                          const float4* __restrict__ vel,
-                                                          const float2* __restrict__ dp,
-                                                          double* __restrict__ partial) {
-    __shared__ double sh[32];
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    double v[kDiagVals] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    if (k < count) {
-        unsigned id = id0 + k;
-        int i = slot_of[id];
-        if (id >= fl) {
-            float4 u = vel[i];
-            v[0] = (double)mass * u.x;
-            v[1] = (double)mass * u.y;
-            v[2] = (double)mass * u.z;
-            v[3] = (double)mass * ((double)u.x * u.x + (double)u.y * u.y + (double)u.z * u.z);
-            v[4] = 1.0;
-            v[5] = sqrt((double)u.x * u.x + (double)u.y * u.y + (double)u.z * u.z);
-        }
-        if (id >= fl && id < cs) {
-            v[6] = (double)mass / (double)dp[i].x;
-            v[7] = 1.0;
-        }
-    }
-    for (int q = 0; q < kDiagVals; ++q) {
-        double x = v[q];
-        if (q == 5) {   // maximum
-#pragma unroll
-            for (int o = 16; o; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
-            if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = x;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                double m = 0.0;
-                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, sh[w]);
-                partial[(size_t)blockIdx.x * kDiagVals + q] = m;
-            }
-            __syncthreads();
-        } else {
-            double t = block_sum_d(x, sh);
-            if (threadIdx.x == 0) partial[(size_t)blockIdx.x * kDiagVals + q] = t;
-        }
-    }
-}
-
-__global__ void fk_diag_final(int nblocks, const double* __restrict__ partial, double* __restrict__ out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double acc[kDiagVals] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int b = 0; b < nblocks; ++b)
-        for (int q = 0; q < kDiagVals; ++q) {
-            double x = partial[(size_t)b * kDiagVals + q];
-            acc[q] = q == 5 ? fmax(acc[q], x) : acc[q] + x;
-        }
-    for (int q = 0; q < kDiagVals; ++q) out[q] = acc[q];
-}
 
 // system index of the slots (set-up, slot = id)
 __global__ void fk_fill_sys(int n, const SysInfo* __restrict__ sys, int nsys, int* __restrict__ sysid) {
@@ -1246,149 +1090,12 @@ __global__ void fk_fill_sys(int n, const SysInfo* __restrict__ sys, int nsys, in
     if (i < n) sysid[i] = find_sys(sys, nsys, (unsigned)i);
 }
 
-}  // namespace
+}  // namespace gcf
 
-// ---------------------------------------------------------------------------
-// Host side
-// ---------------------------------------------------------------------------
 
-namespace {
 
-// Membrane topology of one system as given (local, 1-based), until set-up.
-struct HostCells {
-    bool set = false;
-    int ncell = 0, ntri = 0, nedge = 0;
-    std::vector<int> tri, edge, betri, celltab;
-    std::vector<int> verts;   // first and last vertex of each cell (0-based), from its triangles
-    std::vector<float> shear, bend, hl, hg, hv;
-};
+namespace gcf {
 
-// Device copy of the dynamic state (snapshots for captured steps and the
-// autotuner).
-struct StateCopy {
-    SlotArrays s{};
-    float4* mpos = nullptr;
-    int4* mnthro = nullptr;
-    long long* dstep = nullptr;
-    bool have = false;
-};
-
-}  // namespace
-
-struct GcFused {
-    GcParams p;
-    int nsys = 1;
-    std::vector<SysInfo> hsys;
-    std::vector<GcSystemDesc> desc;
-    std::vector<HostCells> hcells;
-    std::vector<int> c0, t0;       // first cell and triangle of each system (after set-up)
-    std::vector<char> sys_loaded;
-    SysInfo* dsys = nullptr;
-    int K = 0, Kagg = 0;           // cubes of all list grids, of all aggregation grids
-    float skin_rel = 0.1f;         // skin in units of CutRadius
-    float skin = 0.1f;             // skin length
-    int n = 0, cap = 0, block = kBS;
-    int noise_on = 1;
-    bool compact = false;
-    bool graph = false;            // steps run as captured graphs
-    bool ens = false;              // kernels read the system table
-    long long step = -1;           // index keying the noise of the latest step
-    long long rebuilds = 0, steps = 0;
-    cudaStream_t st = 0;
-    // slot arrays (current, and the permutation target)
-    SlotArrays a{}, b{};
-    float4* refpos = nullptr;
-    float2* dp = nullptr;
-    int* slot_of = nullptr;
-    int *keys = nullptr, *vals = nullptr;
-    int *nbr = nullptr, *cnt = nullptr;
-    size_t nbr_elems = 0;
-    unsigned* cmask = nullptr;   // per-step bit mask of the acting list entries
-    size_t cmask_elems = 0;
-    int* ccnt = nullptr;         // number of acting entries
-    int mw = 0;                  // mask words per slot
-    int* rebuild = nullptr;
-    unsigned* flags = nullptr;
-    unsigned* oflag = nullptr;   // list overflow inside captured steps
-    unsigned long long* stat_sum = nullptr;
-    int* stat_max = nullptr;
-    long long* dstep = nullptr;  // device step counter (ensembles, captured steps)
-    unsigned* nkey = nullptr;    // per-system noise key of the current step
-    unsigned long long* drebuilds = nullptr;   // rebuilds inside captured steps
-    // pinned words read back after steps: rebuild flag, overflow flag, device rebuild count
-    struct Pinned {
-        int rebuild;
-        unsigned oflag;
-        unsigned long long drebuilds;
-    }* h = nullptr;
-    unsigned long long drebuilds_seen = 0;
-    // counting-sort temporaries (owned, so a captured step can use them)
-    void* sortmem = nullptr;
-    size_t sortmem_bytes = 0;
-    int sort_n = 0, sort_K = 0;
-    GcSortBufs sb{};
-    void* sortmem_agg = nullptr;   // the aggregation sort's own temporaries: it runs beside the list rebuild
-    int sort_agg_n = 0, sort_agg_K = 0;
-    GcSortBufs sb_agg{};
-    // The membrane kernels depend only on the integrated membrane positions:
-    // they run on their own stream from the end of the integration to the
-    // force pass, beside the rebuild check, the list rebuild and the density.
-    cudaStream_t mst = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    // membranes (global indices over the ensemble)
-    int ncell = 0, ntri = 0, nedge = 0, ncp = 0;
-    int3* tri = nullptr;
-    int6* edge = nullptr;
-    int2* betri = nullptr;
-    int* celltab = nullptr;
-    int *msys = nullptr, *cellsys = nullptr;
-    float *shear = nullptr, *bend = nullptr, *hl = nullptr, *hg = nullptr, *hv = nullptr;
-    float *l0 = nullptr, *lmax = nullptr, *perlen = nullptr, *hpow = nullptr, *hbend = nullptr, *refang = nullptr;
-    float *tarea = nullptr, *reftarea = nullptr;
-    float4 *tnorm = nullptr, *tcen = nullptr;
-    double *carea = nullptr, *cvol = nullptr, *crefarea = nullptr, *crefvol = nullptr;
-    float4 *mpos = nullptr, *mforce = nullptr, *magg = nullptr;
-    int4* mnthro = nullptr;
-    float* parea = nullptr;
-    int *mkeys = nullptr, *mvals = nullptr;
-    float4* mparts = nullptr;    // per-edge and per-triangle vertex forces (4 per edge, then 3 per triangle)
-    int *inc_ptr = nullptr, *inc = nullptr;   // vertex -> its parts (CSR)
-    int2* cell_verts = nullptr;  // first and last membrane vertex of each cell (global, inclusive)
-    double* cell_stats = nullptr;   // ncell x 12, see gc_ensemble_cell_stats
-    double* diag = nullptr;         // diagnostics partial sums and result
-    bool cells_adopted = false;   // membranes taken from the boundary entry points' buffers
-    bool have_agg = false;
-    bool setup_done = false;
-    // captured steps
-    cudaStream_t gst = nullptr, gst2 = nullptr, gst3 = nullptr;
-    cudaGraph_t cg[2] = {};
-    cudaGraphExec_t gexec[2] = {};
-    bool graph_dirty = true;
-    long long kernels_step = 0, kernels_rebuild = 0;   // kernels per captured step and per rebuild body
-    StateCopy snap;    // state at the start of a captured gc_fused_step call
-    StateCopy tsnap;   // state at the start of an autotune
-    // optional CUDA-event timing of the dominant kernels (fk_density, fk_force)
-    bool profile = false;
-    std::vector<cudaEvent_t> ev;   // pairs: density start/stop, force start/stop
-    size_t ev_used = 0;
-    // staging for host pointers
-    void* stage = nullptr;
-    size_t stage_bytes = 0;
-    std::vector<void*> allocs;
-};
-
-namespace {
-
-template <class T>
-int falloc(GcFused* f, T** p, size_t count) {
-    void* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, (count ? count : 1) * sizeof(T));
-    if (e != cudaSuccess) return gc_fail(GC_ENOMEM, "fused: cudaMalloc(%zu) failed: %s", count * sizeof(T),
-                                         cudaGetErrorString(e));
-    f->allocs.push_back(q);
-    *p = (T*)q;
-    return GC_OK;
-}
 
 int stage_bytes(GcFused* f, size_t bytes) {
     if (f->stage_bytes >= bytes) return GC_OK;
@@ -2109,7 +1816,127 @@ int apply_options(GcFused* f, const GcFusedOptions* opt) {
     return GC_OK;
 }
 
-}  // namespace
+}  // namespace gcf
+
+namespace gcf {
+
+// Loads the ids [id_base, id_base + count) from host or device arrays.
+int load_range(GcFused* f, unsigned id_base, int count, const float* pos, const float* vel,
+                      const float* velhalf, const float* force, const int* nthro, int from_device) {
+    if (count <= 0) return GC_OK;
+    cudaStream_t st = f->st;
+    const float *dx = pos, *dv = vel, *dh = velhalf, *df = force;
+    const int* dn = nthro;
+    if (!from_device) {
+        size_t b3 = (size_t)count * 12;
+        GC_TRY(stage_bytes(f, 5 * b3));
+        char* s = (char*)f->stage;
+        cudaError_t ce = cudaSuccess;
+        auto up = [&](const void* src, size_t off) -> const void* {
+            if (!src) return nullptr;
+            cudaError_t e = cudaMemcpyAsync(s + off, src, b3, cudaMemcpyHostToDevice, st);
+            if (e != cudaSuccess) ce = e;
+            return s + off;
+        };
+        dx = (const float*)up(pos, 0);
+        dv = (const float*)up(vel, b3);
+        dh = (const float*)up(velhalf, 2 * b3);
+        df = (const float*)up(force, 3 * b3);
+        dn = (const int*)up(nthro, 4 * b3);
+        GC_CUDA(ce, "fused_load: upload");
+    }
+    int keep = f->setup_done ? 1 : 0;
+    fk_load<<<gc_blocks(count, f->block), f->block, 0, st>>>(count, id_base, f->dsys, f->nsys, keep, dx, dv, dh, df,
+                                                             dn, f->slot_of, f->a.pos, f->a.vel, f->a.vh, f->a.force,
+                                                             f->a.nthro, keep && f->ncell > 0 ? f->mpos : nullptr,
+                                                             f->mnthro);
+    GC_CHECK_LAUNCH("fused: load");
+    if (!from_device) GC_CUDA(cudaStreamSynchronize(st), "fused_load");   // the staging buffer is reused
+    return GC_OK;
+}
+
+int store_range(GcFused* f, unsigned id_base, int count, float* pos, float* vel, float* rho, float* press,
+                       float* force, float* velhalf, int* nthro, int to_device) {
+    if (count <= 0) return GC_OK;
+    cudaStream_t st = f->st;
+    float *x = pos, *v = vel, *r = rho, *pr = press, *fo = force, *vh = velhalf;
+    int* nt = nthro;
+    size_t b3 = (size_t)count * 12, b1 = (size_t)count * 4;
+    if (!to_device) {
+        GC_TRY(stage_bytes(f, 5 * b3 + 2 * b1));
+        char* s = (char*)f->stage;
+        x = pos ? (float*)(s) : nullptr;
+        v = vel ? (float*)(s + b3) : nullptr;
+        fo = force ? (float*)(s + 2 * b3) : nullptr;
+        vh = velhalf ? (float*)(s + 3 * b3) : nullptr;
+        nt = nthro ? (int*)(s + 4 * b3) : nullptr;
+        r = rho ? (float*)(s + 5 * b3) : nullptr;
+        pr = press ? (float*)(s + 5 * b3 + b1) : nullptr;
+    }
+    fk_store<<<gc_blocks(count, f->block), f->block, 0, st>>>(count, id_base, f->p, f->slot_of, f->a.pos, f->a.vel,
+                                                              f->a.vh, f->a.force, f->dp, f->a.nthro, x, v, r, pr, fo,
+                                                              vh, nt);
+    GC_CHECK_LAUNCH("fused: store");
+    if (!to_device) {
+        if (pos) GC_CUDA(cudaMemcpyAsync(pos, x, b3, cudaMemcpyDeviceToHost, st), "fused_store");
+        if (vel) GC_CUDA(cudaMemcpyAsync(vel, v, b3, cudaMemcpyDeviceToHost, st), "fused_store");
+        if (force) GC_CUDA(cudaMemcpyAsync(force, fo, b3, cudaMemcpyDeviceToHost, st), "fused_store");
+        if (velhalf) GC_CUDA(cudaMemcpyAsync(velhalf, vh, b3, cudaMemcpyDeviceToHost, st), "fused_store");
+        if (nthro) GC_CUDA(cudaMemcpyAsync(nthro, nt, b3, cudaMemcpyDeviceToHost, st), "fused_store");
+        if (rho) GC_CUDA(cudaMemcpyAsync(rho, r, b1, cudaMemcpyDeviceToHost, st), "fused_store");
+        if (press) GC_CUDA(cudaMemcpyAsync(press, pr, b1, cudaMemcpyDeviceToHost, st), "fused_store");
+        GC_CUDA(cudaStreamSynchronize(st), "fused_store");
+    }
+    return GC_OK;
+}
+
+// Membrane outputs of cells [c0, c0 + nc), vertices [m0, m0 + nv),
+// triangles [t0, t0 + nt).
+int store_cells_range(GcFused* f, int c0, int nc, int m0, int nv, int t0, int nt, float* area, float* vol,
+                             float* defforce, float* aggforce, float* trinordir, float* tricenter, float* pararea,
+                             int to_device) {
+    if (f->ncell <= 0 || nc <= 0) return GC_OK;
+    cudaStream_t st = f->st;
+    float *a = area, *vo = vol, *df = defforce, *ag = aggforce, *tn = trinordir, *tc = tricenter, *pa = pararea;
+    size_t snc = nc, snv = nv, snt = nt;
+    if (!to_device) {
+        GC_TRY(stage_bytes(f, 4 * (2 * snc + 3 * snv + 3 * snv + 3 * snt + 3 * snt + snv) + 64));
+        char* s = (char*)f->stage;
+        size_t off = 0;
+        auto take = [&](size_t cnt) { float* q = (float*)(s + off); off += 4 * cnt; return q; };
+        a = take(snc); vo = take(snc); df = take(3 * snv); ag = take(3 * snv); tn = take(3 * snt); tc = take(3 * snt);
+        pa = take(snv);
+    }
+    fk_cast_cells<<<gc_blocks(nc, 128), 128, 0, st>>>(nc, c0, f->carea, f->cvol, a, vo);
+    GC_CHECK_LAUNCH("fused: store cells");
+    int m = nv > nt ? nv : nt;
+    fk_store_cells<<<gc_blocks(m, 128), 128, 0, st>>>(nv, m0, nt, t0, f->mforce, f->magg, f->parea, f->tnorm, f->tcen,
+                                                     df, ag, pa, tn, tc, f->have_agg ? 1 : 0);
+    GC_CHECK_LAUNCH("fused: store cells");
+    if (!to_device) {
+        if (area) GC_CUDA(cudaMemcpyAsync(area, a, 4 * snc, cudaMemcpyDeviceToHost, st), "store cells");
+        if (vol) GC_CUDA(cudaMemcpyAsync(vol, vo, 4 * snc, cudaMemcpyDeviceToHost, st), "store cells");
+        if (defforce) GC_CUDA(cudaMemcpyAsync(defforce, df, 12 * snv, cudaMemcpyDeviceToHost, st), "store cells");
+        if (aggforce) GC_CUDA(cudaMemcpyAsync(aggforce, ag, 12 * snv, cudaMemcpyDeviceToHost, st), "store cells");
+        if (trinordir) GC_CUDA(cudaMemcpyAsync(trinordir, tn, 12 * snt, cudaMemcpyDeviceToHost, st), "store cells");
+        if (tricenter) GC_CUDA(cudaMemcpyAsync(tricenter, tc, 12 * snt, cudaMemcpyDeviceToHost, st), "store cells");
+        if (pararea) GC_CUDA(cudaMemcpyAsync(pararea, pa, 4 * snv, cudaMemcpyDeviceToHost, st), "store cells");
+        GC_CUDA(cudaStreamSynchronize(st), "store cells");
+    }
+    return GC_OK;
+}
+
+int cell_sums_range(GcFused* f, int c0, int nc, double* area, double* vol) {
+    if (f->ncell <= 0 || nc <= 0) return GC_OK;
+    if (area) GC_CUDA(cudaMemcpyAsync(area, f->carea + c0, 8 * (size_t)nc, cudaMemcpyDeviceToHost, f->st), "cell sums");
+    if (vol) GC_CUDA(cudaMemcpyAsync(vol, f->cvol + c0, 8 * (size_t)nc, cudaMemcpyDeviceToHost, f->st), "cell sums");
+    GC_CUDA(cudaStreamSynchronize(f->st), "cell sums");
+    return GC_OK;
+}
+
+}  // namespace gcf
+
+using namespace gcf;
 
 extern "C" {
 
@@ -2320,40 +2147,6 @@ int gc_fused_set_cells(GcFused* f, int ncell, int ntri, int nedge, const int* tr
                                  hgarea, hvol);
 }
 
-// Loads the ids [id_base, id_base + count) from host or device arrays.
-static int load_range(GcFused* f, unsigned id_base, int count, const float* pos, const float* vel,
-                      const float* velhalf, const float* force, const int* nthro, int from_device) {
-    if (count <= 0) return GC_OK;
-    cudaStream_t st = f->st;
-    const float *dx = pos, *dv = vel, *dh = velhalf, *df = force;
-    const int* dn = nthro;
-    if (!from_device) {
-        size_t b3 = (size_t)count * 12;
-        GC_TRY(stage_bytes(f, 5 * b3));
-        char* s = (char*)f->stage;
-        cudaError_t ce = cudaSuccess;
-        auto up = [&](const void* src, size_t off) -> const void* {
-            if (!src) return nullptr;
-            cudaError_t e = cudaMemcpyAsync(s + off, src, b3, cudaMemcpyHostToDevice, st);
-            if (e != cudaSuccess) ce = e;
-            return s + off;
-        };
-        dx = (const float*)up(pos, 0);
-        dv = (const float*)up(vel, b3);
-        dh = (const float*)up(velhalf, 2 * b3);
-        df = (const float*)up(force, 3 * b3);
-        dn = (const int*)up(nthro, 4 * b3);
-        GC_CUDA(ce, "fused_load: upload");
-    }
-    int keep = f->setup_done ? 1 : 0;
-    fk_load<<<gc_blocks(count, f->block), f->block, 0, st>>>(count, id_base, f->dsys, f->nsys, keep, dx, dv, dh, df,
-                                                             dn, f->slot_of, f->a.pos, f->a.vel, f->a.vh, f->a.force,
-                                                             f->a.nthro, keep && f->ncell > 0 ? f->mpos : nullptr,
-                                                             f->mnthro);
-    GC_CHECK_LAUNCH("fused: load");
-    if (!from_device) GC_CUDA(cudaStreamSynchronize(st), "fused_load");   // the staging buffer is reused
-    return GC_OK;
-}
 
 int gc_ensemble_load(GcFused* f, int sys, const float* pos, const float* vel, const float* velhalf, const float* force,
                      const int* nthro, int from_device) {
@@ -2422,40 +2215,6 @@ int gc_fused_step(GcFused* f, int nsteps, int drive_on) {
     return GC_OK;
 }
 
-static int store_range(GcFused* f, unsigned id_base, int count, float* pos, float* vel, float* rho, float* press,
-                       float* force, float* velhalf, int* nthro, int to_device) {
-    if (count <= 0) return GC_OK;
-    cudaStream_t st = f->st;
-    float *x = pos, *v = vel, *r = rho, *pr = press, *fo = force, *vh = velhalf;
-    int* nt = nthro;
-    size_t b3 = (size_t)count * 12, b1 = (size_t)count * 4;
-    if (!to_device) {
-        GC_TRY(stage_bytes(f, 5 * b3 + 2 * b1));
-        char* s = (char*)f->stage;
-        x = pos ? (float*)(s) : nullptr;
-        v = vel ? (float*)(s + b3) : nullptr;
-        fo = force ? (float*)(s + 2 * b3) : nullptr;
-        vh = velhalf ? (float*)(s + 3 * b3) : nullptr;
-        nt = nthro ? (int*)(s + 4 * b3) : nullptr;
-        r = rho ? (float*)(s + 5 * b3) : nullptr;
-        pr = press ? (float*)(s + 5 * b3 + b1) : nullptr;
-    }
-    fk_store<<<gc_blocks(count, f->block), f->block, 0, st>>>(count, id_base, f->p, f->slot_of, f->a.pos, f->a.vel,
-                                                              f->a.vh, f->a.force, f->dp, f->a.nthro, x, v, r, pr, fo,
-                                                              vh, nt);
-    GC_CHECK_LAUNCH("fused: store");
-    if (!to_device) {
-        if (pos) GC_CUDA(cudaMemcpyAsync(pos, x, b3, cudaMemcpyDeviceToHost, st), "fused_store");
-        if (vel) GC_CUDA(cudaMemcpyAsync(vel, v, b3, cudaMemcpyDeviceToHost, st), "fused_store");
-        if (force) GC_CUDA(cudaMemcpyAsync(force, fo, b3, cudaMemcpyDeviceToHost, st), "fused_store");
-        if (velhalf) GC_CUDA(cudaMemcpyAsync(velhalf, vh, b3, cudaMemcpyDeviceToHost, st), "fused_store");
-        if (nthro) GC_CUDA(cudaMemcpyAsync(nthro, nt, b3, cudaMemcpyDeviceToHost, st), "fused_store");
-        if (rho) GC_CUDA(cudaMemcpyAsync(rho, r, b1, cudaMemcpyDeviceToHost, st), "fused_store");
-        if (press) GC_CUDA(cudaMemcpyAsync(press, pr, b1, cudaMemcpyDeviceToHost, st), "fused_store");
-        GC_CUDA(cudaStreamSynchronize(st), "fused_store");
-    }
-    return GC_OK;
-}
 
 int gc_fused_store(GcFused* f, float* pos, float* vel, float* rho, float* press, float* force, float* velhalf,
                    int* nthro, int to_device) {
@@ -2470,41 +2229,6 @@ int gc_ensemble_store(GcFused* f, int sys, float* pos, float* vel, float* rho, f
     return store_range(f, S.id0, (int)(S.end - S.id0), pos, vel, rho, press, force, velhalf, nthro, to_device);
 }
 
-// Membrane outputs of cells [c0, c0 + nc), vertices [m0, m0 + nv),
-// triangles [t0, t0 + nt).
-static int store_cells_range(GcFused* f, int c0, int nc, int m0, int nv, int t0, int nt, float* area, float* vol,
-                             float* defforce, float* aggforce, float* trinordir, float* tricenter, float* pararea,
-                             int to_device) {
-    if (f->ncell <= 0 || nc <= 0) return GC_OK;
-    cudaStream_t st = f->st;
-    float *a = area, *vo = vol, *df = defforce, *ag = aggforce, *tn = trinordir, *tc = tricenter, *pa = pararea;
-    size_t snc = nc, snv = nv, snt = nt;
-    if (!to_device) {
-        GC_TRY(stage_bytes(f, 4 * (2 * snc + 3 * snv + 3 * snv + 3 * snt + 3 * snt + snv) + 64));
-        char* s = (char*)f->stage;
-        size_t off = 0;
-        auto take = [&](size_t cnt) { float* q = (float*)(s + off); off += 4 * cnt; return q; };
-        a = take(snc); vo = take(snc); df = take(3 * snv); ag = take(3 * snv); tn = take(3 * snt); tc = take(3 * snt);
-        pa = take(snv);
-    }
-    fk_cast_cells<<<gc_blocks(nc, 128), 128, 0, st>>>(nc, c0, f->carea, f->cvol, a, vo);
-    GC_CHECK_LAUNCH("fused: store cells");
-    int m = nv > nt ? nv : nt;
-    fk_store_cells<<<gc_blocks(m, 128), 128, 0, st>>>(nv, m0, nt, t0, f->mforce, f->magg, f->parea, f->tnorm, f->tcen,
-                                                     df, ag, pa, tn, tc, f->have_agg ? 1 : 0);
-    GC_CHECK_LAUNCH("fused: store cells");
-    if (!to_device) {
-        if (area) GC_CUDA(cudaMemcpyAsync(area, a, 4 * snc, cudaMemcpyDeviceToHost, st), "store cells");
-        if (vol) GC_CUDA(cudaMemcpyAsync(vol, vo, 4 * snc, cudaMemcpyDeviceToHost, st), "store cells");
-        if (defforce) GC_CUDA(cudaMemcpyAsync(defforce, df, 12 * snv, cudaMemcpyDeviceToHost, st), "store cells");
-        if (aggforce) GC_CUDA(cudaMemcpyAsync(aggforce, ag, 12 * snv, cudaMemcpyDeviceToHost, st), "store cells");
-        if (trinordir) GC_CUDA(cudaMemcpyAsync(trinordir, tn, 12 * snt, cudaMemcpyDeviceToHost, st), "store cells");
-        if (tricenter) GC_CUDA(cudaMemcpyAsync(tricenter, tc, 12 * snt, cudaMemcpyDeviceToHost, st), "store cells");
-        if (pararea) GC_CUDA(cudaMemcpyAsync(pararea, pa, 4 * snv, cudaMemcpyDeviceToHost, st), "store cells");
-        GC_CUDA(cudaStreamSynchronize(st), "store cells");
-    }
-    return GC_OK;
-}
 
 int gc_fused_store_cells(GcFused* f, float* area, float* vol, float* defforce, float* aggforce, float* trinordir,
                          float* tricenter, float* pararea, int to_device) {
@@ -2524,13 +2248,6 @@ int gc_ensemble_store_cells(GcFused* f, int sys, float* area, float* vol, float*
                              defforce, aggforce, trinordir, tricenter, pararea, to_device);
 }
 
-static int cell_sums_range(GcFused* f, int c0, int nc, double* area, double* vol) {
-    if (f->ncell <= 0 || nc <= 0) return GC_OK;
-    if (area) GC_CUDA(cudaMemcpyAsync(area, f->carea + c0, 8 * (size_t)nc, cudaMemcpyDeviceToHost, f->st), "cell sums");
-    if (vol) GC_CUDA(cudaMemcpyAsync(vol, f->cvol + c0, 8 * (size_t)nc, cudaMemcpyDeviceToHost, f->st), "cell sums");
-    GC_CUDA(cudaStreamSynchronize(f->st), "cell sums");
-    return GC_OK;
-}
 
 int gc_fused_cell_sums(GcFused* f, double* area, double* vol) {
     if (!f) return gc_fail(GC_EINVAL, "fused_cell_sums: NULL handle");
@@ -2541,108 +2258,6 @@ int gc_ensemble_cell_sums(GcFused* f, int sys, double* area, double* vol) {
     GC_TRY(check_sys(f, sys, "cell_sums"));
     if (!f->setup_done || !f->hcells[sys].set) return GC_OK;
     return cell_sums_range(f, f->c0[sys], f->hcells[sys].ncell, area, vol);
-}
-
-int gc_ensemble_cell_stats(GcFused* f, int sys, double* out) {
-    GC_TRY(check_sys(f, sys, "cell_stats"));
-    if (!out) return gc_fail(GC_EINVAL, "cell_stats: NULL output");
-    if (!f->setup_done) return gc_fail(GC_ESTATE, "cell_stats: call gc_fused_setup first");
-    const HostCells& h = f->hcells[sys];
-    if (!h.set || h.ncell <= 0) return GC_OK;
-    fk_cell_stats<<<h.ncell, 256, 0, f->st>>>(f->c0[sys], f->cell_verts, f->dsys, f->cellsys, f->slot_of, f->a.vel,
-                                             f->mforce, f->magg, f->have_agg ? 1 : 0, f->carea, f->cvol,
-                                             f->cell_stats);
-    GC_CHECK_LAUNCH("fused: cell statistics");
-    GC_CUDA(cudaMemcpyAsync(out, f->cell_stats, 12 * sizeof(double) * h.ncell, cudaMemcpyDeviceToHost, f->st),
-            "cell_stats");
-    GC_CUDA(cudaStreamSynchronize(f->st), "cell_stats");
-    return GC_OK;
-}
-
-int gc_ensemble_diagnostics(GcFused* f, int sys, double* out) {
-    GC_TRY(check_sys(f, sys, "diagnostics"));
-    if (!out) return gc_fail(GC_EINVAL, "diagnostics: NULL output");
-    if (!f->setup_done) return gc_fail(GC_ESTATE, "diagnostics: call gc_fused_setup first");
-    const SysInfo& S = f->hsys[sys];
-    const int count = (int)(S.end - S.id0);
-    const int nb = gc_blocks(count, kDiagBS);
-    if (!f->diag) {
-        int most = 0;
-        for (const SysInfo& T : f->hsys) most = std::max(most, gc_blocks((int)(T.end - T.id0), kDiagBS));
-        GC_TRY(falloc(f, &f->diag, (size_t)(most + 1) * kDiagVals));
-    }
-    fk_diag_partial<<<nb, kDiagBS, 0, f->st>>>(count, S.id0, S.fl, S.cs, f->p.mass, f->slot_of, f->a.vel, f->dp,
-                                              f->diag);
-    GC_CHECK_LAUNCH("fused: diagnostics");
-    double* res = f->diag + (size_t)nb * kDiagVals;
-    fk_diag_final<<<1, 32, 0, f->st>>>(nb, f->diag, res);
-    GC_CHECK_LAUNCH("fused: diagnostics");
-    double r[kDiagVals];
-    GC_CUDA(cudaMemcpyAsync(r, res, sizeof(r), cudaMemcpyDeviceToHost, f->st), "diagnostics");
-    GC_CUDA(cudaStreamSynchronize(f->st), "diagnostics");
-    const double nm = r[4] > 0 ? r[4] : 1.0;
-    out[0] = r[0];
-    out[1] = r[1];
-    out[2] = r[2];
-    out[3] = 0.5 * r[3];                                        // kinetic energy
-    // temperature from the peculiar velocities: (2 E_kin - |P|^2 / M) / (3 N)
-    out[4] = (r[3] - (r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) / (f->p.mass * nm)) / (3.0 * nm);
-    out[5] = r[5];                                              // largest speed
-    out[6] = r[7] > 0 ? r[6] / r[7] : 0.0;                      // mean fluid density
-    out[7] = r[4];                                              // moving particles
-    return GC_OK;
-}
-
-int gc_ensemble_write_output(GcFused* f, int sys, const char* dir, long long step_data, double time, int first,
-                             int threads) {
-    GC_TRY(check_sys(f, sys, "write_output"));
-    if (!dir) return gc_fail(GC_EINVAL, "write_output: NULL directory");
-    if (!f->setup_done) return gc_fail(GC_ESTATE, "write_output: call gc_fused_setup first");
-    const SysInfo& S = f->hsys[sys];
-    const HostCells& h = f->hcells[sys];
-    const int n = (int)(S.end - S.id0), ncp = (int)(S.end - S.cs);
-    std::vector<float> pos(3 * (size_t)n), vel(3 * (size_t)n), rho(n), press(n);
-    GC_TRY(store_range(f, S.id0, n, pos.data(), vel.data(), rho.data(), press.data(), nullptr, nullptr, nullptr, 0));
-    GcOutputFrame fr;
-    memset(&fr, 0, sizeof(fr));
-    fr.n = n;
-    fr.n_b1 = S.b2 - S.id0;
-    fr.n_b2 = S.fl - S.b2;
-    fr.n_cell_start = S.cs - S.id0;
-    fr.pos = pos.data();
-    fr.vel = vel.data();
-    fr.rho = rho.data();
-    fr.press = press.data();
-    fr.threads = threads;
-    std::vector<float> def, agg, cen, nor;
-    std::vector<double> stats;
-    if (h.set && h.ncell > 0) {
-        def.resize(3 * (size_t)ncp);
-        agg.resize(3 * (size_t)ncp);
-        cen.resize(3 * (size_t)h.ntri);
-        nor.resize(3 * (size_t)h.ntri);
-        stats.resize(12 * (size_t)h.ncell);
-        GC_TRY(gc_ensemble_store_cells(f, sys, nullptr, nullptr, def.data(), agg.data(), nor.data(), cen.data(),
-                                       nullptr, 0));
-        GC_TRY(gc_ensemble_cell_stats(f, sys, stats.data()));
-        fr.ncell = h.ncell;
-        fr.ntri = h.ntri;
-        fr.cell_verts = h.verts.data();
-        fr.tri = h.tri.data();
-        fr.betri = h.betri.data();
-        fr.defforce = def.data();
-        fr.aggforce = agg.data();
-        fr.tricenter = cen.data();
-        fr.trinordir = nor.data();
-        fr.cell_stats = stats.data();
-    }
-    return gc_output_write(&fr, dir, step_data, time, first);
-}
-
-int gc_fused_write_output(GcFused* f, const char* dir, long long step_data, double time, int first, int threads) {
-    if (!f) return gc_fail(GC_EINVAL, "write_output: NULL handle");
-    if (f->nsys != 1) return gc_fail(GC_EINVAL, "write_output: an ensemble writes one system at a time");
-    return gc_ensemble_write_output(f, 0, dir, step_data, time, first, threads);
 }
 
 int gc_fused_stats(GcFused* f, long long* rebuilds, long long* steps, int* list_capacity, double* mean_neighbors,
@@ -2766,550 +2381,3 @@ int gc_fused_destroy(GcFused* f) {
 }  // extern "C"
 
 
-// ---------------------------------------------------------------------------
-// Checkpoint and restart.
-//
-// The file holds what the next steps depend on: the slot-ordered state (with
-// the slot order itself, through the ids in the positions), the positions
-// and cube keys the current neighbour lists were built from, the density
-// and pressure, the step index that keys the noise, and the membrane
-// reference geometry recorded at set-up.  A restore rebuilds the lists from
-// those positions and keys without re-sorting, which reproduces them entry
-// for entry, so that a restored run continues bit for bit as the original
-// would have (host-driven steps; captured steps rebuild their lists when
-// they are captured).  Layout, little-endian: a 128-byte header, one
-// 16-byte record per system (particles, membrane vertices, seed), then the
-// arrays in the order of ckpt_arrays.
-// ---------------------------------------------------------------------------
-namespace {
-
-struct CkptHeader {
-    char magic[8];
-    uint32_t version, nsys;
-    uint64_t n, ncp, ncell, ntri, nedge;
-    int64_t step;
-    float skin_rel;
-    int32_t K;
-    uint32_t has_sys, has_cells;
-    uint8_t reserved[128 - 8 - 8 - 40 - 8 - 4 - 4 - 8];
-};
-static_assert(sizeof(CkptHeader) == 128, "checkpoint header is 128 bytes");
-
-struct CkptSys {
-    uint32_t n, ncp;
-    uint64_t seed;
-};
-
-struct CkptArray {
-    void* dev;
-    size_t bytes;
-};
-
-std::vector<CkptArray> ckpt_arrays(GcFused* f) {
-    size_t n = f->n;
-    std::vector<CkptArray> v = {
-        {f->a.pos, n * 16}, {f->a.vel, n * 16}, {f->a.vpred, n * 16}, {f->a.vh, n * 16}, {f->a.force, n * 16},
-        {f->a.nthro, n * 16}, {f->refpos, n * 16}, {f->keys, n * 4}, {f->dp, n * 8}};
-    if (f->a.sys) v.push_back({f->a.sys, n * 4});
-    if (f->ncell > 0) {
-        size_t nt = f->ntri, nc = f->ncell, ne = f->nedge;
-        v.push_back({f->reftarea, nt * 4});
-        v.push_back({f->crefarea, nc * 8});
-        v.push_back({f->crefvol, nc * 8});
-        for (float* q : {f->l0, f->lmax, f->perlen, f->hpow, f->hbend, f->refang}) v.push_back({q, ne * 4});
-    }
-    return v;
-}
-
-void ckpt_header(GcFused* f, CkptHeader* h) {
-    memset(h, 0, sizeof(*h));
-    memcpy(h->magic, "GCFCKPT1", 8);
-    h->version = 1;
-    h->nsys = f->nsys;
-    h->n = f->n;
-    h->ncp = f->ncp;
-    h->ncell = f->ncell;
-    h->ntri = f->ntri;
-    h->nedge = f->nedge;
-    h->step = f->step;
-    h->skin_rel = f->skin_rel;
-    h->K = f->K;
-    h->has_sys = f->a.sys ? 1 : 0;
-    h->has_cells = f->ncell > 0 ? 1 : 0;
-}
-
-// The lists exactly as the last rebuild made them: the cube starts from the
-// saved (sorted) keys and the scan over the saved build positions.
-int rebuild_from_ref(GcFused* f) {
-    const int n = f->n, nb = gc_blocks(n, f->block);
-    cudaStream_t st = f->st;
-    fk_iota<<<nb, f->block, 0, st>>>(n, f->vals);
-    GC_CHECK_LAUNCH("restore: identity");
-    GC_TRY(gc_counting_sort_bufs(n, f->K, f->keys, f->vals, f->sb, f->flags, st));
-    float cut = f->p.rc + f->skin;
-    for (int attempt = 0; attempt < 4; ++attempt) {
-        GC_CUDA(cudaMemsetAsync(f->oflag, 0, sizeof(unsigned), st), "restore: flags");
-        fk_build_list<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->refpos, f->sb.cnt, f->nbr, f->cnt, f->cap,
-                                              cut * cut, f->oflag);
-        GC_CHECK_LAUNCH("restore: build lists");
-        GC_CUDA(cudaMemcpyAsync(&f->h->oflag, f->oflag, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "restore");
-        GC_CUDA(cudaStreamSynchronize(st), "restore");
-        if (!(f->h->oflag & GC_FLAG_CELL_OVERFLOW)) return GC_OK;
-        GC_TRY(alloc_list(f, f->cap * 2));
-    }
-    return gc_fail(GC_EDEVICE, "restore: neighbour lists overflow %d entries", f->cap);
-}
-
-}  // namespace
-
-extern "C" int gc_fused_checkpoint(GcFused* f, const char* path) {
-    if (!f || !path) return gc_fail(GC_EINVAL, "checkpoint: NULL argument");
-    if (!f->setup_done) return gc_fail(GC_ESTATE, "checkpoint: call gc_fused_setup first");
-    FILE* fp = fopen(path, "wb");
-    if (!fp) return gc_fail(GC_EINVAL, "checkpoint: cannot open %s for writing", path);
-    CkptHeader h;
-    ckpt_header(f, &h);
-    std::vector<CkptSys> sys(f->nsys);
-    for (int s = 0; s < f->nsys; ++s) {
-        sys[s].n = f->hsys[s].end - f->hsys[s].id0;
-        sys[s].ncp = f->hsys[s].end - f->hsys[s].cs;
-        sys[s].seed = f->hsys[s].seed;
-    }
-    bool ok = fwrite(&h, sizeof(h), 1, fp) == 1 && fwrite(sys.data(), sizeof(CkptSys), sys.size(), fp) == sys.size();
-    std::vector<char> buf;
-    int rc = GC_OK;
-    for (const CkptArray& a : ckpt_arrays(f)) {
-        if (!ok) break;
-        buf.resize(a.bytes);
-        cudaError_t e = cudaMemcpyAsync(buf.data(), a.dev, a.bytes, cudaMemcpyDeviceToHost, f->st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(f->st);
-        if (e != cudaSuccess) {
-            rc = gc_cuda_fail(e, "checkpoint: read state");
-            break;
-        }
-        ok = fwrite(buf.data(), 1, a.bytes, fp) == a.bytes;
-    }
-    if (fclose(fp) != 0) ok = false;
-    if (rc != GC_OK) return rc;
-    if (!ok) return gc_fail(GC_EINVAL, "checkpoint: write to %s failed", path);
-    return GC_OK;
-}
-
-extern "C" int gc_fused_restore(GcFused* f, const char* path) {
-    if (!f || !path) return gc_fail(GC_EINVAL, "restore: NULL argument");
-    if (!f->setup_done) return gc_fail(GC_ESTATE, "restore: set the handle up as for the original run first");
-    FILE* fp = fopen(path, "rb");
-    if (!fp) return gc_fail(GC_EINVAL, "restore: cannot open %s", path);
-    CkptHeader h;
-    int rc = GC_OK;
-    std::vector<CkptSys> sys;
-    if (fread(&h, sizeof(h), 1, fp) != 1 || memcmp(h.magic, "GCFCKPT1", 8) != 0 || h.version != 1) {
-        rc = gc_fail(GC_EINVAL, "restore: %s is not a checkpoint of this library", path);
-    } else if (h.nsys != (uint32_t)f->nsys || h.n != (uint64_t)f->n || h.ncp != (uint64_t)f->ncp ||
-               h.ncell != (uint64_t)f->ncell || h.ntri != (uint64_t)f->ntri || h.nedge != (uint64_t)f->nedge ||
-               h.has_sys != (f->a.sys ? 1u : 0u)) {
-        rc = gc_fail(GC_EINVAL, "restore: the checkpoint holds another configuration (%llu particles in %u systems, "
-                                "%llu cells; this handle: %d in %d, %d)",
-                     (unsigned long long)h.n, h.nsys, (unsigned long long)h.ncell, f->n, f->nsys, f->ncell);
-    } else {
-        sys.resize(h.nsys);
-        if (fread(sys.data(), sizeof(CkptSys), sys.size(), fp) != sys.size()) {
-            rc = gc_fail(GC_EINVAL, "restore: %s is truncated", path);
-        } else {
-            for (int s = 0; s < f->nsys && rc == GC_OK; ++s)
-                if (sys[s].n != f->hsys[s].end - f->hsys[s].id0 || sys[s].ncp != f->hsys[s].end - f->hsys[s].cs ||
-                    sys[s].seed != f->hsys[s].seed)
-                    rc = gc_fail(GC_EINVAL, "restore: system %d differs from the checkpoint's", s);
-        }
-    }
-    if (rc == GC_OK && h.skin_rel != f->skin_rel) {   // the lists were built at the checkpoint's skin
-        f->skin_rel = h.skin_rel;
-        f->skin = f->skin_rel * f->p.rc;
-        rc = build_grids(f);
-    }
-    if (rc == GC_OK && h.K != f->K) rc = gc_fail(GC_EINVAL, "restore: the cube grids differ from the checkpoint's");
-    std::vector<char> buf;
-    for (const CkptArray& a : ckpt_arrays(f)) {
-        if (rc != GC_OK) break;
-        buf.resize(a.bytes);
-        if (fread(buf.data(), 1, a.bytes, fp) != a.bytes) {
-            rc = gc_fail(GC_EINVAL, "restore: %s is truncated", path);
-            break;
-        }
-        cudaError_t e = cudaMemcpyAsync(a.dev, buf.data(), a.bytes, cudaMemcpyHostToDevice, f->st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(f->st);   // the host buffer is reused
-        if (e != cudaSuccess) rc = gc_cuda_fail(e, "restore: write state");
-    }
-    fclose(fp);
-    if (rc != GC_OK) return rc;
-    const int n = f->n;
-    cudaStream_t st = f->st;
-    fk_slot_of<<<gc_blocks(n, 256), 256, 0, st>>>(n, f->a.pos, f->slot_of, f->flags);
-    GC_CHECK_LAUNCH("restore: slots");
-    if (f->ncell > 0) {
-        fk_gather_mpos<<<gc_blocks(f->ncp, 256), 256, 0, st>>>(f->ncp, f->dsys, f->msys, f->slot_of, f->a.pos,
-                                                              f->a.nthro, f->mpos, f->mnthro);
-        GC_CHECK_LAUNCH("restore: membrane positions");
-    }
-    GC_TRY(rebuild_from_ref(f));
-    f->step = h.step;
-    GC_TRY(sync_dstep(f));
-    drop_graphs(f);
-    GcParams p = f->p;
-    GC_TRY(launch_membranes(f, st, p));   // membrane outputs of the restored state
-    GC_CUDA(cudaStreamSynchronize(st), "restore");
-    return GC_OK;
-}
-
-// ---------------------------------------------------------------------------
-// Autotuner: times short runs of candidate settings on the handle's own
-// state and keeps the fastest.  Every trial starts from the same saved state
-// and step index with freshly built lists, and the handle returns to that
-// state afterwards, so tuning does not change the trajectory that follows
-// (beyond the summation order the chosen settings imply).  The search is
-// coordinate-wise: skin (the cube size rc + skin of the list grid and the
-// list length), then threads per block, then per-step compaction of the
-// acting entries, then captured steps.  Choices are cached per size class
-// (ensemble or single system, particle count, density, membranes present,
-// noise) for the life of the process.
-// ---------------------------------------------------------------------------
-namespace {
-
-struct TuneKey {
-    int nsys_class, n_class, dens_class, cells, noise;
-    bool operator<(const TuneKey& o) const {
-        return std::tie(nsys_class, n_class, dens_class, cells, noise) <
-               std::tie(o.nsys_class, o.n_class, o.dens_class, o.cells, o.noise);
-    }
-};
-
-std::mutex g_tune_mutex;
-std::map<TuneKey, GcFusedOptions> g_tune_cache;
-
-TuneKey tune_key(GcFused* f) {
-    double vol = 0.0;
-    for (const SysInfo& S : f->hsys) vol += (double)S.g.L[0] * S.g.L[1] * S.g.L[2];
-    double dens = f->n / (vol > 0 ? vol : 1.0);
-    TuneKey k;
-    k.nsys_class = f->nsys > 1 ? (int)lround(log2((double)f->nsys)) + 1 : 0;
-    k.n_class = (int)lround(4.0 * log2((double)f->n));
-    k.dens_class = (int)lround(8.0 * log2(dens * f->p.rc * f->p.rc * f->p.rc + 1e-30));
-    k.cells = f->ncell > 0;
-    k.noise = f->p.noise_pref > 0.f;
-    return k;
-}
-
-// Milliseconds per step of `steps` steps with the given settings, from the
-// saved state (HUGE_VAL if the settings do not run, e.g. out of memory).
-double trial(GcFused* f, const GcFusedOptions& o, int steps, int drive, cudaEvent_t e0, cudaEvent_t e1) {
-    long long step0 = f->step, steps0 = f->steps, reb0 = f->rebuilds;
-    if (gc_fused_set_options(f, &o) != GC_OK) return HUGE_VAL;
-    if (restore_state(f, &f->tsnap) != GC_OK) return HUGE_VAL;
-    f->step = step0;
-    if (refresh(f) != GC_OK) return HUGE_VAL;
-    if (f->graph && (sync_dstep(f) != GC_OK || prepare_graph(f, drive) != GC_OK)) return HUGE_VAL;
-    if (cudaEventRecord(e0, f->st) != cudaSuccess) return HUGE_VAL;
-    int rc = gc_fused_step(f, steps, drive);
-    cudaEventRecord(e1, f->st);
-    cudaEventSynchronize(e1);
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    f->step = step0;
-    f->steps = steps0;
-    f->rebuilds = reb0;
-    return rc == GC_OK ? ms / steps : HUGE_VAL;
-}
-
-}  // namespace
-
-extern "C" int gc_fused_autotune(GcFused* f, int trial_steps, int drive_on, int flags, GcFusedOptions* chosen,
-                                 double* ms_per_step) {
-    if (!f || !f->setup_done) return gc_fail(GC_ESTATE, "fused_autotune: call gc_fused_setup first");
-    if (trial_steps < 1) trial_steps = 30;
-    int drive = drive_on ? 1 : 0;
-    TuneKey key = tune_key(f);
-    GcFusedOptions best;
-    GC_TRY(gc_fused_get_options(f, &best));
-    best.list_capacity = 0;
-    if (flags & GC_TUNE_CACHE) {
-        std::lock_guard<std::mutex> lock(g_tune_mutex);
-        auto it = g_tune_cache.find(key);
-        if (it != g_tune_cache.end()) {
-            GcFusedOptions o = it->second;
-            int rc = gc_fused_set_options(f, &o);
-            if (rc == GC_OK && chosen) *chosen = o;
-            if (ms_per_step) *ms_per_step = 0.0;
-            return rc;
-        }
-    }
-    bool prof = f->profile;
-    f->profile = false;
-    GC_TRY(save_state(f, &f->tsnap));
-    cudaEvent_t e0, e1;
-    GC_CUDA(cudaEventCreate(&e0), "autotune: events");
-    GC_CUDA(cudaEventCreate(&e1), "autotune: events");
-    double best_ms = trial(f, best, trial_steps, drive, e0, e1);
-    const float skins[] = {0.05f, 0.075f, 0.1f, 0.15f};
-    const int blocks[] = {64, 128, 256};
-    for (float s : skins) {
-        GcFusedOptions o = best;
-        o.skin = s;
-        if (o.skin == best.skin) continue;
-        double ms = trial(f, o, trial_steps, drive, e0, e1);
-        if (ms < best_ms) { best_ms = ms; best = o; }
-    }
-    for (int b : blocks) {
-        GcFusedOptions o = best;
-        o.block = b;
-        if (o.block == best.block) continue;
-        double ms = trial(f, o, trial_steps, drive, e0, e1);
-        if (ms < best_ms) { best_ms = ms; best = o; }
-    }
-    for (int c = 0; c < 2; ++c) {
-        GcFusedOptions o = best;
-        o.compact = c;
-        if (o.compact == best.compact) continue;
-        double ms = trial(f, o, trial_steps, drive, e0, e1);
-        if (ms < best_ms) { best_ms = ms; best = o; }
-    }
-    for (int g = 0; g < 2; ++g) {
-        GcFusedOptions o = best;
-        o.graph = g;
-        if (o.graph == best.graph) continue;
-        double ms = trial(f, o, trial_steps, drive, e0, e1);
-        if (ms < best_ms) { best_ms = ms; best = o; }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    long long step0 = f->step;
-    GC_TRY(gc_fused_set_options(f, &best));
-    GC_TRY(restore_state(f, &f->tsnap));
-    f->step = step0;
-    GC_TRY(sync_dstep(f));
-    GC_TRY(refresh(f));
-    f->profile = prof;
-    {
-        std::lock_guard<std::mutex> lock(g_tune_mutex);
-        g_tune_cache[key] = best;
-    }
-    if (chosen) *chosen = best;
-    if (ms_per_step) *ms_per_step = best_ms;
-    if (!(best_ms < HUGE_VAL)) return gc_fail(GC_EDEVICE, "fused_autotune: no setting ran");
-    return GC_OK;
-}
-
-// ---------------------------------------------------------------------------
-// The fused engine behind the boundary entry points (GPUCELL_ENGINE=fused).
-//
-// GPUCell's host frame owns the state in its own buffers and layout and
-// reads them between steps (src/Particle.cu:693-710).  The engine adopts the
-// state once -- positions, velocities, VelHalf, forces and crossing counts in
-// the caller's slot order, the membrane topology and the reference geometry
-// its set-up calls computed -- then runs each step fused on its own arrays
-// and writes back, at the end of every step, everything the host reads: the
-// particle arrays in the engine's slot order with SortPart and CurPos to
-// match, and the per-cell, per-triangle and per-vertex membrane outputs.
-// ---------------------------------------------------------------------------
-namespace {
-
-__global__ void fk_import_ref(int n, unsigned nC, const int* __restrict__ sortpart, const float* __restrict__ coor,
-                              const float* __restrict__ velrhop, const float* __restrict__ velhalf,
-                              const float* __restrict__ force, const int* __restrict__ nthro, SlotArrays a,
-                              int* __restrict__ slot_of, float4* __restrict__ mpos, int4* __restrict__ mnthro,
-                              unsigned* flags) {
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    int id = sortpart[q];
-    if (id < 0 || id >= n) {
-        raise_flag(flags, GC_FLAG_BAD_INDEX);
-        return;
-    }
-    float4 x = make_float4(coor[3 * q], coor[3 * q + 1], coor[3 * q + 2], __uint_as_float((unsigned)id));
-    a.pos[q] = x;
-    float4 v = make_float4(velrhop[4 * q], velrhop[4 * q + 1], velrhop[4 * q + 2], 0.f);
-    a.vel[q] = v;
-    a.vpred[q] = v;
-    a.vh[q] = make_float4(velhalf[3 * q], velhalf[3 * q + 1], velhalf[3 * q + 2], 0.f);
-    a.force[q] = make_float4(force[3 * q], force[3 * q + 1], force[3 * q + 2], 0.f);
-    int4 t = nthro ? make_int4(nthro[3 * q], nthro[3 * q + 1], nthro[3 * q + 2], 0) : make_int4(0, 0, 0, 0);
-    a.nthro[q] = t;
-    slot_of[id] = q;
-    if ((unsigned)id >= nC && mpos) {
-        mpos[id - nC] = x;
-        mnthro[id - nC] = t;
-    }
-}
-
-__global__ void fk_export_ref(int n, GcParams p, SlotArrays a, const float2* __restrict__ dp, int* __restrict__ sortpart,
-                              int* __restrict__ curpos, float* __restrict__ coor, float* __restrict__ velrhop,
-                              float* __restrict__ velhalf, float* __restrict__ force, float* __restrict__ press,
-                              int* __restrict__ nthro) {
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    float4 x = a.pos[q];
-    unsigned id = fid(x);
-    sortpart[q] = (int)id;
-    if (curpos) curpos[id] = q;
-    coor[3 * q] = x.x; coor[3 * q + 1] = x.y; coor[3 * q + 2] = x.z;
-    float4 v = a.vel[q];
-    float2 d = dp[q];
-    velrhop[4 * q] = v.x; velrhop[4 * q + 1] = v.y; velrhop[4 * q + 2] = v.z; velrhop[4 * q + 3] = p.mass / d.x;
-    float4 h = a.vh[q];
-    velhalf[3 * q] = h.x; velhalf[3 * q + 1] = h.y; velhalf[3 * q + 2] = h.z;
-    float4 f = a.force[q];
-    force[3 * q] = f.x; force[3 * q + 1] = f.y; force[3 * q + 2] = f.z;
-    if (press) press[q] = d.y / (d.x * d.x);
-    if (nthro) {
-        int4 t = a.nthro[q];
-        nthro[3 * q] = t.x; nthro[3 * q + 1] = t.y; nthro[3 * q + 2] = t.z;
-    }
-}
-
-// one block per cell: cell values and their per-triangle copies
-__global__ void fk_export_cells_ref(int ncell, int ntri, const int2* __restrict__ betri, const double* __restrict__ carea,
-                                    const double* __restrict__ cvol, const float* __restrict__ tarea,
-                                    const float4* __restrict__ tnorm, const float4* __restrict__ tcen,
-                                    float* __restrict__ area, float* __restrict__ vol, float* __restrict__ area_para,
-                                    float* __restrict__ vol_para, float* __restrict__ triarea,
-                                    float* __restrict__ trinordir, float* __restrict__ tricenter) {
-    int c = blockIdx.x;
-    int2 be = betri[c];
-    if (be.x < 0 || be.y >= ntri || be.y < be.x) return;
-    float A = (float)carea[c], V = (float)cvol[c];
-    if (threadIdx.x == 0) {
-        if (area) area[c] = A;
-        if (vol) vol[c] = V;
-    }
-    for (int t = be.x + threadIdx.x; t <= be.y; t += blockDim.x) {
-        if (area_para) area_para[t] = A;
-        if (vol_para) vol_para[t] = V;
-        if (triarea) triarea[t] = tarea[t];
-        float4 nrm = tnorm[t], cen = tcen[t];
-        if (trinordir) { trinordir[3 * t] = nrm.x; trinordir[3 * t + 1] = nrm.y; trinordir[3 * t + 2] = nrm.z; }
-        if (tricenter) { tricenter[3 * t] = cen.x; tricenter[3 * t + 1] = cen.y; tricenter[3 * t + 2] = cen.z; }
-    }
-}
-
-__global__ void fk_import_cellrefs(int ncell, int ntri, const int2* __restrict__ betri,
-                                   const float* __restrict__ refarea_para, const float* __restrict__ refvol_para,
-                                   double* __restrict__ crefarea, double* __restrict__ crefvol) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    int t = betri[c].x;
-    if (t < 0 || t >= ntri) return;
-    crefarea[c] = (double)refarea_para[t];
-    crefvol[c] = (double)refvol_para[t];
-}
-
-// Adopts the membrane topology, moduli and set-up geometry from the caller's
-// device buffers.
-int engine_cells(GcFused* f, const GcRefPtrs& r) {
-    int ncell = r.ncell, ntri = r.ntri, nedge = r.nedge, ncp = (int)f->p.nCP;
-    if (ncell <= 0) return GC_OK;
-    if (!r.tri || !r.betri || !r.edge || !r.celltab || !r.hlarea || !r.hgarea || !r.hvol || !r.refedgelen ||
-        !r.maxrefedgelen || !r.perlen || !r.hpow || !r.hbending || !r.reftriangle || !r.reftriarea ||
-        !r.refarea_para || !r.refvol_para)
-        return gc_fail(GC_ESTATE, "fused engine: a membrane buffer of the set-up calls was not seen");
-    GC_TRY(alloc_cells(f, ncell, ntri, nedge, ncp));
-    f->cells_adopted = true;
-    cudaStream_t st = f->st;
-    auto d2d = [&](void* dst, const void* src, size_t bytes) -> int {
-        if (!src) return GC_OK;
-        GC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st), "fused engine: adopt cells");
-        return GC_OK;
-    };
-    GC_TRY(d2d(f->tri, r.tri, (size_t)ntri * 12));
-    GC_TRY(d2d(f->edge, r.edge, (size_t)nedge * 24));
-    GC_TRY(d2d(f->betri, r.betri, (size_t)ncell * 8));
-    GC_TRY(d2d(f->celltab, r.celltab, (size_t)ncp * 4));
-    GC_TRY(d2d(f->shear, r.shearmod, (size_t)nedge * 4));
-    GC_TRY(d2d(f->bend, r.bendmod, (size_t)nedge * 4));
-    GC_TRY(d2d(f->hl, r.hlarea, (size_t)ntri * 4));
-    GC_TRY(d2d(f->hg, r.hgarea, (size_t)ntri * 4));
-    GC_TRY(d2d(f->hv, r.hvol, (size_t)ntri * 4));
-    GC_TRY(d2d(f->l0, r.refedgelen, (size_t)nedge * 4));
-    GC_TRY(d2d(f->lmax, r.maxrefedgelen, (size_t)nedge * 4));
-    GC_TRY(d2d(f->perlen, r.perlen, (size_t)nedge * 4));
-    GC_TRY(d2d(f->hpow, r.hpow, (size_t)nedge * 4));
-    GC_TRY(d2d(f->hbend, r.hbending, (size_t)nedge * 4));
-    GC_TRY(d2d(f->refang, r.reftriangle, (size_t)nedge * 4));
-    GC_TRY(d2d(f->reftarea, r.reftriarea, (size_t)ntri * 4));
-    fk_import_cellrefs<<<gc_blocks(ncell, 128), 128, 0, st>>>(ncell, ntri, f->betri, r.refarea_para, r.refvol_para,
-                                                            f->crefarea, f->crefvol);
-    GC_CHECK_LAUNCH("fused engine: reference areas and volumes");
-    std::vector<int> htri(3 * (size_t)ntri), hedge(6 * (size_t)nedge);
-    GC_CUDA(cudaMemcpyAsync(htri.data(), f->tri, htri.size() * 4, cudaMemcpyDeviceToHost, st), "fused engine: topology");
-    GC_CUDA(cudaMemcpyAsync(hedge.data(), f->edge, hedge.size() * 4, cudaMemcpyDeviceToHost, st), "fused engine: topology");
-    GC_CUDA(cudaStreamSynchronize(st), "fused engine: topology");
-    GC_TRY(build_incidence(f, htri.data(), hedge.data()));
-    return build_grids(f);   // aggregation grid
-}
-
-int engine_start(GcState& s) {
-    const GcRefPtrs& r = s.ref;
-    if (!r.sortpart || !r.coor || !r.velrhop || !r.velhalf || !r.force || !r.bbox)
-        return gc_fail(GC_ESTATE, "fused engine: the first step did not show every particle buffer");
-    float bb[6];
-    GC_CUDA(cudaMemcpyAsync(bb, r.bbox, sizeof(bb), cudaMemcpyDeviceToHost, s.stream), "fused engine: bbox");
-    GC_CUDA(cudaStreamSynchronize(s.stream), "fused engine: bbox");
-    GcFused* f = nullptr;
-    GcFusedOptions opt;
-    memset(&opt, 0, sizeof(opt));
-    opt.compact = 1;
-    GC_TRY(gc_fused_create(&s.c, bb, s.periodic_mask, s.noise_on, &opt, &f));
-    int rc = engine_cells(f, r);
-    if (rc == GC_OK) {
-        fk_import_ref<<<gc_blocks(f->n, f->block), f->block, 0, f->st>>>(
-            f->n, f->p.nC, r.sortpart, r.coor, r.velrhop, r.velhalf, r.force, r.nthro, f->a, f->slot_of,
-            f->ncell > 0 ? f->mpos : nullptr, f->mnthro, f->flags);
-        cudaError_t e = cudaGetLastError();
-        gc_count_launch();
-        if (e != cudaSuccess) rc = gc_cuda_fail(e, "fused engine: adopt state");
-    }
-    if (rc == GC_OK) rc = rebuild_lists(f);
-    if (rc != GC_OK) {
-        gc_fused_destroy(f);
-        return rc;
-    }
-    for (int k = 0; k < f->nsys; ++k) f->sys_loaded[k] = 1;
-    f->setup_done = true;
-    s.engine = f;
-    return GC_OK;
-}
-
-int engine_export(GcFused* f, const GcRefPtrs& r) {
-    cudaStream_t st = f->st;
-    fk_export_ref<<<gc_blocks(f->n, f->block), f->block, 0, st>>>(f->n, f->p, f->a, f->dp, r.sortpart, r.curpos,
-                                                                 r.coor, r.velrhop, r.velhalf, r.force, r.press,
-                                                                 r.nthro);
-    GC_CHECK_LAUNCH("fused engine: write back particles");
-    if (f->ncell > 0) {
-        fk_export_cells_ref<<<f->ncell, 256, 0, st>>>(f->ncell, f->ntri, f->betri, f->carea, f->cvol, f->tarea,
-                                                     f->tnorm, f->tcen, r.area, r.vol, r.area_para, r.vol_para,
-                                                     r.triarea, r.trinordir, r.tricenter);
-        GC_CHECK_LAUNCH("fused engine: write back cells");
-        int m = f->ncp;
-        fk_store_cells<<<gc_blocks(m, 128), 128, 0, st>>>(m, 0, 0, 0, f->mforce, f->magg, f->parea, f->tnorm, f->tcen,
-                                                         r.defforce, r.aggforce, r.pararea, nullptr, nullptr,
-                                                         f->have_agg ? 1 : 0);
-        GC_CHECK_LAUNCH("fused engine: write back membrane forces");
-    }
-    return GC_OK;
-}
-
-}  // namespace
-
-int gc_engine_step(int drive_on) {
-    GcState& s = gc_state();
-    if (!s.engine) GC_TRY(engine_start(s));
-    GcFused* f = s.engine;
-    f->step = s.step - 1;   // one_step advances it to the step index of this UpdatePar
-    GC_TRY(one_step(f, drive_on));
-    return engine_export(f, s.ref);
-}
-
-void gc_engine_reset() {
-    GcState& s = gc_state();
-    if (s.engine) gc_fused_destroy(s.engine);
-    s.engine = nullptr;
-}

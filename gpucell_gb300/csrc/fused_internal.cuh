@@ -1,0 +1,243 @@
+// fused_internal.cuh -- what the translation units of the fused step share:
+// the per-system table, the slot arrays, the handle (GcFused), a few device
+// helpers, and the host functions and kernels that more than one of
+// fused.cu (state, passes, steps, API), fused_ckpt.cu (checkpoint and
+// restart), fused_tune.cu (autotuner), fused_report.cu (per-cell statistics,
+// diagnostics, output files) and fused_engine.cu (the engine behind the
+// boundary entry points) use.
+#pragma once
+
+#include "gc_internal.cuh"
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+namespace gcf {
+
+constexpr int kBS = 128;      // default threads per block
+constexpr int kMaxBS = 256;   // largest block the particle kernels accept
+
+__device__ __forceinline__ unsigned fid(float4 x) { return __float_as_uint(x.w); }
+__device__ __forceinline__ float3 xyz(float4 a) { return f3(a.x, a.y, a.z); }
+
+__device__ __forceinline__ size_t sell(int i, int k, int cap) {
+    return ((size_t)(i >> 5) * cap + k) * 32 + (i & 31);
+}
+
+__device__ __forceinline__ size_t mrow(int i, int w, int mw) {
+    return ((size_t)(i >> 5) * mw + w) * 32 + (i & 31);
+}
+
+__device__ __forceinline__ double block_sum_d(double v, double* sh) {
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) sh[0] = t;
+    }
+    __syncthreads();
+    double t = sh[0];
+    __syncthreads();
+    return t;
+}
+
+// One system of an ensemble: global id ranges, grids, body force, seed.
+struct SysInfo {
+    uint64_t seed;                   // iSeed of the system (pair noise)
+    unsigned id0, b2, fl, cs, end;   // first id; first Bound2, fluid and membrane id; one past the last
+    unsigned m0;                     // first membrane index (membrane-ordered arrays)
+    int cube0;                       // first global cube of the list grid
+    int mcube0;                      // first global cube of the aggregation grid
+    float gx;                        // body force in x (ConstExtForce)
+    float invL[3];
+    int lr;                          // list-grid stencil radius: 2 for cells >= (rc + skin)/2, 1 for cubes >= rc + skin
+    GcGrid g;                        // list grid over the box
+    GcGrid mg;                       // aggregation grid: cubes at least MaxCut wide
+};
+
+struct SlotArrays {
+    float4 *pos, *vel, *vpred, *vh, *force;
+    int4* nthro;
+    int* sys;   // system of each slot (nullptr for one system)
+};
+
+// Membrane topology of one system as given (local, 1-based), until set-up.
+struct HostCells {
+    bool set = false;
+    int ncell = 0, ntri = 0, nedge = 0;
+    std::vector<int> tri, edge, betri, celltab;
+    std::vector<int> verts;   // first and last vertex of each cell (0-based), from its triangles
+    std::vector<float> shear, bend, hl, hg, hv;
+};
+
+// Device copy of the dynamic state (snapshots for captured steps and the
+// autotuner).
+struct StateCopy {
+    SlotArrays s{};
+    float4* mpos = nullptr;
+    int4* mnthro = nullptr;
+    long long* dstep = nullptr;
+    bool have = false;
+};
+
+
+}  // namespace gcf
+
+struct GcFused {
+    GcParams p;
+    int nsys = 1;
+    std::vector<gcf::SysInfo> hsys;
+    std::vector<GcSystemDesc> desc;
+    std::vector<gcf::HostCells> hcells;
+    std::vector<int> c0, t0;       // first cell and triangle of each system (after set-up)
+    std::vector<char> sys_loaded;
+    gcf::SysInfo* dsys = nullptr;
+    int K = 0, Kagg = 0;           // cubes of all list grids, of all aggregation grids
+    float skin_rel = 0.1f;         // skin in units of CutRadius
+    float skin = 0.1f;             // skin length
+    int n = 0, cap = 0, block = gcf::kBS;
+    int noise_on = 1;
+    bool compact = false;
+    bool graph = false;            // steps run as captured graphs
+    bool ens = false;              // kernels read the system table
+    long long step = -1;           // index keying the noise of the latest step
+    long long rebuilds = 0, steps = 0;
+    cudaStream_t st = 0;
+    // slot arrays (current, and the permutation target)
+    gcf::SlotArrays a{}, b{};
+    float4* refpos = nullptr;
+    float2* dp = nullptr;
+    int* slot_of = nullptr;
+    int *keys = nullptr, *vals = nullptr;
+    int *nbr = nullptr, *cnt = nullptr;
+    size_t nbr_elems = 0;
+    unsigned* cmask = nullptr;   // per-step bit mask of the acting list entries
+    size_t cmask_elems = 0;
+    int* ccnt = nullptr;         // number of acting entries
+    int mw = 0;                  // mask words per slot
+    int* rebuild = nullptr;
+    unsigned* flags = nullptr;
+    unsigned* oflag = nullptr;   // list overflow inside captured steps
+    unsigned long long* stat_sum = nullptr;
+    int* stat_max = nullptr;
+    long long* dstep = nullptr;  // device step counter (ensembles, captured steps)
+    unsigned* nkey = nullptr;    // per-system noise key of the current step
+    unsigned long long* drebuilds = nullptr;   // rebuilds inside captured steps
+    // pinned words read back after steps: rebuild flag, overflow flag, device rebuild count
+    struct Pinned {
+        int rebuild;
+        unsigned oflag;
+        unsigned long long drebuilds;
+    }* h = nullptr;
+    unsigned long long drebuilds_seen = 0;
+    // counting-sort temporaries (owned, so a captured step can use them)
+    void* sortmem = nullptr;
+    size_t sortmem_bytes = 0;
+    int sort_n = 0, sort_K = 0;
+    GcSortBufs sb{};
+    void* sortmem_agg = nullptr;   // the aggregation sort's own temporaries: it runs beside the list rebuild
+    int sort_agg_n = 0, sort_agg_K = 0;
+    GcSortBufs sb_agg{};
+    // The membrane kernels depend only on the integrated membrane positions:
+    // they run on their own stream from the end of the integration to the
+    // force pass, beside the rebuild check, the list rebuild and the density.
+    cudaStream_t mst = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // membranes (global indices over the ensemble)
+    int ncell = 0, ntri = 0, nedge = 0, ncp = 0;
+    int3* tri = nullptr;
+    int6* edge = nullptr;
+    int2* betri = nullptr;
+    int* celltab = nullptr;
+    int *msys = nullptr, *cellsys = nullptr;
+    float *shear = nullptr, *bend = nullptr, *hl = nullptr, *hg = nullptr, *hv = nullptr;
+    float *l0 = nullptr, *lmax = nullptr, *perlen = nullptr, *hpow = nullptr, *hbend = nullptr, *refang = nullptr;
+    float *tarea = nullptr, *reftarea = nullptr;
+    float4 *tnorm = nullptr, *tcen = nullptr;
+    double *carea = nullptr, *cvol = nullptr, *crefarea = nullptr, *crefvol = nullptr;
+    float4 *mpos = nullptr, *mforce = nullptr, *magg = nullptr;
+    int4* mnthro = nullptr;
+    float* parea = nullptr;
+    int *mkeys = nullptr, *mvals = nullptr;
+    float4* mparts = nullptr;    // per-edge and per-triangle vertex forces (4 per edge, then 3 per triangle)
+    int *inc_ptr = nullptr, *inc = nullptr;   // vertex -> its parts (CSR)
+    int2* cell_verts = nullptr;  // first and last membrane vertex of each cell (global, inclusive)
+    double* cell_stats = nullptr;   // ncell x 12, see gc_ensemble_cell_stats
+    double* diag = nullptr;         // diagnostics partial sums and result
+    bool cells_adopted = false;   // membranes taken from the boundary entry points' buffers
+    bool have_agg = false;
+    bool setup_done = false;
+    // captured steps
+    cudaStream_t gst = nullptr, gst2 = nullptr, gst3 = nullptr;
+    cudaGraph_t cg[2] = {};
+    cudaGraphExec_t gexec[2] = {};
+    bool graph_dirty = true;
+    long long kernels_step = 0, kernels_rebuild = 0;   // kernels per captured step and per rebuild body
+    gcf::StateCopy snap;    // state at the start of a captured gc_fused_step call
+    gcf::StateCopy tsnap;   // state at the start of an autotune
+    // optional CUDA-event timing of the dominant kernels (fk_density, fk_force)
+    bool profile = false;
+    std::vector<cudaEvent_t> ev;   // pairs: density start/stop, force start/stop
+    size_t ev_used = 0;
+    // staging for host pointers
+    void* stage = nullptr;
+    size_t stage_bytes = 0;
+    std::vector<void*> allocs;
+};
+
+namespace gcf {
+
+template <class T>
+int falloc(GcFused* f, T** p, size_t count) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, (count ? count : 1) * sizeof(T));
+    if (e != cudaSuccess) return gc_fail(GC_ENOMEM, "fused: cudaMalloc(%zu) failed: %s", count * sizeof(T),
+                                         cudaGetErrorString(e));
+    f->allocs.push_back(q);
+    *p = (T*)q;
+    return GC_OK;
+}
+
+int stage_bytes(GcFused* f, size_t bytes);
+void drop_graphs(GcFused* f);
+int alloc_list(GcFused* f, int cap);
+int build_grids(GcFused* f);
+int sync_dstep(GcFused* f);
+int rebuild_lists(GcFused* f);
+int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p);
+int one_step(GcFused* f, int drive);
+int prepare_graph(GcFused* f, int drive);
+int save_state(GcFused* f, StateCopy* c);
+int restore_state(GcFused* f, StateCopy* c);
+int refresh(GcFused* f);
+int alloc_cells(GcFused* f, int ncell, int ntri, int nedge, int ncp);
+int build_incidence(GcFused* f, const int* tri, const int* edge);
+int check_sys(GcFused* f, int sys, const char* what);
+int store_range(GcFused* f, unsigned id_base, int count, float* pos, float* vel, float* rho, float* press,
+                float* force, float* velhalf, int* nthro, int to_device);
+int store_cells_range(GcFused* f, int c0, int nc, int m0, int nv, int t0, int nt, float* area, float* vol,
+                      float* defforce, float* aggforce, float* trinordir, float* tricenter, float* pararea,
+                      int to_device);
+
+__global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, const SysInfo* __restrict__ sys,
+                                                     const int* __restrict__ sysid, const float4* __restrict__ pos,
+                                                     const unsigned* __restrict__ start, int* __restrict__ nbr,
+                                                     int* __restrict__ cnt, int cap, float cut2, unsigned* flags);
+
+__global__ void fk_gather_mpos(int ncp, const SysInfo* __restrict__ sys, const int* __restrict__ msys,
+                               const int* __restrict__ slot_of, const float4* __restrict__ pos,
+                               const int4* __restrict__ nthro, float4* __restrict__ mpos, int4* __restrict__ mnthro);
+
+__global__ void fk_store_cells(int ncp, int m0, int ntri, int t0, const float4* __restrict__ mforce,
+                               const float4* __restrict__ magg, const float* __restrict__ parea,
+                               const float4* __restrict__ tnorm, const float4* __restrict__ tcen,
+                               float* __restrict__ defforce, float* __restrict__ aggforce, float* __restrict__ pararea,
+                               float* __restrict__ trinor, float* __restrict__ tricen, int have_agg);
+
+}  // namespace gcf
