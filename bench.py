@@ -344,7 +344,7 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "fp32 (fp64 membrane area/volume sums)",
+        "dtype": "fp32 pair physics; double-float (fp32 pair) positions; fp64 membrane area/volume sums",
         "data": "synthetic (seeded generator, no dataset)",
         "variant": "fused step: Verlet lists with skin, fused passes (gc_fused_*)",
         "config": dict(wdesc, particles=n, membrane_vertices=cfg.ncp, triangles=cfg.ntri, edges=cfg.nedge,

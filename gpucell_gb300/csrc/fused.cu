@@ -157,9 +157,9 @@ template <bool ENS>
 __global__ void fk_integrate(int n, GcParams p, SysInfo s0, const SysInfo* __restrict__ sys,
                              const int* __restrict__ sysid, float4* __restrict__ pos, const float4* __restrict__ vel,
                              float4* __restrict__ vh, float4* __restrict__ vpred, const float4* __restrict__ force,
-                             const float4* __restrict__ refpos, int4* __restrict__ nthro, float half_skin2,
-                             int* __restrict__ rebuild, float4* __restrict__ mpos, int4* __restrict__ mnthro,
-                             unsigned* flags) {
+                             float4* __restrict__ plo, const float4* __restrict__ refpos, int4* __restrict__ nthro,
+                             float half_skin2, int* __restrict__ rebuild, float4* __restrict__ mpos,
+                             int4* __restrict__ mnthro, unsigned* flags) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool far = false;
     if (i < n) {
@@ -169,24 +169,27 @@ __global__ void fk_integrate(int n, GcParams p, SysInfo s0, const SysInfo* __res
         if (id >= S.fl) {
             float4 v = vel[i], f = force[i];
             float h = 0.5f * p.dt * p.dt * p.inv_mass;
-            x.x += p.dt * v.x + h * f.x;
-            x.y += p.dt * v.y + h * f.y;
-            x.z += p.dt * v.z + h * f.z;
+            // the displacement in FP32, added to the double-float position
+            float4 lo = plo[i];
+            dd_add(x.x, lo.x, p.dt * v.x + h * f.x);
+            dd_add(x.y, lo.y, p.dt * v.y + h * f.y);
+            dd_add(x.z, lo.z, p.dt * v.z + h * f.z);
             if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) raise_flag(flags, GC_FLAG_NONFINITE);
             int4 t = nthro[i];
             bool crossed = false;
             float* xs[3] = {&x.x, &x.y, &x.z};
+            float* ls[3] = {&lo.x, &lo.y, &lo.z};
             int* ts[3] = {&t.x, &t.y, &t.z};
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 if (!(S.g.pmask & (1 << a))) continue;
                 float c = *xs[a];
-                if (c >= S.g.hi[a]) { c -= S.g.L[a]; *ts[a] += 1; crossed = true; }
-                else if (c < S.g.lo[a]) { c += S.g.L[a]; *ts[a] -= 1; crossed = true; }
-                *xs[a] = c;
+                if (c >= S.g.hi[a]) { dd_add(*xs[a], *ls[a], -S.g.L[a]); *ts[a] += 1; crossed = true; }
+                else if (c < S.g.lo[a]) { dd_add(*xs[a], *ls[a], S.g.L[a]); *ts[a] -= 1; crossed = true; }
             }
             if (crossed) nthro[i] = t;
             pos[i] = x;
+            plo[i] = lo;
             float hs = 0.5f * p.dt * p.inv_mass, l = p.lambda * p.dt * p.inv_mass;
             float4 w = vh[i];
             vh[i] = make_float4(v.x + hs * f.x, v.y + hs * f.y, v.z + hs * f.z, w.w);
@@ -227,9 +230,10 @@ __global__ void fk_permute(int n, const SysInfo* __restrict__ sys, const int* __
     int o = perm[q];
     int s = src.sys ? src.sys[o] : 0;
     const GcGrid& g = sys[s].g;
-    float4 x = src.pos[o];
+    float4 x = src.pos[o], lo = src.plo[o];
     int4 t = src.nthro[o];
     float* xs[3] = {&x.x, &x.y, &x.z};
+    float* ls[3] = {&lo.x, &lo.y, &lo.z};
     int* ts[3] = {&t.x, &t.y, &t.z};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -238,14 +242,14 @@ __global__ void fk_permute(int n, const SysInfo* __restrict__ sys, const int* __
         if (!isfinite(c)) continue;
         int w = (int)floorf((c - g.lo[a]) / g.L[a]);
         if (w != 0) {
-            c -= (float)w * g.L[a];
-            if (c >= g.hi[a]) { c -= g.L[a]; ++w; }
-            else if (c < g.lo[a]) { c += g.L[a]; --w; }
-            *xs[a] = c;
+            dd_add(*xs[a], *ls[a], -(float)w * g.L[a]);
+            if (*xs[a] >= g.hi[a]) { dd_add(*xs[a], *ls[a], -g.L[a]); ++w; }
+            else if (*xs[a] < g.lo[a]) { dd_add(*xs[a], *ls[a], g.L[a]); --w; }
             *ts[a] += w;
         }
     }
     dst.pos[q] = x;
+    dst.plo[q] = lo;
     dst.vel[q] = src.vel[o];
     dst.vpred[q] = src.vpred[o];
     dst.vh[q] = src.vh[o];
@@ -262,6 +266,7 @@ __global__ void fk_copy_slots(int n, SlotArrays src, SlotArrays dst) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     dst.pos[q] = src.pos[q];
+    dst.plo[q] = src.plo[q];
     dst.vel[q] = src.vel[q];
     dst.vpred[q] = src.vpred[q];
     dst.vh[q] = src.vh[q];
@@ -969,9 +974,9 @@ __global__ void fk_magg(int ncp, GcParams p, const SysInfo* __restrict__ sys, co
 __global__ void fk_load(int count, unsigned id_base, const SysInfo* __restrict__ sys, int nsys, int keep,
                         const float* __restrict__ x, const float* __restrict__ v, const float* __restrict__ vhalf,
                         const float* __restrict__ f, const int* __restrict__ nt, int* __restrict__ slot_of,
-                        float4* __restrict__ pos, float4* __restrict__ vel, float4* __restrict__ vh,
-                        float4* __restrict__ force, int4* __restrict__ nthro, float4* __restrict__ mpos,
-                        int4* __restrict__ mnthro) {
+                        float4* __restrict__ pos, float4* __restrict__ plo, float4* __restrict__ vel,
+                        float4* __restrict__ vh, float4* __restrict__ force, int4* __restrict__ nthro,
+                        float4* __restrict__ mpos, int4* __restrict__ mnthro) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count) return;
     unsigned id = id_base + k;
@@ -985,6 +990,7 @@ __global__ void fk_load(int count, unsigned id_base, const SysInfo* __restrict__
     float4 a = make_float4(x[3 * k], x[3 * k + 1], x[3 * k + 2], __uint_as_float(id));
     pos[i] = a;
     float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    plo[i] = z;   // an FP32 position is exact: no low part
     if (v) vel[i] = make_float4(v[3 * k], v[3 * k + 1], v[3 * k + 2], 0.f);
     else if (!keep) vel[i] = z;
     if (vhalf) vh[i] = make_float4(vhalf[3 * k], vhalf[3 * k + 1], vhalf[3 * k + 2], 0.f);
@@ -1282,12 +1288,12 @@ int launch_integrate(GcFused* f, cudaStream_t st, const GcParams& p) {
     float hs = 0.5f * f->skin * 0.99f;
     if (f->ens)
         fk_integrate<true><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vel, f->a.vh,
-                                                     f->a.vpred, f->a.force, f->refpos, f->a.nthro, hs * hs,
-                                                     f->rebuild, f->mpos, f->mnthro, f->flags);
+                                                     f->a.vpred, f->a.force, f->a.plo, f->refpos, f->a.nthro,
+                                                     hs * hs, f->rebuild, f->mpos, f->mnthro, f->flags);
     else
         fk_integrate<false><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vel, f->a.vh,
-                                                      f->a.vpred, f->a.force, f->refpos, f->a.nthro, hs * hs,
-                                                      f->rebuild, f->mpos, f->mnthro, f->flags);
+                                                      f->a.vpred, f->a.force, f->a.plo, f->refpos, f->a.nthro,
+                                                      hs * hs, f->rebuild, f->mpos, f->mnthro, f->flags);
     GC_CHECK_LAUNCH("fused: integrate");
     return GC_OK;
 }
@@ -1527,6 +1533,7 @@ int alloc_copy(GcFused* f, StateCopy* c) {
     if (c->have) return GC_OK;
     size_t n = f->n;
     GC_TRY(falloc(f, &c->s.pos, n));
+    GC_TRY(falloc(f, &c->s.plo, n));
     GC_TRY(falloc(f, &c->s.vel, n));
     GC_TRY(falloc(f, &c->s.vpred, n));
     GC_TRY(falloc(f, &c->s.vh, n));
@@ -1552,6 +1559,7 @@ int copy_state(GcFused* f, const SlotArrays& src, const float4* mpos, const int4
         return GC_OK;
     };
     GC_TRY(cp(dst.pos, src.pos, n * 16));
+    GC_TRY(cp(dst.plo, src.plo, n * 16));
     GC_TRY(cp(dst.vel, src.vel, n * 16));
     GC_TRY(cp(dst.vpred, src.vpred, n * 16));
     GC_TRY(cp(dst.vh, src.vh, n * 16));
@@ -1847,9 +1855,9 @@ int load_range(GcFused* f, unsigned id_base, int count, const float* pos, const 
     }
     int keep = f->setup_done ? 1 : 0;
     fk_load<<<gc_blocks(count, f->block), f->block, 0, st>>>(count, id_base, f->dsys, f->nsys, keep, dx, dv, dh, df,
-                                                             dn, f->slot_of, f->a.pos, f->a.vel, f->a.vh, f->a.force,
-                                                             f->a.nthro, keep && f->ncell > 0 ? f->mpos : nullptr,
-                                                             f->mnthro);
+                                                             dn, f->slot_of, f->a.pos, f->a.plo, f->a.vel, f->a.vh,
+                                                             f->a.force, f->a.nthro,
+                                                             keep && f->ncell > 0 ? f->mpos : nullptr, f->mnthro);
     GC_CHECK_LAUNCH("fused: load");
     if (!from_device) GC_CUDA(cudaStreamSynchronize(st), "fused_load");   // the staging buffer is reused
     return GC_OK;
@@ -2000,6 +2008,7 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
     SlotArrays* sa[2] = {&f->a, &f->b};
     for (SlotArrays* s : sa) {
         if (ok == GC_OK) ok = falloc(f, &s->pos, (size_t)n + 1);   // slot n: the list padding sentinel
+        if (ok == GC_OK) ok = falloc(f, &s->plo, n);
         if (ok == GC_OK) ok = falloc(f, &s->vel, n);
         if (ok == GC_OK) ok = falloc(f, &s->vpred, n);
         if (ok == GC_OK) ok = falloc(f, &s->vh, n);

@@ -74,7 +74,7 @@ struct CkptArray {
 std::vector<CkptArray> ckpt_arrays(GcFused* f) {
     size_t n = f->n;
     std::vector<CkptArray> v = {
-        {f->a.pos, n * 16}, {f->a.vel, n * 16}, {f->a.vpred, n * 16}, {f->a.vh, n * 16}, {f->a.force, n * 16},
+        {f->a.pos, n * 16}, {f->a.plo, n * 16}, {f->a.vel, n * 16}, {f->a.vpred, n * 16}, {f->a.vh, n * 16}, {f->a.force, n * 16},
         {f->a.nthro, n * 16}, {f->refpos, n * 16}, {f->keys, n * 4}, {f->dp, n * 8}};
     if (f->a.sys) v.push_back({f->a.sys, n * 4});
     if (f->ncell > 0) {
@@ -89,8 +89,8 @@ std::vector<CkptArray> ckpt_arrays(GcFused* f) {
 
 void ckpt_header(GcFused* f, CkptHeader* h) {
     memset(h, 0, sizeof(*h));
-    memcpy(h->magic, "GCFCKPT1", 8);
-    h->version = 1;
+    memcpy(h->magic, "GCFCKPT2", 8);
+    h->version = 2;
     h->nsys = f->nsys;
     h->n = f->n;
     h->ncp = f->ncp;
@@ -169,7 +169,7 @@ extern "C" int gc_fused_restore(GcFused* f, const char* path) {
     CkptHeader h;
     int rc = GC_OK;
     std::vector<CkptSys> sys;
-    if (fread(&h, sizeof(h), 1, fp) != 1 || memcmp(h.magic, "GCFCKPT1", 8) != 0 || h.version != 1) {
+    if (fread(&h, sizeof(h), 1, fp) != 1 || memcmp(h.magic, "GCFCKPT2", 8) != 0 || h.version != 2) {
         rc = gc_fail(GC_EINVAL, "restore: %s is not a checkpoint of this library", path);
     } else if (h.nsys != (uint32_t)f->nsys || h.n != (uint64_t)f->n || h.ncp != (uint64_t)f->ncp ||
                h.ncell != (uint64_t)f->ncell || h.ntri != (uint64_t)f->ntri || h.nedge != (uint64_t)f->nedge ||

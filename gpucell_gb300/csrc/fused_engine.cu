@@ -43,6 +43,7 @@ __global__ void fk_import_ref(int n, unsigned nC, const int* __restrict__ sortpa
     }
     float4 x = make_float4(coor[3 * q], coor[3 * q + 1], coor[3 * q + 2], __uint_as_float((unsigned)id));
     a.pos[q] = x;
+    a.plo[q] = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 v = make_float4(velrhop[4 * q], velrhop[4 * q + 1], velrhop[4 * q + 2], 0.f);
     a.vel[q] = v;
     a.vpred[q] = v;

@@ -29,6 +29,18 @@ __device__ __forceinline__ size_t mrow(int i, int w, int mw) {
     return ((size_t)(i >> 5) * mw + w) * 32 + (i & 31);
 }
 
+// (hi, lo) += d for a double-float number: Knuth's TwoSum of hi + d, its
+// rounding error folded into lo, renormalised by Dekker's Fast2Sum.  The
+// _rn intrinsics keep the compiler from contracting or reordering them.
+__device__ __forceinline__ void dd_add(float& hi, float& lo, float d) {
+    float s = __fadd_rn(hi, d);
+    float bb = __fsub_rn(s, hi);
+    float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(d, bb));
+    float t = __fadd_rn(lo, e);
+    hi = __fadd_rn(s, t);
+    lo = __fsub_rn(t, __fsub_rn(hi, s));
+}
+
 __device__ __forceinline__ double block_sum_d(double v, double* sh) {
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -61,8 +73,13 @@ struct SysInfo {
     GcGrid mg;                       // aggregation grid: cubes at least MaxCut wide
 };
 
+// Positions are double-float: pos holds the FP32 position (what the pair,
+// membrane and list kernels read) and plo the FP32 remainder x - pos, so that
+// the position update accumulates with ~48-bit precision while the pair
+// kernels keep FP32 arithmetic.
 struct SlotArrays {
     float4 *pos, *vel, *vpred, *vh, *force;
+    float4* plo;   // low parts of the positions (x, y, z; w unused)
     int4* nthro;
     int* sys;   // system of each slot (nullptr for one system)
 };

@@ -5,7 +5,10 @@ Particle::UpdatePar does; with gc_set_engine(1) every step after the first
 runs fused inside SetFluidExtForce and writes back what the host reads.
 Compared with the entry-point kernels on the same sequence (noise on, so the
 same Philox pair noise): positions within 1e-5, velocities and forces within
-1e-4 of their largest magnitude, membrane outputs within 1e-5 relative.
+1e-4 of their largest magnitude, densities within 1e-5 relative (the fused
+step's double-float positions differ from the entry points' FP32 positions
+by up to an FP32 ulp per step, 1.3e-6 relative in density after 4 steps),
+membrane outputs within 1e-5 relative.
 """
 import numpy as np
 import pytest
@@ -53,7 +56,7 @@ def test_engine_follows_entry_point_kernels(cuda_device, engine_mode, name):
     np.testing.assert_allclose(b["pos"], a["pos"], atol=1e-5)
     _close_rel(b["vel"], a["vel"], 1e-4)
     _close_rel(b["force"], a["force"], 1e-4)
-    _close_rel(b["rho"], a["rho"], 1e-6)
+    _close_rel(b["rho"], a["rho"], 1e-5)
     assert np.array_equal(b["nthro"], a["nthro"])
     # the host's view: SortPart is a permutation and CurPos its inverse
     assert np.array_equal(np.sort(b["sortpart"]), np.arange(cfg.n))

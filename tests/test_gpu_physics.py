@@ -10,7 +10,10 @@
 * membrane area and volume follow the oracle within 1e-5 relative over 300
   steps (measured 1.1e-7);
 * trajectory drift against the oracle over 1000 steps (noise off) stays
-  below 5e-4 cut-off radii (measured 5e-5).
+  below 5e-5 cut-off radii (measured 5.3e-6);
+* double-float positions: particles far from the origin under a small body
+  force stay within one FP32 ulp of the FP64 oracle over 1000 steps, where
+  plain FP32 accumulation of the same displacements loses most of them.
 """
 import numpy as np
 import pytest
@@ -129,7 +132,7 @@ def test_trajectory_drift_1000_steps(cuda_device):
         d[:, 2] -= Lz * np.rint(d[:, 2] / Lz)
         drift.append(np.abs(d).max())
     print("\ndrift per 100 steps: " + " ".join(f"{x:.1e}" for x in drift))
-    assert drift[-1] < 5e-4
+    assert drift[-1] < 5e-5
 
 
 def test_gpu_diagnostics_match_the_stored_state(cuda_device):
@@ -154,3 +157,53 @@ def test_gpu_diagnostics_match_the_stored_state(cuda_device):
     assert d["mean_fluid_density"] == pytest.approx(rho.mean(), rel=1e-6)
     assert d["moving"] == v.shape[0]
     assert np.abs(d["momentum"]).max() < 1e-6 * np.sqrt(2 * E * m * v.shape[0])   # pairwise forces, no drive
+
+
+def _sparse_gas(x0=100.0, spacing=1.5, nx=64, nyz=4, g=0.02):
+    """Fluid particles farther apart than the cut-off (no pairs act), at
+    x in [x0, x0 + nx*spacing), in a periodic box; only the body force
+    moves them."""
+    ix, iy, iz = np.meshgrid(np.arange(nx), np.arange(nyz), np.arange(nyz), indexing="ij")
+    coor = np.stack([x0 + spacing * ix, spacing * (iy + 0.5), spacing * (iz + 0.5)], -1).reshape(-1, 3)
+    coor = coor.astype(np.float32)
+    L = spacing * nyz
+    return gen.Config(name="sparse_gas", bbox=np.array([0, 2 * x0, 0, L, 0, L], np.float32), pmask=7, n_b1=0,
+                      n_b2=0, n_fluid=coor.shape[0], coor=coor, velhalf=np.zeros_like(coor),
+                      den_init=gen.lattice_density(1.0 / 3.0), phys=gen.Physics(ext_force=g))
+
+
+def test_double_float_positions_far_from_the_origin(cuda_device):
+    """At x ~ 100-200 an FP32 ulp is 7.6e-6-1.5e-5, larger than the per-step
+    displacement dt*v (< 2e-8 * step for g = 0.02, dt = 1e-3): FP32 positions
+    do not move for hundreds of steps.  The fused step keeps each position as
+    an FP32 value plus its FP32 remainder and must track the FP64 oracle to
+    within one ulp of the stored FP32 value."""
+    from gpucell_gb300.fused import FusedSystem
+    cfg = _sparse_gas()
+    fs = FusedSystem(cfg, noise=False)
+    fs.step(1000, 1)
+    g = fs.fetch()
+    o = _oracle(cfg, False)
+    for _ in range(1000):
+        o.step()
+    x_gpu = g["pos"].astype(np.float64)
+    ulp = np.spacing(np.abs(g["pos"])).astype(np.float64)
+    err = np.abs(x_gpu - o.pos)
+    moved = o.pos[:, 0] - cfg.coor[:, 0].astype(np.float64)
+    # the same displacements accumulated in FP32, for the record
+    x32 = cfg.coor[:, 0].copy()
+    v = np.zeros_like(x32)
+    dt, a = np.float32(cfg.phys.dt), np.float32(cfg.phys.ext_force)
+    h, lam = np.float32(0.5) * dt * dt, np.float32(0.5) * dt
+    f = np.zeros_like(x32)
+    for _ in range(1000):
+        x32 = x32 + (dt * v + h * f)
+        f_new = np.full_like(x32, a)
+        v = v + lam * (f + f_new)
+        f = f_new
+    err32 = np.abs(x32.astype(np.float64) - o.pos[:, 0])
+    print(f"\ndisplacement {moved.mean():.3e}; |GPU - oracle| max {err.max():.2e} "
+          f"({(err / ulp).max():.2f} ulp); FP32 accumulation would be off by {err32.max():.2e} "
+          f"({(err32 / ulp[:, 0]).max():.0f} ulp)")
+    assert moved.min() > 5e-3
+    assert (err <= ulp).all()
