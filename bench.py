@@ -63,6 +63,13 @@ def parse():
                     help="skip the parity check against the FP64 oracle on a small channel")
     ap.add_argument("--no-output", dest="output", action="store_false",
                     help="skip timing one output step (GPUCell's output files)")
+    ap.add_argument("--rouleaux-run", action="store_true",
+                    help="instead of the suspension: rouleau sizes of 64 cells in Couette flow (1.0M fluid "
+                         "particles) tracked over --rouleaux-steps steps at three shear rates")
+    ap.add_argument("--rouleaux-steps", type=int, default=20000)
+    ap.add_argument("--rouleaux-every", type=int, default=1000)
+    ap.add_argument("--rouleaux-contact", type=float, default=0.6)
+    ap.add_argument("--shear-rates", type=str, default="0.005,0.05,0.5")
     return ap.parse_args()
 
 
@@ -217,6 +224,13 @@ def run_ours(args):
         t = torch.tensor([x], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
+
+    if args.rouleaux_run:
+        if rank == 0:
+            print(json.dumps(run_rouleaux(args)), flush=True)
+        if world > 1:
+            dist.destroy_process_group()
+        return
 
     if args.ensemble_only:
         ens = run_ensemble(args, dev, rank, world, barrier, max_over_ranks)
@@ -408,6 +422,68 @@ def run_ours(args):
 
 
 ENS_METRIC = "particle-steps/s on a 64-suspension ensemble (8k-200k particles, 0-16 cells of 642 vertices)"
+
+
+def run_rouleaux(args):
+    """Aggregation under shear: 64 cells of 2562 vertices at random positions
+    and orientations in Couette flow (walls moving at -+U, Morse aggregation
+    De = 3e-3, beta = 1.5, r0 = 0.3, cut-off 2.5, thermal noise on), the same
+    initial state at each shear rate; every `rouleaux_every` steps the
+    rouleaux are found on the GPU (cells in contact: a vertex pair closer than
+    `rouleaux_contact`).  Steps are timed with CUDA events, the rouleau
+    searches apart."""
+    import numpy as np
+    import torch
+    from gpucell_gb300 import generator
+    from gpucell_gb300.fused import FusedSystem
+
+    runs = []
+    S, E = max(1, args.rouleaux_steps), max(1, args.rouleaux_every)
+    for rate in [float(x) for x in args.shear_rates.split(",") if x]:
+        cfg = generator.sheared_suspension(shear_rate=rate)
+        fs = FusedSystem(cfg, noise=args.noise, skin=0.1, compact=True, graph=args.graph)
+        fs.step(3, 1)
+        torch.cuda.synchronize()
+        series, step_ms, search_ms = [], 0.0, []
+        done = 0
+
+        def sample():
+            t0 = time.perf_counter()
+            _, size = fs.rouleaux(args.rouleaux_contact)
+            search_ms.append(1e3 * (time.perf_counter() - t0))
+            series.append([done, int(size.size), int(size.max()), float(size.mean())])
+
+        sample()
+        r0 = fs.stats()["rebuilds"]
+        sampler = ClockSampler()
+        sampler.start()
+        while done < S:
+            k = min(E, S - done)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record()
+            fs.step(k, 0)
+            ev1.record()
+            torch.cuda.synchronize()
+            step_ms += ev0.elapsed_time(ev1)
+            done += k
+            sample()
+        clocks = sampler.stop()
+        st = fs.stats()
+        flags = fs.flags()
+        fs.close()
+        runs.append({"shear_rate": rate, "wall_speed": cfg.meta["wall_speed"], "clocks": clocks,
+                     "list_rebuilds": st["rebuilds"] - r0, "max_list": st["max_neighbors"],
+                     "strain": rate * S * cfg.phys.dt, "ms_per_step": step_ms / S,
+                     "particle_steps_per_s": cfg.n * S / (step_ms / 1e3), "rouleau_search_ms": float(np.median(search_ms)),
+                     "device_flags": flags,
+                     "series_columns": ["step", "rouleaux", "largest", "mean_cells"], "series": series})
+    return {"workload": "sheared_suspension", "particles": cfg.n, "fluid": cfg.n_fluid, "walls": cfg.n_b2,
+            "cells": cfg.ncell, "vertices_per_cell": int(cfg.npar[0]), "steps": S, "dt": cfg.phys.dt,
+            "contact": args.rouleaux_contact, "noise": "on" if args.noise else "off",
+            "captured_steps": bool(args.graph),
+            "morse": {"De": cfg.phys.sur_energy, "beta": cfg.phys.sca_fac, "r0": cfg.phys.zero_len,
+                      "cutoff": cfg.phys.max_cut},
+            "data": "synthetic (seeded generator, no dataset)", "runs": runs}
 
 
 def run_ensemble(args, dev, rank, world, barrier, max_over_ranks):

@@ -168,6 +168,8 @@ _SIGS = {
     "gc_ensemble_cell_sums": [_P, _I, _P, _P],
     "gc_ensemble_cell_stats": [_P, _I, _P],
     "gc_ensemble_diagnostics": [_P, _I, _P],
+    "gc_ensemble_rouleaux": [_P, _I, C.c_float, _P, _P, _P],
+    "gc_rouleaux_from_pairs": [_I, _I, _P, _P, _P, _P],
     "gc_ensemble_write_output": [_P, _I, C.c_char_p, C.c_longlong, C.c_double, _I, _I],
     "gc_fused_write_output": [_P, C.c_char_p, C.c_longlong, C.c_double, _I, _I],
     "gc_output_write": [_P, C.c_char_p, C.c_longlong, C.c_double, _I],

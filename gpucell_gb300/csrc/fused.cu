@@ -918,19 +918,41 @@ __global__ void fk_mkey(int ncp, const SysInfo* __restrict__ sys, const int* __r
     vals[v] = v;
 }
 
+// Membrane positions in aggregation-grid order, so that the candidates of a
+// cube are one contiguous run of float4 loads (the id bits in .w say which
+// vertex each is).
+__global__ void fk_msort(int ncp, const int* __restrict__ order, const float4* __restrict__ mpos,
+                         float4* __restrict__ mspos) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < ncp) mspos[q] = mpos[order[q]];
+}
+
+// Morse aggregation between vertices of different cells, one thread per
+// vertex in grid order.  The sort is stable and membrane vertices are in id
+// order, so within a cube the candidates ascend by id.  RUNS (every cell is
+// one contiguous id range that carries its CellTab index, checked at set-up):
+// the vertex's own cell is one run of each cube's candidates, skipped by a
+// binary search for its end; otherwise every candidate's CellTab is compared.
+template <bool RUNS>
 __global__ void fk_magg(int ncp, GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ msys,
                         const int* __restrict__ order, const unsigned* __restrict__ start,
-                        const float4* __restrict__ mpos, const int* __restrict__ celltab,
-                        const float* __restrict__ parea, float4* __restrict__ magg, float4* __restrict__ mforce) {
+                        const float4* __restrict__ mspos, const int* __restrict__ celltab,
+                        const int2* __restrict__ cell_verts, const float* __restrict__ parea,
+                        float4* __restrict__ magg, float4* __restrict__ mforce) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= ncp) return;
     int v = order[q];
     const SysInfo& S = sys[msys ? msys[v] : 0];
     const GcGrid& g = S.mg;
-    float4 x4 = mpos[v];
-    float3 xi = xyz(x4);
+    float3 xi = xyz(mspos[q]);
     int ci = celltab[v];
     float ai = parea[v];
+    unsigned own_lo = 0, own_hi = 0;   // ids of the vertex's own cell
+    if (RUNS) {
+        int2 cv = cell_verts[ci];
+        own_lo = S.cs + (unsigned)(cv.x - (int)S.m0);
+        own_hi = S.cs + (unsigned)(cv.y - (int)S.m0);
+    }
     int cx = cube_coord(xi.x, 0, g), cy = cube_coord(xi.y, 1, g), cz = cube_coord(xi.z, 2, g);
     float3 f = f3(0.f, 0.f, 0.f);
     for (int dz = -1; dz <= 1; ++dz) {
@@ -943,10 +965,29 @@ __global__ void fk_magg(int ncp, GcParams p, const SysInfo* __restrict__ sys, co
                 int x = cube_step(cx, dx, 0, g);
                 if (x < 0) continue;
                 int c = S.mcube0 + cube_key(x, y, z, g);
-                for (unsigned s = start[c]; s < start[c + 1]; ++s) {
-                    int w = order[s];
-                    if (celltab[w] == ci) continue;
-                    float3 d = min_image(xi, xyz(mpos[w]), g);
+                const unsigned s1 = start[c + 1];
+                for (unsigned s = start[c]; s < s1; ++s) {
+                    float4 y4 = mspos[s];
+                    unsigned idw = fid(y4);
+                    int w;
+                    if (RUNS) {
+                        if (idw >= own_lo && idw <= own_hi) {
+                            // first candidate past the own cell: ids ascend within the cube
+                            unsigned lo = s + 1, hi = s1;
+                            while (lo < hi) {
+                                unsigned mid = (lo + hi) >> 1;
+                                if (fid(mspos[mid]) <= own_hi) lo = mid + 1;
+                                else hi = mid;
+                            }
+                            s = lo - 1;
+                            continue;
+                        }
+                        w = (int)S.m0 + (int)(idw - S.cs);
+                    } else {
+                        w = order[s];
+                        if (celltab[w] == ci) continue;
+                    }
+                    float3 d = min_image(xi, xyz(y4), g);
                     float r2 = norm2_rn(d);
                     if (r2 >= p.maxcut2 || r2 <= 0.f) continue;
                     float r = sqrtf(r2);
@@ -1334,8 +1375,15 @@ int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p) {
                                                                   f->mvals);
         GC_CHECK_LAUNCH("fused: aggregation keys");
         GC_TRY(gc_counting_sort_bufs(f->ncp, f->Kagg, f->mkeys, f->mvals, f->sb_agg, f->flags, st));
-        fk_magg<<<gc_blocks(f->ncp, f->block), f->block, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mvals, f->sb_agg.cnt,
-                                                                  f->mpos, f->celltab, f->parea, f->magg, f->mforce);
+        const int nb = gc_blocks(f->ncp, f->block);
+        fk_msort<<<nb, f->block, 0, st>>>(f->ncp, f->mvals, f->mpos, f->mspos);
+        GC_CHECK_LAUNCH("fused: aggregation order");
+        if (f->agg_runs)
+            fk_magg<true><<<nb, f->block, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mvals, f->sb_agg.cnt, f->mspos,
+                                                   f->celltab, f->cell_verts, f->parea, f->magg, f->mforce);
+        else
+            fk_magg<false><<<nb, f->block, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mvals, f->sb_agg.cnt, f->mspos,
+                                                    f->celltab, f->cell_verts, f->parea, f->magg, f->mforce);
         GC_CHECK_LAUNCH("fused: aggregation");
     }
     return GC_OK;
@@ -1617,7 +1665,20 @@ int prepare_graph(GcFused* f, int drive) {
     return GC_OK;
 }
 
+// Captured steps run in segments of at most kGraphSegment steps, each from a
+// snapshot of the state: a list overflow (checked after each segment) sends
+// only that segment back to its snapshot, to run again with longer lists.
+constexpr int kGraphSegment = 128;
+
+int graph_segment(GcFused* f, int nsteps, int drive);
+
 int graph_steps(GcFused* f, int nsteps, int drive) {
+    for (int done = 0; done < nsteps; done += kGraphSegment)
+        GC_TRY(graph_segment(f, std::min(kGraphSegment, nsteps - done), drive));
+    return GC_OK;
+}
+
+int graph_segment(GcFused* f, int nsteps, int drive) {
     if (nsteps <= 0) return GC_OK;
     long long step0 = f->step;
     for (int attempt = 0; attempt < 4; ++attempt) {
@@ -1671,6 +1732,7 @@ int alloc_cells(GcFused* f, int ncell, int ntri, int nedge, int ncp) {
     GC_TRY(falloc(f, &f->magg, ncp));
     GC_TRY(falloc(f, &f->parea, ncp));
     GC_TRY(falloc(f, &f->mkeys, ncp));
+    GC_TRY(falloc(f, &f->mspos, ncp));
     GC_TRY(falloc(f, &f->mvals, ncp));
     GC_TRY(falloc(f, &f->mparts, 4 * (size_t)nedge + 3 * (size_t)ntri));
     GC_TRY(falloc(f, &f->inc_ptr, (size_t)ncp + 1));
@@ -1787,6 +1849,20 @@ int finalize_cells(GcFused* f) {
         GC_TRY(falloc(f, &f->cell_verts, ncell));
         GC_TRY(falloc(f, &f->cell_stats, 12 * (size_t)ncell));
         GC_TRY(up(f->cell_verts, cv.data(), cv.size() * 4));
+        // the aggregation pass may skip a vertex's own cell as one run of
+        // ids when each cell's vertex range is exactly the vertices whose
+        // CellTab names it (GPUCell labels the vertices of each cell in
+        // file order, src/Particle.cu:240)
+        bool runs = true;
+        for (int c = 0; c < ncell && runs; ++c) {
+            if (cv[2 * c] < 0 || cv[2 * c + 1] >= f->ncp || cv[2 * c + 1] < cv[2 * c]) runs = false;
+            for (int v = cv[2 * c]; runs && v <= cv[2 * c + 1]; ++v) runs = celltab[v] == c;
+        }
+        for (int v = 0; v < f->ncp && runs; ++v) {
+            int c = celltab[v];
+            runs = c >= 0 && c < ncell && v >= cv[2 * c] && v <= cv[2 * c + 1];
+        }
+        f->agg_runs = runs;
     }
     if (f->nsys > 1) {
         GC_TRY(falloc(f, &f->msys, f->ncp));

@@ -126,6 +126,17 @@ class _Handle:
         return dict(momentum=out[0:3].copy(), kinetic_energy=float(out[3]), temperature=float(out[4]),
                     max_speed=float(out[5]), mean_fluid_density=float(out[6]), moving=int(out[7]))
 
+    def rouleaux(self, contact, sys=0) -> tuple[np.ndarray, np.ndarray]:
+        """Rouleau label of every cell and the number of cells of each rouleau
+        (cells in contact: a vertex pair closer than `contact`), found on the
+        GPU (gc_ensemble_rouleaux)."""
+        cfg = self.cfgs[sys] if hasattr(self, "cfgs") else self.cfg
+        label = np.zeros(max(cfg.ncell, 1), np.int32)
+        size = np.zeros(max(cfg.ncell, 1), np.int32)
+        n = C.c_int()
+        _lib.call("gc_ensemble_rouleaux", self.h, int(sys), float(contact), _ptr(label), _ptr(size), C.byref(n))
+        return label[:cfg.ncell], size[:n.value]
+
     def checkpoint(self, path):
         _lib.call("gc_fused_checkpoint", self.h, str(path).encode())
 

@@ -342,6 +342,71 @@ def couette(nx=64, ny=32, nz=32, wall_layers=3, ncells=4, subdiv=3, cell_diamete
                    cell_centers=centers if ncells else None)
 
 
+def sheared_suspension(nx=136, ny=64, nz=136, wall_layers=3, ncells=64, subdiv=4, cell_diameter=None,
+                       shear_rate=0.05, seed=12345, phys: Physics | None = None, max_tries=20000,
+                       name="sheared_suspension") -> Config:
+    """Red cells in Couette flow for rouleau tracking: the channel of `couette`
+    (walls at y = -+Ly/2 moving at -+U, U = shear_rate * Ly / 2, no body
+    force, Morse aggregation on) with `ncells` cells of 10*4^subdiv+2
+    vertices at random positions and orientations, no two overlapping and
+    each at least one lattice spacing from the walls; the fluid lattice
+    sites nearest the membrane vertices are removed, one per vertex.  The
+    default is 64 cells of 2562 vertices and 1,019,776 fluid particles
+    (136 x 64 x 136 sites less 163,968).  The default diameter, 8, gives
+    membrane edges of about 0.29 (0.87 dx); at the diameter of `channel`'s
+    cell (5.33) a 2562-vertex membrane has edges of 0.19 and collapses
+    within 500 steps at dt = 1e-3."""
+    phys = phys or Physics(ext_force=0.0, sur_energy=3.0e-3, sca_fac=1.5, zero_len=0.3, max_cut=2.5)
+    rng = np.random.default_rng(seed)
+    dx = 1.0 / 3.0
+    Lx, Ly, Lz = nx * dx, ny * dx, nz * dx
+    d = cell_diameter if cell_diameter is not None else 8.0
+    v_unit, faces = icosphere(subdiv)
+    shape = biconcave(v_unit, d)
+    body = rbc_body_points(d, dx * 0.9, 0.5 * dx)
+    grid_n = np.array([int(Lx / dx), int(Ly / dx), int(Lz / dx)])
+    occ = np.zeros(tuple(grid_n), bool)
+    cells = []
+    for _ in range(ncells):
+        for _try in range(max_tries):
+            R = random_rotation(rng)
+            cen = rng.uniform(0, 1, 3) * np.array([Lx, Ly, Lz]) - np.array([0.0, Ly / 2, Lz / 2])
+            verts = shape @ R.T + cen
+            if np.abs(verts[:, 1]).max() > Ly / 2 - dx:
+                continue
+            pts = body @ R.T + cen
+            idx = np.floor((pts + np.array([0.0, Ly / 2, Lz / 2])) / dx).astype(int)
+            idx[:, 0] %= grid_n[0]
+            idx[:, 2] %= grid_n[2]
+            idx[:, 1] = np.clip(idx[:, 1], 0, grid_n[1] - 1)
+            if occ[idx[:, 0], idx[:, 1], idx[:, 2]].any():
+                continue
+            occ[idx[:, 0], idx[:, 1], idx[:, 2]] = True
+            cells.append((verts, faces))
+            break
+        else:
+            raise RuntimeError(f"could not place cell {len(cells)} without overlap")
+    base = couette(nx=nx, ny=ny, nz=nz, wall_layers=wall_layers, ncells=0, shear_rate=shear_rate, seed=seed,
+                   phys=phys, name=name)
+    fl0, fl1 = base.n_b1 + base.n_b2, base.n_b1 + base.n_b2 + base.n_fluid
+    lattice = base.coor[fl0:fl1].astype(np.float64)
+    ncp = sum(c[0].shape[0] for c in cells)
+    if ncp:
+        from scipy.spatial import cKDTree
+        per = np.array([Lx, 2.0 * Ly + 1.0, Lz])   # x and z periodic; y far wider than the channel
+        shift = np.array([0.0, Ly, Lz / 2])
+        mv = np.mod(np.concatenate([c[0] for c in cells]) + shift, per)
+        tree = cKDTree(mv, boxsize=per)
+        dist, _ = tree.query(np.mod(lattice + shift, per), k=1, workers=-1)
+        keep = np.argsort(dist, kind="stable")[ncp:]
+        lattice = lattice[np.sort(keep)]
+    b2 = base.coor[base.n_b1:fl0]
+    cfg = _assemble(name, base.bbox, base.pmask, np.zeros((0, 3)), b2, lattice, cells, phys, dx,
+                    wall_vel=base.velhalf[base.n_b1:fl0])
+    cfg.meta = dict(ncells=ncells, diameter=d, shear_rate=shear_rate, wall_speed=shear_rate * Ly / 2.0, seed=seed)
+    return cfg
+
+
 def constriction(nx=96, ny=36, nz=24, wall_layers=3, b1_layers=1, ratio=2.0, ncells=2, subdiv=3,
                  cell_diameter=None, seed=12345, phys: Physics | None = None, name="constriction") -> Config:
     """Channel with a smooth 2:1 constriction of frozen wall particles: the

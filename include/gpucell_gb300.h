@@ -323,6 +323,19 @@ int gc_ensemble_cell_stats(GcFused* f, int sys, double* out);
  * ((2 E_kin - |P|^2/M) / 3N), out[5] the largest speed, out[6] the mean fluid
  * density, out[7] the number of moving particles.  Host pointer, 8 doubles. */
 int gc_ensemble_diagnostics(GcFused* f, int sys, double* out);
+/* Rouleaux (aggregates of red cells) of one system: two cells are in contact
+ * when a vertex of one and a vertex of the other are closer than `contact`
+ * (minimum image; FP32 squared distance < contact^2), and a rouleau is a
+ * connected set of cells under contact.  label[c] (ncell ints, may be NULL)
+ * receives the rouleau of cell c, numbered 0.. in the order of each
+ * rouleau's lowest cell; size[k] (ncell ints, may be NULL) the number of
+ * cells of rouleau k (0 past the last); *nrouleaux the number of rouleaux.
+ * Contacts are found on the GPU: bounding spheres of the cells select the
+ * candidate pairs, then one block per pair tests their vertices. */
+int gc_ensemble_rouleaux(GcFused* f, int sys, float contact, int* label, int* size, int* nrouleaux);
+/* The rouleau labelling of gc_ensemble_rouleaux from a list of contact pairs
+ * (npairs x 2 cell indices in 0..ncell-1); host only. */
+int gc_rouleaux_from_pairs(int ncell, int npairs, const int* pairs, int* label, int* size, int* nrouleaux);
 /* Stores one system of a fused handle and writes its output files. */
 int gc_ensemble_write_output(GcFused* f, int sys, const char* dir, long long step_data, double time, int first,
                              int threads);

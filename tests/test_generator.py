@@ -104,3 +104,23 @@ def test_constriction_walls_follow_the_profile():
     b2 = cfg.coor[cfg.n_b1:cfg.n_b1 + cfg.n_b2]
     assert np.abs(b2[np.abs(b2[:, 0] - Lx / 2) < 0.2, 1]).min() >= 0.49 * H
     assert cfg.n_b1 > 0 and cfg.ncell == 2 and cfg.pmask == 5
+
+
+def test_sheared_suspension_places_cells_inside_the_channel():
+    cfg = gen.sheared_suspension(nx=36, ny=24, nz=36, ncells=6, subdiv=2, cell_diameter=3.0, shear_rate=0.5, seed=3)
+    Ly = 24 / 3.0
+    assert cfg.ncell == 6 and cfg.ncp == 6 * 162
+    assert cfg.n_fluid == 36 * 24 * 36 - cfg.ncp          # one lattice site removed per vertex
+    m = cfg.coor[cfg.n_cell_start:].astype(np.float64)
+    assert np.abs(m[:, 1]).max() <= Ly / 2 - 1.0 / 3.0   # clear of the walls
+    u = 0.5 * Ly / 2
+    b2 = cfg.velhalf[cfg.n_b1:cfg.n_b1 + cfg.n_b2]
+    y = cfg.coor[cfg.n_b1:cfg.n_b1 + cfg.n_b2, 1]
+    assert np.allclose(b2[y < 0, 0], -u) and np.allclose(b2[y > 0, 0], u)
+    # no two cells overlap: their vertices stay apart (periodic in x and z)
+    L = np.array([36 / 3.0, np.inf, 36 / 3.0])
+    for a in range(6):
+        for b in range(a + 1, 6):
+            d = m[162 * a:162 * (a + 1), None, :] - m[None, 162 * b:162 * (b + 1), :]
+            d[..., [0, 2]] -= L[[0, 2]] * np.rint(d[..., [0, 2]] / L[[0, 2]])
+            assert np.sqrt((d ** 2).sum(-1)).min() > 0.2

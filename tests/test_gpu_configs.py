@@ -87,3 +87,26 @@ def test_boundary_path_tracks_oracle(cuda_device, shape):
     got = ps.fetch()
     got["Area64"], got["Vol64"] = got["Area"].astype(np.float64), got["Vol"].astype(np.float64)
     _check(got, o, cfg, agg=shape == "couette")
+
+
+def test_aggregation_fallback_without_contiguous_cell_labels(cuda_device):
+    """The aggregation pass skips a vertex's own cell as one run of ids when
+    each cell's vertices carry its own CellTab index; with the labels of the
+    cells permuted (still one label per cell) it compares every candidate's
+    label instead.  Both must give bit-identical aggregation forces and
+    trajectories."""
+    import dataclasses
+    from gpucell_gb300.fused import FusedSystem
+    cfg = gen.couette(nx=36, ny=24, nz=24, ncells=3, subdiv=2, cell_diameter=3.0, shear_rate=0.5, seed=31)
+    perm = np.array([2, 0, 1], np.int32)
+    swapped = dataclasses.replace(cfg, celltab=perm[cfg.celltab])
+    out = []
+    for c in (cfg, swapped):
+        fs = FusedSystem(c, noise=True)
+        fs.step(20, 1)
+        out.append(fs.fetch())
+        fs.close()
+    a, b = out
+    assert np.abs(a["AggForce"]).max() > 0
+    assert np.array_equal(a["AggForce"], b["AggForce"])
+    assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
