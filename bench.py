@@ -70,6 +70,11 @@ def parse():
     ap.add_argument("--rouleaux-every", type=int, default=1000)
     ap.add_argument("--rouleaux-contact", type=float, default=0.6)
     ap.add_argument("--shear-rates", type=str, default="0.005,0.05,0.5")
+    ap.add_argument("--constriction-run", action="store_true",
+                    help="instead of the suspension: 100 cells through a 2:1 constriction (2.0M particles), with "
+                         "an FP64 host check of every cell's area and volume every --check-every steps")
+    ap.add_argument("--constriction-steps", type=int, default=1000)
+    ap.add_argument("--check-every", type=int, default=100)
     return ap.parse_args()
 
 
@@ -225,9 +230,9 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    if args.rouleaux_run:
+    if args.rouleaux_run or args.constriction_run:
         if rank == 0:
-            print(json.dumps(run_rouleaux(args)), flush=True)
+            print(json.dumps(run_rouleaux(args) if args.rouleaux_run else run_constriction(args)), flush=True)
         if world > 1:
             dist.destroy_process_group()
         return
@@ -340,13 +345,12 @@ def run_ours(args):
 
     fs.close()
     ens = run_ensemble(args, dev, rank, world, barrier, max_over_ranks) if args.ensemble else None
-    parity = parity_check() if (args.parity and rank == 0) else None
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return
 
-    cpu = cpu_baseline(cfg, args.cpu_steps) if (world == 1 and args.cpu_steps > 0) else None
+    cpu, parity = cpu_leg(cfg, args.cpu_steps if world == 1 else 0, 100 if args.parity else 0)
     line = {
         "metric": METRIC,
         "value": value,
@@ -486,6 +490,80 @@ def run_rouleaux(args):
             "data": "synthetic (seeded generator, no dataset)", "runs": runs}
 
 
+def cell_geometry_fp64(cfg, pos, nthro):
+    """Area and volume of every cell in FP64 on the host, from the stored FP32
+    positions unwrapped by their crossing counts (x + n L on periodic axes):
+    triangle areas |(b - a) x (c - a)| / 2 and, by the divergence theorem,
+    volumes a . (b x c) / 6, summed over each cell's triangles."""
+    import numpy as np
+    L = (cfg.bbox[1::2].astype(np.float64) - cfg.bbox[0::2].astype(np.float64))
+    L = L * np.array([(cfg.pmask >> k) & 1 for k in range(3)], np.float64)
+    cs = cfg.n_cell_start
+    m = pos[cs:].astype(np.float64) + nthro[cs:].astype(np.float64) * L
+    t = cfg.tri.astype(np.int64) - 1
+    a, b, c = m[t[:, 0]], m[t[:, 1]], m[t[:, 2]]
+    area_t = 0.5 * np.linalg.norm(np.cross(b - a, c - a), axis=1)
+    vol_t = np.einsum("ij,ij->i", a, np.cross(b, c)) / 6.0
+    first = cfg.betri[:, 0].astype(np.int64)
+    return np.add.reduceat(area_t, first), np.add.reduceat(vol_t, first)
+
+
+def run_constriction(args):
+    """Complex geometry: 100 cells of 642 vertices at random positions and
+    orientations in a channel with a 2:1 constriction of frozen wall
+    particles (1,951,322 particles), driven by the body force.  Every
+    `check_every` steps the GPU's FP64 per-cell area and volume are checked
+    against an FP64 host evaluation from the stored positions, and their
+    drift from the set-up values is recorded.  Steps are timed with CUDA
+    events, the checks apart."""
+    import numpy as np
+    import torch
+    from gpucell_gb300 import generator
+    from gpucell_gb300.fused import FusedSystem
+
+    cfg = generator.constriction(nx=280, ny=96, nz=72, ncells=100, subdiv=3, layout="random")
+    fs = FusedSystem(cfg, noise=args.noise, skin=0.075, compact=True, graph=args.graph)
+    S, E = max(1, args.constriction_steps), max(1, args.check_every)
+    g = fs.fetch()
+    a0, v0 = g["Area64"].copy(), g["Vol64"].copy()
+    checks, step_ms, done = [], 0.0, 0
+
+    def check():
+        g = fs.fetch()
+        ha, hv = cell_geometry_fp64(cfg, g["pos"], g["nthro"])
+        checks.append([done, float(np.abs(g["Area64"] / ha - 1).max()), float(np.abs(g["Vol64"] / hv - 1).max()),
+                       float(np.abs(g["Area64"] / a0 - 1).max()), float(np.abs(g["Vol64"] / v0 - 1).max())])
+
+    check()
+    r0 = fs.stats()["rebuilds"]
+    sampler = ClockSampler()
+    sampler.start()
+    while done < S:
+        k = min(E, S - done)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        fs.step(k, 1)
+        ev1.record()
+        torch.cuda.synchronize()
+        step_ms += ev0.elapsed_time(ev1)
+        done += k
+        check()
+    clocks = sampler.stop()
+    st = fs.stats()
+    flags = fs.flags()
+    fs.close()
+    arr = np.array(checks)
+    return {"workload": "constriction", "particles": cfg.n, "fluid": cfg.n_fluid, "walls": cfg.n_b1 + cfg.n_b2,
+            "cells": cfg.ncell, "vertices_per_cell": int(cfg.npar[0]), "steps": S, "dt": cfg.phys.dt,
+            "noise": "on" if args.noise else "off", "captured_steps": bool(args.graph),
+            "ms_per_step": step_ms / S, "particle_steps_per_s": cfg.n * S / (step_ms / 1e3),
+            "max_area_error_vs_fp64_host": float(arr[:, 1].max()),
+            "max_volume_error_vs_fp64_host": float(arr[:, 2].max()),
+            "checks_columns": ["step", "area_error", "volume_error", "area_drift", "volume_drift"],
+            "checks": checks, "list_rebuilds": st["rebuilds"] - r0, "max_list": st["max_neighbors"],
+            "device_flags": flags, "clocks": clocks, "data": "synthetic (seeded generator, no dataset)"}
+
+
 def run_ensemble(args, dev, rank, world, barrier, max_over_ranks):
     """Independent suspensions of uneven size stepped together (one ensemble
     per GPU, systems shared out by LPT over ranks), against the same systems
@@ -575,6 +653,20 @@ def run_ensemble(args, dev, rank, world, barrier, max_over_ranks):
     return out
 
 
+def cpu_leg(cfg, cpu_steps, parity_steps):
+    """The FP64 CPU oracle's leg of the bench (rank 0): `cpu_baseline` times
+    `cpu_steps` full oracle steps of the workload on the host cores; `parity`
+    steps a small walled channel `parity_steps` times with the oracle as the
+    checker beside the fused step.  The oracle is used nowhere else here."""
+    from gpucell_gb300.build import build_oracle
+    if cpu_steps <= 0 and parity_steps <= 0:
+        return None, None
+    build_oracle()
+    cpu = cpu_baseline(cfg, cpu_steps) if cpu_steps > 0 else None
+    par = parity_check(parity_steps) if parity_steps > 0 else None
+    return cpu, par
+
+
 def parity_check(steps=100):
     """The fused step against the FP64 oracle on a walled channel with one
     red cell (Bound1 and Bound2 walls, 5.9k particles, noise off): largest
@@ -583,9 +675,7 @@ def parity_check(steps=100):
     after `steps` steps."""
     import numpy as np
     from gpucell_gb300 import generator
-    from gpucell_gb300.build import build_oracle
     from gpucell_gb300.fused import FusedSystem
-    build_oracle()
     from oracle.binding import Oracle
     cfg = generator.small_channel()
     fs = FusedSystem(cfg, noise=False)

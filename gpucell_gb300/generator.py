@@ -408,7 +408,8 @@ def sheared_suspension(nx=136, ny=64, nz=136, wall_layers=3, ncells=64, subdiv=4
 
 
 def constriction(nx=96, ny=36, nz=24, wall_layers=3, b1_layers=1, ratio=2.0, ncells=2, subdiv=3,
-                 cell_diameter=None, seed=12345, phys: Physics | None = None, name="constriction") -> Config:
+                 cell_diameter=None, seed=12345, phys: Physics | None = None, name="constriction",
+                 layout="line", max_tries=20000) -> Config:
     """Channel with a smooth 2:1 constriction of frozen wall particles: the
     walls y = +-h(x) follow the signed-distance profile
     h(x) = H - (H - H/ratio) (1 + cos(2 pi (x - Lx/2)/w))/2 for |x - Lx/2| < w/2
@@ -417,8 +418,11 @@ def constriction(nx=96, ny=36, nz=24, wall_layers=3, b1_layers=1, ratio=2.0, nce
     |y| < h(x) is fluid, h(x) <= |y| < h(x) + wall_layers dx is Bound2 and the
     next b1_layers dx is Bound1; the rest is empty.  Periodic in x and z;
     the body force drives the flow through the throat (the pressure drop of a
-    driven inflow in a periodic channel).  Cells sit in the wide part,
-    upstream of the throat."""
+    driven inflow in a periodic channel).  layout "line": the cells sit in
+    a row along z in the wide part, upstream of the throat, disc normals
+    facing the flow; "random": at seeded random positions and orientations
+    anywhere in the channel, no two overlapping and every vertex at least
+    one lattice spacing inside the walls."""
     phys = phys or Physics()
     rng = np.random.default_rng(seed)
     dx = 1.0 / 3.0
@@ -440,7 +444,33 @@ def constriction(nx=96, ny=36, nz=24, wall_layers=3, b1_layers=1, ratio=2.0, nce
     b2 = lat[(ay >= hx) & (ay < hx + wall_layers * dx)]
     b1 = lat[(ay >= hx + wall_layers * dx) & (ay < hx + t)]
     cells = []
-    if ncells:
+    if ncells and layout == "random":
+        d = cell_diameter if cell_diameter is not None else 8.0 / 1.5
+        v, f = icosphere(subdiv)
+        shape = biconcave(v, d)
+        body = rbc_body_points(d, dx * 0.9, 0.5 * dx)
+        grid_n = np.array([int(round(Lx / dx)), int(round(Ly / dx)), int(round(Lz / dx))])
+        occ = np.zeros(tuple(grid_n), bool)
+        off = np.array([0.0, H, Lz / 2])
+        for _ in range(ncells):
+            for _try in range(max_tries):
+                R = random_rotation(rng)
+                cen = rng.uniform(0, 1, 3) * np.array([Lx, Ly, Lz]) - np.array([0.0, H, Lz / 2])
+                verts = shape @ R.T + cen
+                if (np.abs(verts[:, 1]) > h(np.mod(verts[:, 0], Lx)) - dx).any():
+                    continue
+                idx = np.floor((body @ R.T + cen + off) / dx).astype(int)
+                idx[:, 0] %= grid_n[0]
+                idx[:, 2] %= grid_n[2]
+                idx[:, 1] = np.clip(idx[:, 1], 0, grid_n[1] - 1)
+                if occ[idx[:, 0], idx[:, 1], idx[:, 2]].any():
+                    continue
+                occ[idx[:, 0], idx[:, 1], idx[:, 2]] = True
+                cells.append((verts, f))
+                break
+            else:
+                raise RuntimeError(f"could not place cell {len(cells)} without overlap")
+    elif ncells:
         d = cell_diameter if cell_diameter is not None else 0.5 * H
         v, f = icosphere(subdiv)
         shape = biconcave(v, d)
@@ -450,10 +480,12 @@ def constriction(nx=96, ny=36, nz=24, wall_layers=3, b1_layers=1, ratio=2.0, nce
             if abs(z) + 0.55 * d > Lz / 2:
                 raise ValueError("box too thin for the cells")
             cells.append((shape @ rot.T + np.array([Lx / 6, 0.0, z]), f))
-        mv = np.concatenate([c[0] for c in cells])
+    if cells:
         from scipy.spatial import cKDTree
-        tree = cKDTree(mv)
-        dist, _ = tree.query(fluid, k=1)
+        per = np.array([Lx, 4.0 * (H + t) + 1.0, Lz])   # x and z periodic; y wider than the box
+        shift = np.array([0.0, 2.0 * (H + t), Lz / 2])
+        tree = cKDTree(np.mod(np.concatenate([c[0] for c in cells]) + shift, per), boxsize=per)
+        dist, _ = tree.query(np.mod(fluid + shift, per), k=1, workers=-1)
         fluid = fluid[dist > 0.6 * dx]   # room for the membranes
     bbox = [0.0, Lx, -H - t, H + t, -Lz / 2, Lz / 2]
     return _assemble(name, bbox, 1 | 4, b1, b2, fluid, cells, phys, dx)
