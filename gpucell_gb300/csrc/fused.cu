@@ -918,27 +918,67 @@ __global__ void fk_mkey(int ncp, const SysInfo* __restrict__ sys, const int* __r
     vals[v] = v;
 }
 
-// Membrane positions in aggregation-grid order, so that the candidates of a
-// cube are one contiguous run of float4 loads (the id bits in .w say which
-// vertex each is).
+// Membrane positions and vertex areas in aggregation-grid order, so that the
+// candidates of a cube are contiguous runs of loads (the id bits in .w say
+// which vertex each is).
 __global__ void fk_msort(int ncp, const int* __restrict__ order, const float4* __restrict__ mpos,
-                         float4* __restrict__ mspos) {
+                         const float* __restrict__ parea, float4* __restrict__ mspos, float* __restrict__ msarea) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < ncp) mspos[q] = mpos[order[q]];
+    if (q >= ncp) return;
+    int v = order[q];
+    mspos[q] = mpos[v];
+    msarea[q] = parea[v];
+}
+
+// Morse force on a vertex at xi (area ai) from a vertex at y (area *aj).
+__device__ __forceinline__ void morse_pair(const GcParams& p, const GcGrid& g, float3 xi, float ai, float4 y,
+                                           const float* __restrict__ aj, float3& f) {
+    float3 d = min_image(xi, xyz(y), g);
+    float r2 = norm2_rn(d);
+    if (r2 >= p.maxcut2 || r2 <= 0.f) return;
+    float r = sqrtf(r2);
+    float ex = __expf(p.beta * (p.r0m - r));
+    float fm = 2.f * p.De * p.beta * (ex * ex - ex) * 0.5f * (ai + *aj);
+    f += (fm / r) * d;
+}
+
+// Candidates [a, b) of the cube-ordered arrays, four loads in flight.
+__device__ __forceinline__ void morse_run(const GcParams& p, const GcGrid& g, float3 xi, float ai, unsigned a,
+                                          unsigned b, const float4* __restrict__ mspos,
+                                          const float* __restrict__ msarea, float3& f) {
+    unsigned s = a;
+    for (; s + 4 <= b; s += 4) {
+        float4 y0 = mspos[s], y1 = mspos[s + 1], y2 = mspos[s + 2], y3 = mspos[s + 3];
+        morse_pair(p, g, xi, ai, y0, msarea + s, f);
+        morse_pair(p, g, xi, ai, y1, msarea + s + 1, f);
+        morse_pair(p, g, xi, ai, y2, msarea + s + 2, f);
+        morse_pair(p, g, xi, ai, y3, msarea + s + 3, f);
+    }
+    for (; s < b; ++s) morse_pair(p, g, xi, ai, mspos[s], msarea + s, f);
 }
 
 // Morse aggregation between vertices of different cells, one thread per
-// vertex in grid order.  The sort is stable and membrane vertices are in id
-// order, so within a cube the candidates ascend by id.  RUNS (every cell is
-// one contiguous id range that carries its CellTab index, checked at set-up):
-// the vertex's own cell is one run of each cube's candidates, skipped by a
-// binary search for its end; otherwise every candidate's CellTab is compared.
+// vertex in grid order.  The sort is stable and membrane vertices are in id order, so
+// within a cube the candidates ascend by id.  RUNS (every cell is one
+// contiguous id range that carries its CellTab index, checked at set-up):
+// the vertex's own cell is one run of a cube's candidates, bounded by two
+// binary searches where the cube's first and last ids say it is there, and
+// the candidates on either side are scanned without a test; otherwise every
+// candidate's CellTab is compared.  Both visit the same candidates in the
+// same order.
+#ifndef GC_AGG_BS
+#define GC_AGG_BS 128
+#endif
+constexpr int kAggBS = GC_AGG_BS;
+
 template <bool RUNS>
-__global__ void fk_magg(int ncp, GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ msys,
-                        const int* __restrict__ order, const unsigned* __restrict__ start,
-                        const float4* __restrict__ mspos, const int* __restrict__ celltab,
-                        const int2* __restrict__ cell_verts, const float* __restrict__ parea,
-                        float4* __restrict__ magg, float4* __restrict__ mforce) {
+__global__ void __launch_bounds__(kAggBS) fk_magg(int ncp, GcParams p, const SysInfo* __restrict__ sys,
+                                                  const int* __restrict__ msys, const int* __restrict__ order,
+                                                  const unsigned* __restrict__ start,
+                                                  const float4* __restrict__ mspos, const float* __restrict__ msarea,
+                                                  const int* __restrict__ celltab,
+                                                  const int2* __restrict__ cell_verts, float4* __restrict__ magg,
+                                                  float4* __restrict__ mforce) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= ncp) return;
     int v = order[q];
@@ -946,7 +986,7 @@ __global__ void fk_magg(int ncp, GcParams p, const SysInfo* __restrict__ sys, co
     const GcGrid& g = S.mg;
     float3 xi = xyz(mspos[q]);
     int ci = celltab[v];
-    float ai = parea[v];
+    float ai = msarea[q];
     unsigned own_lo = 0, own_hi = 0;   // ids of the vertex's own cell
     if (RUNS) {
         int2 cv = cell_verts[ci];
@@ -965,35 +1005,31 @@ __global__ void fk_magg(int ncp, GcParams p, const SysInfo* __restrict__ sys, co
                 int x = cube_step(cx, dx, 0, g);
                 if (x < 0) continue;
                 int c = S.mcube0 + cube_key(x, y, z, g);
-                const unsigned s1 = start[c + 1];
-                for (unsigned s = start[c]; s < s1; ++s) {
-                    float4 y4 = mspos[s];
-                    unsigned idw = fid(y4);
-                    int w;
-                    if (RUNS) {
-                        if (idw >= own_lo && idw <= own_hi) {
-                            // first candidate past the own cell: ids ascend within the cube
-                            unsigned lo = s + 1, hi = s1;
-                            while (lo < hi) {
-                                unsigned mid = (lo + hi) >> 1;
-                                if (fid(mspos[mid]) <= own_hi) lo = mid + 1;
-                                else hi = mid;
-                            }
-                            s = lo - 1;
-                            continue;
-                        }
-                        w = (int)S.m0 + (int)(idw - S.cs);
-                    } else {
-                        w = order[s];
-                        if (celltab[w] == ci) continue;
+                const unsigned s0 = start[c], s1 = start[c + 1];
+                if (s0 == s1) continue;
+                if (RUNS) {
+                    if (own_hi < fid(mspos[s0]) || own_lo > fid(mspos[s1 - 1])) {
+                        morse_run(p, g, xi, ai, s0, s1, mspos, msarea, f);
+                        continue;
                     }
-                    float3 d = min_image(xi, xyz(y4), g);
-                    float r2 = norm2_rn(d);
-                    if (r2 >= p.maxcut2 || r2 <= 0.f) continue;
-                    float r = sqrtf(r2);
-                    float ex = __expf(p.beta * (p.r0m - r));
-                    float fm = 2.f * p.De * p.beta * (ex * ex - ex) * 0.5f * (ai + parea[w]);
-                    f += (fm / r) * d;
+                    unsigned lo = s0, hi = s1;
+                    while (lo < hi) {   // first candidate of the own cell
+                        unsigned mid = (lo + hi) >> 1;
+                        if (fid(mspos[mid]) < own_lo) lo = mid + 1;
+                        else hi = mid;
+                    }
+                    const unsigned a = lo;
+                    hi = s1;
+                    while (lo < hi) {   // first candidate past it
+                        unsigned mid = (lo + hi) >> 1;
+                        if (fid(mspos[mid]) <= own_hi) lo = mid + 1;
+                        else hi = mid;
+                    }
+                    morse_run(p, g, xi, ai, s0, a, mspos, msarea, f);
+                    morse_run(p, g, xi, ai, lo, s1, mspos, msarea, f);
+                } else {
+                    for (unsigned s = s0; s < s1; ++s)
+                        if (celltab[order[s]] != ci) morse_pair(p, g, xi, ai, mspos[s], msarea + s, f);
                 }
             }
         }
@@ -1376,14 +1412,15 @@ int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p) {
         GC_CHECK_LAUNCH("fused: aggregation keys");
         GC_TRY(gc_counting_sort_bufs(f->ncp, f->Kagg, f->mkeys, f->mvals, f->sb_agg, f->flags, st));
         const int nb = gc_blocks(f->ncp, f->block);
-        fk_msort<<<nb, f->block, 0, st>>>(f->ncp, f->mvals, f->mpos, f->mspos);
+        fk_msort<<<nb, f->block, 0, st>>>(f->ncp, f->mvals, f->mpos, f->parea, f->mspos, f->msarea);
         GC_CHECK_LAUNCH("fused: aggregation order");
+        const int nba = gc_blocks(f->ncp, kAggBS);
         if (f->agg_runs)
-            fk_magg<true><<<nb, f->block, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mvals, f->sb_agg.cnt, f->mspos,
-                                                   f->celltab, f->cell_verts, f->parea, f->magg, f->mforce);
+            fk_magg<true><<<nba, kAggBS, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mvals, f->sb_agg.cnt, f->mspos,
+                                                  f->msarea, f->celltab, f->cell_verts, f->magg, f->mforce);
         else
-            fk_magg<false><<<nb, f->block, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mvals, f->sb_agg.cnt, f->mspos,
-                                                    f->celltab, f->cell_verts, f->parea, f->magg, f->mforce);
+            fk_magg<false><<<nba, kAggBS, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mvals, f->sb_agg.cnt, f->mspos,
+                                                   f->msarea, f->celltab, f->cell_verts, f->magg, f->mforce);
         GC_CHECK_LAUNCH("fused: aggregation");
     }
     return GC_OK;
@@ -1733,6 +1770,7 @@ int alloc_cells(GcFused* f, int ncell, int ntri, int nedge, int ncp) {
     GC_TRY(falloc(f, &f->parea, ncp));
     GC_TRY(falloc(f, &f->mkeys, ncp));
     GC_TRY(falloc(f, &f->mspos, ncp));
+    GC_TRY(falloc(f, &f->msarea, ncp));
     GC_TRY(falloc(f, &f->mvals, ncp));
     GC_TRY(falloc(f, &f->mparts, 4 * (size_t)nedge + 3 * (size_t)ntri));
     GC_TRY(falloc(f, &f->inc_ptr, (size_t)ncp + 1));

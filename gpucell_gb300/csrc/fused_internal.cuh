@@ -183,6 +183,7 @@ struct GcFused {
     float* parea = nullptr;
     int *mkeys = nullptr, *mvals = nullptr;
     float4* mspos = nullptr;     // membrane positions in aggregation-grid order (after the aggregation sort)
+    float* msarea = nullptr;     // vertex areas in the same order
     bool agg_runs = false;       // every cell's vertices are one contiguous range carrying its CellTab index
     float4* mparts = nullptr;    // per-edge and per-triangle vertex forces (4 per edge, then 3 per triangle)
     int *inc_ptr = nullptr, *inc = nullptr;   // vertex -> its parts (CSR)
