@@ -958,7 +958,9 @@ __device__ __forceinline__ void morse_run(const GcParams& p, const GcGrid& g, fl
 }
 
 // Morse aggregation between vertices of different cells, one thread per
-// vertex in grid order.  The sort is stable and membrane vertices are in id order, so
+// vertex in grid order, over the (2R+1)^3 aggregation cubes around it (R = 2
+// for cubes at least MaxCut/2 wide, 1 for cubes at least MaxCut wide).  The
+// sort is stable and membrane vertices are in id order, so
 // within a cube the candidates ascend by id.  RUNS (every cell is one
 // contiguous id range that carries its CellTab index, checked at set-up):
 // the vertex's own cell is one run of a cube's candidates, bounded by two
@@ -994,14 +996,15 @@ __global__ void __launch_bounds__(kAggBS) fk_magg(int ncp, GcParams p, const Sys
         own_hi = S.cs + (unsigned)(cv.y - (int)S.m0);
     }
     int cx = cube_coord(xi.x, 0, g), cy = cube_coord(xi.y, 1, g), cz = cube_coord(xi.z, 2, g);
+    const int R = S.mlr;
     float3 f = f3(0.f, 0.f, 0.f);
-    for (int dz = -1; dz <= 1; ++dz) {
+    for (int dz = -R; dz <= R; ++dz) {
         int z = cube_step(cz, dz, 2, g);
         if (z < 0) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
+        for (int dy = -R; dy <= R; ++dy) {
             int y = cube_step(cy, dy, 1, g);
             if (y < 0) continue;
-            for (int dx = -1; dx <= 1; ++dx) {
+            for (int dx = -R; dx <= R; ++dx) {
                 int x = cube_step(cx, dx, 0, g);
                 if (x < 0) continue;
                 int c = S.mcube0 + cube_key(x, y, z, g);
@@ -1278,11 +1281,20 @@ int build_grids(GcFused* f) {
         S.cube0 = K;
         K += S.g.ncells;
         if (f->have_agg) {
-            GC_TRY(gc_build_grid(d.bbox, f->p.maxcut, d.periodic_mask, &S.mg));
+            // the same for the aggregation grid: half-width cubes cut the
+            // candidates of the Morse pass by ~40 %
+            S.mlr = 2;
+            if (gc_build_grid(d.bbox, 0.5f * f->p.maxcut, d.periodic_mask, &S.mg) != GC_OK ||
+                ((d.periodic_mask & 1) && S.mg.n[0] < 5) || ((d.periodic_mask & 2) && S.mg.n[1] < 5) ||
+                ((d.periodic_mask & 4) && S.mg.n[2] < 5)) {
+                S.mlr = 1;
+                GC_TRY(gc_build_grid(d.bbox, f->p.maxcut, d.periodic_mask, &S.mg));
+            }
             S.mcube0 = Kagg;
             Kagg += S.mg.ncells;
         } else {
             S.mg = S.g;
+            S.mlr = S.lr;
             S.mcube0 = 0;
         }
     }

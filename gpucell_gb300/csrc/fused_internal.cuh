@@ -69,6 +69,7 @@ struct SysInfo {
     float gx;                        // body force in x (ConstExtForce)
     float invL[3];
     int lr;                          // list-grid stencil radius: 2 for cells >= (rc + skin)/2, 1 for cubes >= rc + skin
+    int mlr;                         // aggregation-grid stencil radius: 2 for cubes >= MaxCut/2, 1 for cubes >= MaxCut
     GcGrid g;                        // list grid over the box
     GcGrid mg;                       // aggregation grid: cubes at least MaxCut wide
 };
