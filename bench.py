@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--rouleaux-every", type=int, default=1000)
     ap.add_argument("--rouleaux-contact", type=float, default=0.6)
     ap.add_argument("--shear-rates", type=str, default="0.005,0.05,0.5")
+    ap.add_argument("--rouleaux-temp", type=float, default=0.1,
+                    help="k_B T of the rouleaux run (the Morse adhesion of a cell contact is ~1.5 energy units)")
     ap.add_argument("--constriction-run", action="store_true",
                     help="instead of the suspension: 100 cells through a 2:1 constriction (2.0M particles), with "
                          "an FP64 host check of every cell's area and volume every --check-every steps")
@@ -431,11 +433,14 @@ ENS_METRIC = "particle-steps/s on a 64-suspension ensemble (8k-200k particles, 0
 def run_rouleaux(args):
     """Aggregation under shear: 64 cells of 2562 vertices at random positions
     and orientations in Couette flow (walls moving at -+U, Morse aggregation
-    De = 3e-3, beta = 1.5, r0 = 0.3, cut-off 2.5, thermal noise on), the same
+    De = 3e-3, beta = 1.5, r0 = 0.3, cut-off 2.5, thermal noise on at
+    k_B T = `rouleaux_temp`), the same
     initial state at each shear rate; every `rouleaux_every` steps the
     rouleaux are found on the GPU (cells in contact: a vertex pair closer than
     `rouleaux_contact`).  Steps are timed with CUDA events, the rouleau
     searches apart."""
+    import dataclasses
+
     import numpy as np
     import torch
     from gpucell_gb300 import generator
@@ -443,8 +448,10 @@ def run_rouleaux(args):
 
     runs = []
     S, E = max(1, args.rouleaux_steps), max(1, args.rouleaux_every)
+    phys = dataclasses.replace(generator.Physics(ext_force=0.0, sur_energy=3.0e-3, sca_fac=1.5, zero_len=0.3,
+                                                 max_cut=2.5), temp=args.rouleaux_temp)
     for rate in [float(x) for x in args.shear_rates.split(",") if x]:
-        cfg = generator.sheared_suspension(shear_rate=rate)
+        cfg = generator.sheared_suspension(shear_rate=rate, phys=phys)
         fs = FusedSystem(cfg, noise=args.noise, skin=0.1, compact=True, graph=args.graph)
         fs.step(3, 1)
         torch.cuda.synchronize()
@@ -483,7 +490,7 @@ def run_rouleaux(args):
                      "series_columns": ["step", "rouleaux", "largest", "mean_cells"], "series": series})
     return {"workload": "sheared_suspension", "particles": cfg.n, "fluid": cfg.n_fluid, "walls": cfg.n_b2,
             "cells": cfg.ncell, "vertices_per_cell": int(cfg.npar[0]), "steps": S, "dt": cfg.phys.dt,
-            "contact": args.rouleaux_contact, "noise": "on" if args.noise else "off",
+            "contact": args.rouleaux_contact, "noise": "on" if args.noise else "off", "kT": cfg.phys.temp,
             "captured_steps": bool(args.graph),
             "morse": {"De": cfg.phys.sur_energy, "beta": cfg.phys.sca_fac, "r0": cfg.phys.zero_len,
                       "cutoff": cfg.phys.max_cut},
