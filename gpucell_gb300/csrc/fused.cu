@@ -293,6 +293,18 @@ __device__ __forceinline__ void scan_range(const float4* __restrict__ pos, unsig
     }
 }
 
+// Gap between a coordinate and the slab of cell c along an axis (0 inside
+// it); the first and last cells of a wall axis extend to infinity.
+__device__ __forceinline__ float slab_gap(float x, int c, int axis, const GcGrid& g) {
+    const bool per = g.pmask & (1 << axis);
+    const float w = 1.f / g.invw[axis];
+    const float lo = g.origin[axis] + (float)c * w, hi = lo + w;
+    float gap = 0.f;
+    if (x < lo && (per || c > 0)) gap = lo - x;
+    else if (x > hi && (per || c < g.n[axis] - 1)) gap = x - hi;
+    return gap;
+}
+
 // One thread per slot scans the cells of its system's list grid within the
 // stencil radius R around its own (R = 2 for cells at least (rc + skin)/2
 // wide, R = 1 for cubes at least rc + skin wide; either way every pair
@@ -321,23 +333,46 @@ __global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, const SysInfo* __
     if (t != PT_B1) {
         const int R = S.lr;
         int cx = cube_coord(xi.x, 0, g), cy = cube_coord(xi.y, 1, g), cz = cube_coord(xi.z, 2, g);
+        // Rows and cells that lie wholly beyond the cut-off are not scanned:
+        // the distance from the (image of the) position to a row's y/z slab
+        // leaves a reach along x, and only the cells within it are read.
+        // The slabs are taken with a margin far above the rounding of the
+        // cell assignment, and the edge cells of a wall axis reach to
+        // infinity (particles beyond the grid are clamped into them), so no
+        // candidate within the cut-off is skipped and the lists are the same
+        // entries in the same order as a scan of all (2R+1)^3 cells.
+        const float cut = sqrtf(cut2), eps = 2e-3f;
+        const float lim2 = (cut + eps) * (cut + eps);
         for (int dz = -R; dz <= R; ++dz) {
             int z = cz + dz;
             float sz = 0.f;
             if (z < 0) { if (!(g.pmask & 4)) continue; z += g.n[2]; sz = g.L[2]; }
             else if (z >= g.n[2]) { if (!(g.pmask & 4)) continue; z -= g.n[2]; sz = -g.L[2]; }
+            const float dzv = slab_gap(xi.z + sz, z, 2, g);
+            if (dzv * dzv > lim2) continue;
             for (int dy = -R; dy <= R; ++dy) {
                 int y = cy + dy;
                 float sy = 0.f;
                 if (y < 0) { if (!(g.pmask & 2)) continue; y += g.n[1]; sy = g.L[1]; }
                 else if (y >= g.n[1]) { if (!(g.pmask & 2)) continue; y -= g.n[1]; sy = -g.L[1]; }
+                const float dyv = slab_gap(xi.y + sy, y, 1, g);
+                const float d2 = dyv * dyv + dzv * dzv;
+                if (d2 > lim2) continue;
+                // cells along x within the reach left by this row
+                const float reach = sqrtf(fmaxf(cut2 - d2, 0.f)) + eps;
+                const int xlo = max(cx - R, (int)floorf((xi.x - reach - g.origin[0]) * g.invw[0]));
+                const int xhi = min(cx + R, (int)floorf((xi.x + reach - g.origin[0]) * g.invw[0]));
                 int row = S.cube0 + g.n[0] * (y + g.n[1] * z);
-                if (cx >= R && cx + R < g.n[0]) {
-                    scan_range(pos, start[row + cx - R], start[row + cx + R + 1], f3(xi.x, xi.y + sy, xi.z + sz), i,
-                               cut2, mobile_only, fl, cap, lst, k);
+                if (xlo >= 0 && xhi < g.n[0]) {
+                    if (xlo <= xhi)
+                        scan_range(pos, start[row + xlo], start[row + xhi + 1], f3(xi.x, xi.y + sy, xi.z + sz), i,
+                                   cut2, mobile_only, fl, cap, lst, k);
                 } else {
-                    for (int dx = -R; dx <= R; ++dx) {
-                        int x = cx + dx;
+                    // near a face of the x axis: cell by cell (the edge cells
+                    // of a wall axis hold clamped particles: always scanned)
+                    const int a = (g.pmask & 1) ? xlo : cx - R, b = (g.pmask & 1) ? xhi : cx + R;
+                    for (int x0 = a; x0 <= b; ++x0) {
+                        int x = x0;
                         float sx = 0.f;
                         if (x < 0) { if (!(g.pmask & 1)) continue; x += g.n[0]; sx = g.L[0]; }
                         else if (x >= g.n[0]) { if (!(g.pmask & 1)) continue; x -= g.n[0]; sx = -g.L[0]; }
