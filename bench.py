@@ -721,8 +721,56 @@ def cpu_baseline(cfg, steps):
     for _ in range(steps):
         o.step()
     dt = time.perf_counter() - t0
+    del o
+    # one core, on a bounded sample: one step of a 1/16-size suspension with
+    # cells of the same size at about the same hematocrit (262,144
+    # particles, 12 cells)
+    from gpucell_gb300 import generator
+    small = generator.suspension(nx=64, ny=64, nz=64, ncells=12, seed=7, diameter=cell_diameter(cfg))
+    o1 = Oracle(small, noise=True, nthreads=1)
+    o1.setup()
+    t1 = time.perf_counter()
+    o1.step()
+    dt1 = time.perf_counter() - t1
     return {"value": cfg.n * steps / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} full step(s) of the {cfg.n}-particle workload, FP64, OpenMP"}
+            "sample": f"{steps} full step(s) of the {cfg.n}-particle workload, FP64, OpenMP",
+            "cpu_model": cpu_model(),
+            "one_core": {"value": small.n / dt1, "unit": "particle-steps/s",
+                         "sample": f"one step of a {small.n}-particle suspension ({small.ncell} cells of "
+                                   f"{int(small.npar[0])} vertices), FP64, 1 thread"}}
+
+
+def cell_diameter(cfg):
+    """Diameter of the first cell of a configuration (its extent), or None."""
+    import numpy as np
+    if not cfg.ncell:
+        return None
+    m = cfg.coor[cfg.n_cell_start:cfg.n_cell_start + int(cfg.npar[0])].astype(np.float64)
+    return float(np.ptp(m, axis=0).max())
+
+
+def cpu_model():
+    """The host CPU's model name (or architecture) and logical core count."""
+    import platform
+    name = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k, _, v = line.partition(":")
+                if k.strip() in ("model name", "Model", "CPU part") and v.strip():
+                    name = v.strip()
+                    break
+    except OSError:
+        pass
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=5).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                name = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return f"{name or platform.machine()}, {os.cpu_count()} logical cores"
 
 
 def run_reference(args):
