@@ -172,6 +172,11 @@ FORCE_TRAFFIC_4M = 2.845227264e9 + 0.127872512e9
 # per cycle.
 FORCE_WARP_INST_PER_PARTICLE = 345528243 / 524288
 GB300_SCHEDULERS = 152 * 4
+# FP32 operations of fk_force per particle (FADD + FMUL + 2 FFMA, thread
+# level) from the same ncu capture: 5.224e9 over 524,288 particles; the
+# FP32 peak is 152 SMs x 128 lanes x 2 (FMA) per cycle.
+FORCE_FP32_FLOP_PER_PARTICLE = 5.224e9 / 524288
+GB300_FP32_FLOP_PER_CYCLE = 152 * 128 * 2
 
 
 def measure_plain(cfg, dev, steps, warmup):
@@ -403,6 +408,17 @@ def run_ours(args):
                     / (GB300_SCHEDULERS * (clocks["sm_mhz"] if clocks else 2070.0) * 1e6),
             "note": "instructions per particle from ncu on the 524k-particle suspension; peak = 608 schedulers x "
                     "the sampled SM clock x 1 warp instruction per cycle",
+        },
+        "fp32_roofline": {
+            "kernel": "fk_force",
+            "bound": "FP32 pipe",
+            "achieved": FORCE_FP32_FLOP_PER_PARTICLE * n / (force_ms / 1e3) / 1e12,
+            "peak": GB300_FP32_FLOP_PER_CYCLE * (clocks["sm_mhz"] if clocks else 2070.0) * 1e6 / 1e12,
+            "unit": "TFLOP/s",
+            "frac": FORCE_FP32_FLOP_PER_PARTICLE * n / (force_ms / 1e3)
+                    / (GB300_FP32_FLOP_PER_CYCLE * (clocks["sm_mhz"] if clocks else 2070.0) * 1e6),
+            "note": "FP32 operations per particle (FADD + FMUL + 2 FFMA) from ncu on the 524k-particle suspension, "
+                    "~88 per acting pair; peak = 152 SMs x 128 lanes x 2 x the sampled SM clock",
         },
         "kernels_ms_per_step": {"fk_force": force_ms, "fk_density": dens_ms},
         "output_step": out_info,
