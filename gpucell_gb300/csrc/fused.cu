@@ -314,7 +314,7 @@ __device__ __forceinline__ float slab_gap(float x, int c, int axis, const GcGrid
 // periodic axes (the permutation wraps them), so each neighbouring row of
 // cells has one image shift, and the 2R + 1 cells of a row that do not wrap
 // are one contiguous range of slots.
-__global__ void __launch_bounds__(kMaxBS) fk_build_list(int n, const SysInfo* __restrict__ sys,
+__global__ void __launch_bounds__(kMaxBS, GC_BUILD_MIN_BLOCKS) fk_build_list(int n, const SysInfo* __restrict__ sys,
                                                      const int* __restrict__ sysid, const float4* __restrict__ pos,
                                                      const unsigned* __restrict__ start, int* __restrict__ nbr,
                                                      int* __restrict__ cnt, int cap, float cut2, unsigned* flags) {
