@@ -56,6 +56,25 @@ __global__ void fk_cell_stats(int c0, const int2* __restrict__ cell_verts, const
 // membrane), their count, the largest speed, and the density sum and count
 // of the fluid particles; fk_diag_final adds the blocks in order.
 constexpr int kDiagBS = 256;
+
+// Largest value over the block (non-negative inputs), on every thread.
+__device__ __forceinline__ double block_max_d(double v, double* sh) {
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
+        if (threadIdx.x == 0) sh[0] = t;
+    }
+    __syncthreads();
+    double t = sh[0];
+    __syncthreads();
+    return t;
+}
 constexpr int kDiagVals = 9;   // px py pz  2 E_kin  n_mobile  max|v|  sum rho  n_fluid  (unused)
 
 __global__ void __launch_bounds__(kDiagBS) fk_diag_partial(int count, unsigned id0, unsigned fl, unsigned cs,
@@ -84,34 +103,27 @@ __global__ void __launch_bounds__(kDiagBS) fk_diag_partial(int count, unsigned i
         }
     }
     for (int q = 0; q < kDiagVals; ++q) {
-        double x = v[q];
-        if (q == 5) {   // maximum
-#pragma unroll
-            for (int o = 16; o; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
-            if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = x;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                double m = 0.0;
-                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, sh[w]);
-                partial[(size_t)blockIdx.x * kDiagVals + q] = m;
-            }
-            __syncthreads();
-        } else {
-            double t = block_sum_d(x, sh);
-            if (threadIdx.x == 0) partial[(size_t)blockIdx.x * kDiagVals + q] = t;
-        }
+        double t = q == 5 ? block_max_d(v[q], sh) : block_sum_d(v[q], sh);
+        if (threadIdx.x == 0) partial[(size_t)blockIdx.x * kDiagVals + q] = t;
     }
 }
 
-__global__ void fk_diag_final(int nblocks, const double* __restrict__ partial, double* __restrict__ out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// One block adds the blocks' partials: thread t takes the partials t,
+// t + kDiagBS, ... in order, then a fixed tree joins the threads, so the
+// result does not depend on timing.
+__global__ void __launch_bounds__(kDiagBS) fk_diag_final(int nblocks, const double* __restrict__ partial,
+                                                        double* __restrict__ out) {
+    __shared__ double sh[32];
     double acc[kDiagVals] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int b = 0; b < nblocks; ++b)
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
         for (int q = 0; q < kDiagVals; ++q) {
             double x = partial[(size_t)b * kDiagVals + q];
             acc[q] = q == 5 ? fmax(acc[q], x) : acc[q] + x;
         }
-    for (int q = 0; q < kDiagVals; ++q) out[q] = acc[q];
+    for (int q = 0; q < kDiagVals; ++q) {
+        double t = q == 5 ? block_max_d(acc[q], sh) : block_sum_d(acc[q], sh);
+        if (threadIdx.x == 0) out[q] = t;
+    }
 }
 
 
@@ -237,7 +249,7 @@ int gc_ensemble_diagnostics(GcFused* f, int sys, double* out) {
                                               f->diag);
     GC_CHECK_LAUNCH("fused: diagnostics");
     double* res = f->diag + (size_t)nb * kDiagVals;
-    fk_diag_final<<<1, 32, 0, f->st>>>(nb, f->diag, res);
+    fk_diag_final<<<1, kDiagBS, 0, f->st>>>(nb, f->diag, res);
     GC_CHECK_LAUNCH("fused: diagnostics");
     double r[kDiagVals];
     GC_CUDA(cudaMemcpyAsync(r, res, sizeof(r), cudaMemcpyDeviceToHost, f->st), "diagnostics");
