@@ -29,6 +29,8 @@
 // follows), the per-cell means arrive precomputed (the fused step reduces
 // them on the GPU in FP64), and the text is formatted by several threads.
 #include <errno.h>
+#include <math.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <string.h>
 #include <sys/stat.h>
@@ -55,16 +57,107 @@ int mkdirs(const std::string& path) {
     return GC_OK;
 }
 
+// "%.5e" of a float without snprintf.  A finite float is k * 2^q exactly
+// (k < 2^24), so the six significant digits m = floor(|v| / 10^(X - 5)) and
+// the remainder are exact in 128-bit integers for 1e-15 <= |v| < 2^128; the
+// last digit is rounded to nearest with ties to even, as printf does with
+// the exact binary value.  Zeros are written directly; subnormals, values
+// below 1e-15, infinities and NaNs go to snprintf (returns false).
+typedef unsigned __int128 u128;
+
+struct Pow10Table {
+    u128 p[40];
+    Pow10Table() {
+        p[0] = 1;
+        for (int i = 1; i < 40; ++i) p[i] = p[i - 1] * 10u;
+    }
+};
+const Pow10Table kPow10;
+
+// m = floor(k 2^q / 10^S) and the comparison of the remainder with half the
+// divisor (-1 below, 0 equal, 1 above)
+inline void scaled_digits(uint32_t k, int q, int S, uint64_t& m, int& half) {
+    u128 N, D;
+    if (S >= 0) {
+        if (q >= 0) { N = (u128)k << q; D = kPow10.p[S]; }
+        else { N = k; D = kPow10.p[S] << (-q); }
+    } else {
+        N = (u128)k * kPow10.p[-S];
+        if (q >= 0) { N <<= q; D = 1; }
+        else D = (u128)1 << (-q);
+    }
+    u128 quo = N / D, rem = N - quo * D;
+    m = (uint64_t)quo;
+    u128 r2 = rem << 1;
+    half = r2 < D ? -1 : (r2 == D ? 0 : 1);
+}
+
+inline bool fast_e(float f, char* out, int& len) {
+    uint32_t bits;
+    memcpy(&bits, &f, 4);
+    const bool neg = bits >> 31;
+    const int ex = (int)((bits >> 23) & 0xFF);
+    const uint32_t frac = bits & 0x7FFFFFu;
+    char* p = out;
+    if (ex == 0xFF) return false;
+    if (ex == 0) {
+        if (frac) return false;   // subnormal
+        if (neg) *p++ = '-';
+        memcpy(p, "0.00000e+00", 11);
+        len = (int)(p - out) + 11;
+        return true;
+    }
+    const double a = fabs((double)f);
+    if (a < 1e-15) return false;
+    const uint32_t k = frac | 0x800000u;
+    const int q = ex - 150;
+    int X = (int)floor(log10(a));
+    uint64_t m = 0;
+    int half = -1;
+    for (int it = 0; it < 4; ++it) {
+        scaled_digits(k, q, X - 5, m, half);
+        if (m >= 1000000u) ++X;
+        else if (m < 100000u) --X;
+        else break;
+    }
+    if (m < 100000u || m >= 1000000u) return false;
+    if (half > 0 || (half == 0 && (m & 1u))) ++m;
+    if (m == 1000000u) { m = 100000u; ++X; }
+    if (neg) *p++ = '-';
+    *p++ = (char)('0' + m / 100000u);
+    *p++ = '.';
+    uint32_t r = (uint32_t)(m % 100000u);
+    for (int d = 4; d >= 0; --d) { p[d] = (char)('0' + r % 10u); r /= 10u; }
+    p += 5;
+    *p++ = 'e';
+    *p++ = X < 0 ? '-' : '+';
+    int ax = X < 0 ? -X : X;
+    if (ax >= 100) { *p++ = (char)('0' + ax / 100); ax %= 100; }
+    *p++ = (char)('0' + ax / 10);
+    *p++ = (char)('0' + ax % 10);
+    len = (int)(p - out);
+    return true;
+}
+
 inline void put_e(std::string& s, float v, int width) {
     char b[64];
-    int k = snprintf(b, sizeof b, "%-*.5e", width, (double)v);
+    int k;
+    if (!fast_e(v, b, k)) k = snprintf(b, sizeof b, "%.5e", (double)v);
     s.append(b, (size_t)k);
+    if (k < width) s.append((size_t)(width - k), ' ');
 }
 
 inline void put_d(std::string& s, long long v, int width) {
-    char b[64];
-    int k = snprintf(b, sizeof b, "%-*lld", width, v);
+    char b[32];
+    int k = 0;
+    unsigned long long u = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    char t[24];
+    int n = 0;
+    do { t[n++] = (char)('0' + u % 10u); u /= 10u; } while (u);
+    if (v < 0) b[k++] = '-';
+    while (n) b[k++] = t[--n];
     s.append(b, (size_t)k);
+    if (k < width) s.append((size_t)(width - k), ' ');
 }
 
 inline void put_padded(std::string& s, const char* text, int width) {

@@ -137,3 +137,47 @@ def test_bad_frames_are_refused(built_library, tmp_path):
     fr["tri"][0, 0] = 7           # a vertex of the other cell
     with pytest.raises(_lib.GcError, match="vertex of another cell"):
         write_frame(str(tmp_path), 0, 0.0, True, **fr)
+
+
+def _hard_floats(seed=3):
+    """Floats that stress a %.5e formatter: random bit patterns over the whole
+    exponent range, decimal ties at the sixth digit (integers n*10+5 below
+    2^24 and their binary scalings), powers of ten and their neighbours, the
+    float extremes, subnormals, signed zeros, infinities and NaN."""
+    rng = np.random.default_rng(seed)
+    bits = rng.integers(0, 2**32, size=60000, dtype=np.uint64).astype(np.uint32)
+    vals = [bits.view(np.float32)]
+    ties = (rng.integers(100000, 1677721, size=4000) * 10 + 5).astype(np.float32)
+    vals += [ties, ties * np.float32(2.0**-20), ties * np.float32(2.0**30), -ties]
+    p10 = np.array([10.0**e for e in range(-15, 39)], np.float64).astype(np.float32)
+    vals += [p10, np.nextafter(p10, np.float32(np.inf)), np.nextafter(p10, np.float32(0)), -p10]
+    fi = np.finfo(np.float32)
+    vals.append(np.array([0.0, -0.0, fi.max, -fi.max, fi.tiny, fi.tiny * np.float32(0.5), 1e-16, 9.999995e-16,
+                          np.inf, -np.inf, np.nan, 999999.5, 9.999995, 0.9999995, 1.0, -1.0], np.float32))
+    return np.concatenate(vals).astype(np.float32)
+
+
+def test_float_formatting_matches_printf(built_library, tmp_path):
+    """The writer formats floats itself (exact integer arithmetic for the six
+    digits); every value must come out as printf's %-20.5e would write it."""
+    v = _hard_floats()
+    n = v.size // 3 * 3
+    pos = v[:n].reshape(-1, 3)
+    m = pos.shape[0]
+    fr = dict(pos=pos, vel=np.zeros((m, 3), np.float32), rho=np.zeros(m, np.float32), press=np.zeros(m, np.float32),
+              n_b1=0, n_b2=0, n_cell_start=m, cell_verts=np.zeros((0, 2), np.int32), tri=np.zeros((0, 3), np.int32),
+              betri=np.zeros((0, 2), np.int32), defforce=np.zeros((0, 3), np.float32),
+              aggforce=np.zeros((0, 3), np.float32), tricenter=np.zeros((0, 3), np.float32),
+              trinordir=np.zeros((0, 3), np.float32), cell_stats=np.zeros((0, 12)))
+    d = str(tmp_path / "Result")
+    write_frame(d, 0, 0.0, True, **fr)
+    got = _lines(os.path.join(d, "FluidCoor", "0.plt"))[3:]
+    assert len(got) == m
+    def c_e20(x):   # printf writes a NaN with its sign bit set as -nan (Python: nan)
+        if np.isnan(x):
+            return "%-20s" % ("-nan" if np.signbit(x) else "nan")
+        return e20(x)
+
+    for i in range(m):
+        want = c_e20(pos[i, 0]) + c_e20(pos[i, 1]) + c_e20(pos[i, 2]) + d20(i)
+        assert got[i] == want, (i, pos[i], got[i], want)
