@@ -37,6 +37,8 @@
 #include <sys/types.h>
 
 #include <algorithm>
+#include <atomic>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -166,33 +168,6 @@ inline void put_padded(std::string& s, const char* text, int width) {
     s.append(b, (size_t)k);
 }
 
-// Formats lines [0, count) with `line(i, out)` on several threads and
-// returns the text in order.
-template <class F>
-std::string format_lines(long long count, int threads, F line) {
-    if (count <= 0) return std::string();
-    int t = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
-    if (t < 1) t = 1;
-    if (count < 20000) t = 1;
-    std::vector<std::string> parts(t);
-    auto work = [&](int w) {
-        long long b = count * w / t, e = count * (w + 1) / t;
-        std::string& s = parts[w];
-        s.reserve((size_t)(e - b) * 96);
-        for (long long i = b; i < e; ++i) line(i, s);
-    };
-    std::vector<std::thread> pool;
-    for (int w = 1; w < t; ++w) pool.emplace_back(work, w);
-    work(0);
-    for (auto& th : pool) th.join();
-    size_t total = 0;
-    for (auto& p : parts) total += p.size();
-    std::string out;
-    out.reserve(total);
-    for (auto& p : parts) out += p;
-    return out;
-}
-
 struct File {
     FILE* fp = nullptr;
     bool ok = true;
@@ -209,10 +184,67 @@ struct File {
     }
 };
 
+// Formats `ntasks` pieces of text with `task(i, out)` on a pool of threads
+// (taken in order from a shared counter) and writes them to f in order: the
+// calling thread writes piece i as soon as it is done and formats pending
+// pieces itself while it waits, so writing overlaps formatting and each
+// piece's memory is released once written.
+template <class F>
+void emit_ordered(File& f, long long ntasks, int threads, F task) {
+    if (ntasks <= 0) return;
+    int t = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+    if (t < 1) t = 1;
+    if ((long long)t > ntasks) t = (int)ntasks;
+    std::vector<std::string> out((size_t)ntasks);
+    std::unique_ptr<std::atomic<int>[]> done(new std::atomic<int>[(size_t)ntasks]);
+    for (long long i = 0; i < ntasks; ++i) done[i].store(0, std::memory_order_relaxed);
+    std::atomic<long long> next{0};
+    auto run_one = [&]() -> bool {
+        long long i = next.fetch_add(1);
+        if (i >= ntasks) return false;
+        task(i, out[(size_t)i]);
+        done[i].store(1, std::memory_order_release);
+        return true;
+    };
+    std::vector<std::thread> pool;
+    for (int w = 1; w < t; ++w)
+        pool.emplace_back([&] {
+            while (run_one()) {
+            }
+        });
+    for (long long i = 0; i < ntasks; ++i) {
+        while (!done[i].load(std::memory_order_acquire))
+            if (!run_one()) std::this_thread::yield();
+        f.put(out[(size_t)i]);
+        std::string().swap(out[(size_t)i]);
+    }
+    for (auto& th : pool) th.join();
+}
+
+// Lines [0, count) as pieces of kLinesPerPiece lines, `line(i, s)` each.
+constexpr long long kLinesPerPiece = 16384;
+
+template <class F>
+void emit_lines(File& f, long long count, int threads, size_t line_bytes, F line) {
+    const long long pieces = (count + kLinesPerPiece - 1) / kLinesPerPiece;
+    emit_ordered(f, pieces, threads, [&](long long p, std::string& s) {
+        const long long b = p * kLinesPerPiece, e = std::min(count, b + kLinesPerPiece);
+        s.reserve((size_t)(e - b) * line_bytes);
+        for (long long i = b; i < e; ++i) line(i, s);
+    });
+}
+
 int fail_write(const std::string& path) { return gc_fail(GC_EINVAL, "output: cannot write %s", path.c_str()); }
 
 std::string step_file(const std::string& dir, const char* sub, long long step) {
     return dir + "/" + sub + "/" + std::to_string(step) + ".plt";
+}
+
+std::string zone_line() {
+    std::string zone;
+    put_padded(zone, "Zone", 20);
+    zone += '\n';
+    return zone;
 }
 
 int write_coor(const GcOutputFrame& fr, const std::string& dir, long long step, int threads) {
@@ -226,19 +258,16 @@ int write_coor(const GcOutputFrame& fr, const std::string& dir, long long step, 
     const long long hi[4] = {fr.n_b1, b12, fr.n_cell_start, fr.n};
     for (int z = 0; z < 4; ++z) {
         if (hi[z] <= lo[z]) continue;
-        std::string zone;
-        put_padded(zone, "Zone", 20);
-        zone += '\n';
-        f.put(zone);
+        f.put(zone_line());
         const long long base = lo[z];
-        f.put(format_lines(hi[z] - lo[z], threads, [&](long long k, std::string& s) {
+        emit_lines(f, hi[z] - lo[z], threads, 81, [&](long long k, std::string& s) {
             long long i = base + k;
             put_e(s, fr.pos[3 * i], 20);
             put_e(s, fr.pos[3 * i + 1], 20);
             put_e(s, fr.pos[3 * i + 2], 20);
             put_d(s, i, 20);
             s += '\n';
-        }));
+        });
     }
     return f.close() ? GC_OK : fail_write(path);
 }
@@ -249,7 +278,7 @@ int write_field(const GcOutputFrame& fr, const std::string& dir, long long step,
     if (!f.ok) return fail_write(path);
     f.put("Title=\"Particle Fluid\"\n");
     f.put("Variables=\"x\",\"y\",\"z\",\"Den\",\"Press\",\"Vx\",\"Vy\",\"Vz\"\n");
-    f.put(format_lines(fr.n_cell_start, threads, [&](long long i, std::string& s) {
+    emit_lines(f, fr.n_cell_start, threads, 161, [&](long long i, std::string& s) {
         put_e(s, fr.pos[3 * i], 20);
         put_e(s, fr.pos[3 * i + 1], 20);
         put_e(s, fr.pos[3 * i + 2], 20);
@@ -259,11 +288,12 @@ int write_field(const GcOutputFrame& fr, const std::string& dir, long long step,
         put_e(s, fr.vel[3 * i + 1], 20);
         put_e(s, fr.vel[3 * i + 2], 20);
         s += '\n';
-    }));
+    });
     return f.close() ? GC_OK : fail_write(path);
 }
 
-// CellCoor (forces = false) or CellForce (forces = true).
+// CellCoor (forces = false) or CellForce (forces = true): one piece per cell
+// (its zone line, vertices, then triangles as zone-local vertex numbers).
 int write_cells(const GcOutputFrame& fr, const std::string& dir, long long step, int threads, bool forces) {
     std::string path = step_file(dir, forces ? "CellForce" : "CellCoor", step);
     File f(path, "w");
@@ -271,14 +301,15 @@ int write_cells(const GcOutputFrame& fr, const std::string& dir, long long step,
     f.put(forces ? "Title=\"Particle Force\"\n" : "Title=\"Particle Coordinate\"\n");
     f.put(forces ? "Variables=\"x\",\"y\",\"z\", \"DFx\",\"DFy\",\"DFz\",\"AFx\",\"AFy\",\"AFz\"\n"
                  : "Variables=\"x\",\"y\",\"z\"\n");
-    for (int c = 0; c < fr.ncell; ++c) {
+    emit_ordered(f, fr.ncell, threads, [&](long long c, std::string& s) {
         const int v0 = fr.cell_verts[2 * c], v1 = fr.cell_verts[2 * c + 1] + 1;
         const int t0 = fr.betri[2 * c], t1 = fr.betri[2 * c + 1];
+        s.reserve((size_t)(v1 - v0) * (forces ? 181 : 61) + (size_t)(t1 - t0 + 1) * 61 + 64);
         char head[160];
-        snprintf(head, sizeof head, "Zone N=%d, E=%d, F=FEPOINT, ET=TRIANGLE\n", v1 - v0, t1 - t0 + 1);
-        f.put(head);
-        f.put(format_lines(v1 - v0, threads, [&](long long k, std::string& s) {
-            long long m = v0 + k, i = fr.n_cell_start + m;
+        int k = snprintf(head, sizeof head, "Zone N=%d, E=%d, F=FEPOINT, ET=TRIANGLE\n", v1 - v0, t1 - t0 + 1);
+        s.append(head, (size_t)k);
+        for (long long m = v0; m < v1; ++m) {
+            long long i = fr.n_cell_start + m;
             put_e(s, fr.pos[3 * i], 20);
             put_e(s, fr.pos[3 * i + 1], 20);
             put_e(s, fr.pos[3 * i + 2], 20);
@@ -287,13 +318,12 @@ int write_cells(const GcOutputFrame& fr, const std::string& dir, long long step,
                 for (int a = 0; a < 3; ++a) put_e(s, fr.aggforce[3 * m + a], 20);
             }
             s += '\n';
-        }));
-        f.put(format_lines(t1 - t0 + 1, threads, [&](long long k, std::string& s) {
-            long long t = t0 + k;
+        }
+        for (long long t = t0; t <= t1; ++t) {
             for (int a = 0; a < 3; ++a) put_d(s, (long long)fr.tri[3 * t + a] - 1 - v0 + 1, 20);
             s += '\n';
-        }));
-    }
+        }
+    });
     return f.close() ? GC_OK : fail_write(path);
 }
 
@@ -303,20 +333,18 @@ int write_nordir(const GcOutputFrame& fr, const std::string& dir, long long step
     if (!f.ok) return fail_write(path);
     f.put("Title=\"Triangle information\"\n");
     f.put("Variables=\"Cenx\",\"Ceny\",\"Cenz\",\"Norx\",\"Nory\",\"Norz\",\"ID\"\n");
-    for (int c = 0; c < fr.ncell; ++c) {
+    const std::string zone = zone_line();
+    emit_ordered(f, fr.ncell, threads, [&](long long c, std::string& s) {
         const int t0 = fr.betri[2 * c], t1 = fr.betri[2 * c + 1];
-        std::string zone;
-        put_padded(zone, "Zone", 20);
-        zone += '\n';
-        f.put(zone);
-        f.put(format_lines(t1 - t0 + 1, threads, [&](long long k, std::string& s) {
-            long long t = t0 + k;
+        s.reserve(zone.size() + (size_t)(t1 - t0 + 1) * 141);
+        s += zone;
+        for (long long t = t0; t <= t1; ++t) {
             for (int a = 0; a < 3; ++a) put_e(s, fr.tricenter[3 * t + a], 20);
             for (int a = 0; a < 3; ++a) put_e(s, fr.trinordir[3 * t + a], 20);
             put_d(s, t, 20);
             s += '\n';
-        }));
-    }
+        }
+    });
     return f.close() ? GC_OK : fail_write(path);
 }
 
