@@ -2273,10 +2273,14 @@ int gc_ensemble_set_cells(GcFused* f, int sys, int ncell, int ntri, int nedge, c
         return gc_fail(GC_EINVAL, "set_cells: NULL array");
     for (int k = 0; k < 3 * ntri; ++k)
         if (tri[k] < 1 || tri[k] > ncp) return gc_fail(GC_EINVAL, "set_cells: triangle index out of range");
-    for (int k = 0; k < nedge; ++k)
+    for (int k = 0; k < nedge; ++k) {
         for (int q = 0; q < 4; ++q)
             if (edge[6 * k + q] < 1 || edge[6 * k + q] > ncp)
                 return gc_fail(GC_EINVAL, "set_cells: edge index out of range");
+        for (int q = 4; q < 6; ++q)
+            if (edge[6 * k + q] < 1 || edge[6 * k + q] > ntri)
+                return gc_fail(GC_EINVAL, "set_cells: edge triangle index out of range");
+    }
     for (int k = 0; k < ncell; ++k)
         if (betri[2 * k] < 0 || betri[2 * k + 1] >= ntri || betri[2 * k + 1] < betri[2 * k])
             return gc_fail(GC_EINVAL, "set_cells: bad triangle range of cell %d", k);
