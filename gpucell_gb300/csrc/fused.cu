@@ -159,7 +159,7 @@ __global__ void fk_integrate(int n, GcParams p, SysInfo s0, const SysInfo* __res
                              float4* __restrict__ vh, float4* __restrict__ vpred, const float4* __restrict__ force,
                              float4* __restrict__ plo, const float4* __restrict__ refpos, int4* __restrict__ nthro,
                              float half_skin2, int* __restrict__ rebuild, float4* __restrict__ mpos,
-                             int4* __restrict__ mnthro, unsigned* flags) {
+                             float4* __restrict__ mplo, int4* __restrict__ mnthro, unsigned* flags) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool far = false;
     if (i < n) {
@@ -199,6 +199,7 @@ __global__ void fk_integrate(int n, GcParams p, SysInfo s0, const SysInfo* __res
             if (id >= S.cs) {
                 unsigned m = S.m0 + (id - S.cs);
                 mpos[m] = x;
+                mplo[m] = lo;
                 mnthro[m] = t;
             }
         }
@@ -687,21 +688,37 @@ __global__ void fk_wallvel(int n, GcParams p, SysInfo s0, const SysInfo* __restr
 // Vertex, triangle and cell indices are global over the ensemble; msys and
 // cellsys give the system of a vertex and of a cell (nullptr: system 0).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float3 mdiff(const float4* mpos, const int4* mnt, int a, int b, const GcGrid& g) {
-    float4 xa = mpos[a], xb = mpos[b];
-    int4 ta = mnt[a], tb = mnt[b];
-    float3 d = f3(xa.x - xb.x, xa.y - xb.y, xa.z - xb.z);
-    if (g.pmask & 1) d.x += (float)(ta.x - tb.x) * g.L[0];
-    if (g.pmask & 2) d.y += (float)(ta.y - tb.y) * g.L[1];
-    if (g.pmask & 4) d.z += (float)(ta.z - tb.z) * g.L[2];
-    return d;
+// (a + la) - (b + lb) + k L along one axis for double-float positions
+// (value a, low part la) and crossing counts differing by k: the rounding
+// errors of a - b, of k L and of adding it are kept by TwoSum / FMA and
+// added with the low parts at the end, so the result is the difference of
+// the exact positions rounded once.  A cell's geometry is then the same
+// whether its vertices are wrapped into the box or not.
+__device__ __forceinline__ float dd_sub1(float a, float la, float b, float lb, int k, float L) {
+    const float nb = -b;
+    const float s = __fadd_rn(a, nb), s1 = __fsub_rn(s, a);
+    const float e1 = __fadd_rn(__fsub_rn(a, __fsub_rn(s, s1)), __fsub_rn(nb, s1));
+    const float sh = __fmul_rn((float)k, L), esh = fmaf((float)k, L, -sh);
+    const float t = __fadd_rn(s, sh), t1 = __fsub_rn(t, s);
+    const float e2 = __fadd_rn(__fsub_rn(s, __fsub_rn(t, t1)), __fsub_rn(sh, t1));
+    return __fadd_rn(t, __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(esh, __fsub_rn(la, lb))));
+}
+
+__device__ __forceinline__ float3 mdiff(const float4* mpos, const float4* mplo, const int4* mnt, int a, int b,
+                                        const GcGrid& g) {
+    const float4 xa = mpos[a], xb = mpos[b], la = mplo[a], lb = mplo[b];
+    const int4 ta = mnt[a], tb = mnt[b];
+    return f3(dd_sub1(xa.x, la.x, xb.x, lb.x, (g.pmask & 1) ? ta.x - tb.x : 0, g.L[0]),
+              dd_sub1(xa.y, la.y, xb.y, lb.y, (g.pmask & 2) ? ta.y - tb.y : 0, g.L[1]),
+              dd_sub1(xa.z, la.z, xb.z, lb.z, (g.pmask & 4) ? ta.z - tb.z : 0, g.L[2]));
 }
 
 
 // Triangle geometry and per-cell area/volume (FP64 sums), one block per cell.
 __global__ void fk_mgeo(GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ cellsys, int ncell,
                         int ntri, const int3* __restrict__ tri, const int2* __restrict__ betri,
-                        const float4* __restrict__ mpos, const int4* __restrict__ mnt, float* __restrict__ tarea,
+                        const float4* __restrict__ mpos, const float4* __restrict__ mplo,
+                        const int4* __restrict__ mnt, float* __restrict__ tarea,
                         float4* __restrict__ tnorm, float4* __restrict__ tcen, float* __restrict__ reftarea,
                         double* __restrict__ carea, double* __restrict__ cvol, double* __restrict__ crefarea,
                         double* __restrict__ crefvol, int setup, unsigned* flags) {
@@ -734,8 +751,8 @@ __global__ void fk_mgeo(GcParams p, const SysInfo* __restrict__ sys, const int* 
             tarea[t] = 0.f;
             continue;
         }
-        float3 u1 = mdiff(mpos, mnt, a, r, g);
-        float3 e1 = mdiff(mpos, mnt, b, a, g), e2 = mdiff(mpos, mnt, cc, a, g);
+        float3 u1 = mdiff(mpos, mplo, mnt, a, r, g);
+        float3 e1 = mdiff(mpos, mplo, mnt, b, a, g), e2 = mdiff(mpos, mplo, mnt, cc, a, g);
         float3 xi = cross3(e1, e2);
         float len = sqrtf(dot3(xi, xi));
         float A = 0.5f * len;
@@ -797,7 +814,8 @@ __device__ __forceinline__ bool edge_ok(int6 E, int ncp, int* a, int* b, int* c,
 
 __global__ void fk_mech_setup(GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ msys, int nedge,
                               const int6* __restrict__ edge, const float4* __restrict__ mpos,
-                              const int4* __restrict__ mnt, const float* __restrict__ shear,
+                              const float4* __restrict__ mplo, const int4* __restrict__ mnt,
+                              const float* __restrict__ shear,
                               const float* __restrict__ bend, float* __restrict__ l0a, float* __restrict__ lmax,
                               float* __restrict__ perlen, float* __restrict__ hpow, float* __restrict__ hbend,
                               float* __restrict__ refang, unsigned* flags) {
@@ -809,7 +827,7 @@ __global__ void fk_mech_setup(GcParams p, const SysInfo* __restrict__ sys, const
         return;
     }
     const GcGrid& g = sys[msys ? msys[a] : 0].g;
-    float3 xb = mdiff(mpos, mnt, b, a, g), xc = mdiff(mpos, mnt, c, a, g), xd = mdiff(mpos, mnt, d, a, g);
+    float3 xb = mdiff(mpos, mplo, mnt, b, a, g), xc = mdiff(mpos, mplo, mnt, c, a, g), xd = mdiff(mpos, mplo, mnt, d, a, g);
     float l0 = sqrtf(dot3(xb, xb));
     const float x0 = 1.f / 2.2f, m = 2.f;
     float u = 1.f - x0;
@@ -835,8 +853,8 @@ __global__ void fk_mech_setup(GcParams p, const SysInfo* __restrict__ sys, const
 __device__ __forceinline__ float4 part(float3 f) { return make_float4(f.x, f.y, f.z, 0.f); }
 
 __global__ void fk_medge(GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ msys, int nedge,
-                         const int6* __restrict__ edge, const float4* __restrict__ mpos, const int4* __restrict__ mnt,
-                         const float* __restrict__ lmax, const float* __restrict__ perlen,
+                         const int6* __restrict__ edge, const float4* __restrict__ mpos,
+                         const float4* __restrict__ mplo, const int4* __restrict__ mnt, const float* __restrict__ l0a, const float* __restrict__ lmax, const float* __restrict__ perlen,
                          const float* __restrict__ hpow, const float* __restrict__ refang,
                          const float* __restrict__ hbend, float4* __restrict__ parts, unsigned* flags) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -850,18 +868,32 @@ __global__ void fk_medge(GcParams p, const SysInfo* __restrict__ sys, const int*
     }
     const GcGrid& g = sys[msys ? msys[a] : 0].g;
     float3 z = f3(0.f, 0.f, 0.f);
-    float3 xb = mdiff(mpos, mnt, b, a, g), xc = mdiff(mpos, mnt, c, a, g), xd = mdiff(mpos, mnt, d, a, g);
+    float3 xb = mdiff(mpos, mplo, mnt, b, a, g), xc = mdiff(mpos, mplo, mnt, c, a, g), xd = mdiff(mpos, mplo, mnt, d, a, g);
     float3 f1 = z, f2 = z, f3v = z, f4 = z;
     float pl = perlen[e];
     float r = sqrtf(dot3(xb, xb));
     if (pl > 0.f && r > 0.f) {
-        float x = r / lmax[e];
+        const float lm = lmax[e];
+        float x = r / lm;
+        float fm;
         if (x >= 0.99f) {
             raise_flag(flags, GC_FLAG_STRETCH);
             x = 0.99f;
+            float u = 1.f - x;
+            fm = -(p.kT / pl) * (1.f / (4.f * u * u) - 0.25f + x) + hpow[e] / (r * r);   // power index 2
+        } else {
+            // The WLC and POW terms are large and cancel at the rest length
+            // l0 (hpow is set so); the same force with the factor r - l0
+            // taken out has no cancellation, and is exactly zero at rest:
+            // fm = (kT/p)(r - l0) [-(1/lmax)((2 - x - x0) / (4 u^2 u0^2) + 1)
+            //                      - kwlc (l0 + r) / r^2],  x0 = l0/lmax,
+            // kwlc = 1/(4 u0^2) - 1/4 + x0, u = 1 - x, u0 = 1 - x0.
+            const float l0 = l0a[e], x0 = l0 / lm;
+            const float u = 1.f - x, u0 = 1.f - x0;
+            const float kwlc = 1.f / (4.f * u0 * u0) - 0.25f + x0;
+            const float dwlc = (2.f - x - x0) / (4.f * u * u * u0 * u0) + 1.f;
+            fm = (p.kT / pl) * (r - l0) * (-dwlc / lm - kwlc * (l0 + r) / (r * r));
         }
-        float u = 1.f - x;
-        float fm = -(p.kT / pl) * (1.f / (4.f * u * u) - 0.25f + x) + hpow[e] / (r * r);   // power index 2
         float3 eh = (-1.f / r) * xb;
         f1 += fm * eh;
         f2 -= fm * eh;
@@ -885,7 +917,8 @@ __global__ void fk_medge(GcParams p, const SysInfo* __restrict__ sys, const int*
 
 __global__ void fk_mtri(GcParams p, const SysInfo* __restrict__ sys, const int* __restrict__ cellsys, int ncell,
                         const int2* __restrict__ betri, const int3* __restrict__ tri, const float4* __restrict__ mpos,
-                        const int4* __restrict__ mnt, const float* __restrict__ reftarea,
+                        const float4* __restrict__ mplo, const int4* __restrict__ mnt,
+                        const float* __restrict__ reftarea,
                         const float* __restrict__ hl, const float* __restrict__ hg, const float* __restrict__ hv,
                         const double* __restrict__ carea, const double* __restrict__ cvol,
                         const double* __restrict__ crefarea, const double* __restrict__ crefvol,
@@ -904,7 +937,7 @@ __global__ void fk_mtri(GcParams p, const SysInfo* __restrict__ sys, const int* 
         float4* out = parts + 3 * (size_t)t;
         out[0] = out[1] = out[2] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (a < 0 || b < 0 || cc < 0 || a >= ncp || b >= ncp || cc >= ncp) continue;
-        float3 x2 = mdiff(mpos, mnt, b, a, g), x3 = mdiff(mpos, mnt, cc, a, g);
+        float3 x2 = mdiff(mpos, mplo, mnt, b, a, g), x3 = mdiff(mpos, mplo, mnt, cc, a, g);
         float3 xi = cross3(x2, x3);
         float len = sqrtf(dot3(xi, xi));
         if (!(len > 0.f)) continue;
@@ -1091,7 +1124,7 @@ __global__ void fk_load(int count, unsigned id_base, const SysInfo* __restrict__
                         const float* __restrict__ f, const int* __restrict__ nt, int* __restrict__ slot_of,
                         float4* __restrict__ pos, float4* __restrict__ plo, float4* __restrict__ vel,
                         float4* __restrict__ vh, float4* __restrict__ force, int4* __restrict__ nthro,
-                        float4* __restrict__ mpos, int4* __restrict__ mnthro) {
+                        float4* __restrict__ mpos, float4* __restrict__ mplo, int4* __restrict__ mnthro) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count) return;
     unsigned id = id_base + k;
@@ -1118,6 +1151,7 @@ __global__ void fk_load(int count, unsigned id_base, const SysInfo* __restrict__
         const SysInfo& S = sys[find_sys(sys, nsys, id)];
         if (id >= S.cs) {
             mpos[S.m0 + id - S.cs] = a;
+            mplo[S.m0 + id - S.cs] = z;
             mnthro[S.m0 + id - S.cs] = t;
         }
     }
@@ -1126,12 +1160,14 @@ __global__ void fk_load(int count, unsigned id_base, const SysInfo* __restrict__
 // Membrane-ordered positions from the slots (set-up).
 __global__ void fk_gather_mpos(int ncp, const SysInfo* __restrict__ sys, const int* __restrict__ msys,
                                const int* __restrict__ slot_of, const float4* __restrict__ pos,
-                               const int4* __restrict__ nthro, float4* __restrict__ mpos, int4* __restrict__ mnthro) {
+                               const int4* __restrict__ nthro, const float4* __restrict__ plo,
+                               float4* __restrict__ mpos, float4* __restrict__ mplo, int4* __restrict__ mnthro) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= ncp) return;
     const SysInfo& S = sys[msys ? msys[m] : 0];
     int i = slot_of[S.cs + (unsigned)(m - (int)S.m0)];
     mpos[m] = pos[i];
+    mplo[m] = plo[i];
     mnthro[m] = nthro[i];
 }
 
@@ -1413,11 +1449,11 @@ int launch_integrate(GcFused* f, cudaStream_t st, const GcParams& p) {
     if (f->ens)
         fk_integrate<true><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vel, f->a.vh,
                                                      f->a.vpred, f->a.force, f->a.plo, f->refpos, f->a.nthro,
-                                                     hs * hs, f->rebuild, f->mpos, f->mnthro, f->flags);
+                                                     hs * hs, f->rebuild, f->mpos, f->mplo, f->mnthro, f->flags);
     else
         fk_integrate<false><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vel, f->a.vh,
                                                       f->a.vpred, f->a.force, f->a.plo, f->refpos, f->a.nthro,
-                                                      hs * hs, f->rebuild, f->mpos, f->mnthro, f->flags);
+                                                      hs * hs, f->rebuild, f->mpos, f->mplo, f->mnthro, f->flags);
     GC_CHECK_LAUNCH("fused: integrate");
     return GC_OK;
 }
@@ -1438,15 +1474,17 @@ int launch_density(GcFused* f, cudaStream_t st, const GcParams& p, bool mark) {
 
 int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p) {
     if (f->ncell <= 0) return GC_OK;
-    fk_mgeo<<<f->ncell, 256, 0, st>>>(p, f->dsys, f->cellsys, f->ncell, f->ntri, f->tri, f->betri, f->mpos, f->mnthro,
+    fk_mgeo<<<f->ncell, 256, 0, st>>>(p, f->dsys, f->cellsys, f->ncell, f->ntri, f->tri, f->betri, f->mpos, f->mplo,
+                                      f->mnthro,
                                      f->tarea, f->tnorm, f->tcen, f->reftarea, f->carea, f->cvol, f->crefarea,
                                      f->crefvol, 0, f->flags);
     GC_CHECK_LAUNCH("fused: membrane geometry");
     fk_medge<<<gc_blocks(f->nedge, f->block), f->block, 0, st>>>(p, f->dsys, f->msys, f->nedge, f->edge, f->mpos,
-                                                                 f->mnthro, f->lmax, f->perlen, f->hpow, f->refang,
+                                                                 f->mplo, f->mnthro, f->l0, f->lmax, f->perlen, f->hpow, f->refang,
                                                                  f->hbend, f->mparts, f->flags);
     GC_CHECK_LAUNCH("fused: membrane edges");
-    fk_mtri<<<f->ncell, 256, 0, st>>>(p, f->dsys, f->cellsys, f->ncell, f->betri, f->tri, f->mpos, f->mnthro,
+    fk_mtri<<<f->ncell, 256, 0, st>>>(p, f->dsys, f->cellsys, f->ncell, f->betri, f->tri, f->mpos, f->mplo,
+                                      f->mnthro,
                                      f->reftarea, f->hl, f->hg, f->hv, f->carea, f->cvol, f->crefarea, f->crefvol,
                                      f->mparts + 4 * (size_t)f->nedge, f->ntri);
     GC_CHECK_LAUNCH("fused: membrane triangles");
@@ -1674,6 +1712,7 @@ int alloc_copy(GcFused* f, StateCopy* c) {
     if (f->a.sys) GC_TRY(falloc(f, &c->s.sys, n));
     if (f->ncp > 0) {
         GC_TRY(falloc(f, &c->mpos, f->ncp));
+        GC_TRY(falloc(f, &c->mplo, f->ncp));
         GC_TRY(falloc(f, &c->mnthro, f->ncp));
     }
     GC_TRY(falloc(f, &c->dstep, 1));
@@ -1681,8 +1720,9 @@ int alloc_copy(GcFused* f, StateCopy* c) {
     return GC_OK;
 }
 
-int copy_state(GcFused* f, const SlotArrays& src, const float4* mpos, const int4* mnt, const long long* dstep,
-               SlotArrays& dst, float4* dmpos, int4* dmnt, long long* ddstep) {
+int copy_state(GcFused* f, const SlotArrays& src, const float4* mpos, const float4* mplo, const int4* mnt,
+               const long long* dstep, SlotArrays& dst, float4* dmpos, float4* dmplo, int4* dmnt,
+               long long* ddstep) {
     cudaStream_t st = f->st;
     size_t n = f->n;
     auto cp = [&](void* d, const void* s, size_t bytes) -> int {
@@ -1699,6 +1739,7 @@ int copy_state(GcFused* f, const SlotArrays& src, const float4* mpos, const int4
     GC_TRY(cp(dst.nthro, src.nthro, n * 16));
     GC_TRY(cp(dst.sys, src.sys, n * 4));
     GC_TRY(cp(dmpos, mpos, (size_t)f->ncp * 16));
+    GC_TRY(cp(dmplo, mplo, (size_t)f->ncp * 16));
     GC_TRY(cp(dmnt, mnt, (size_t)f->ncp * 16));
     GC_TRY(cp(ddstep, dstep, 8));
     return GC_OK;
@@ -1706,11 +1747,11 @@ int copy_state(GcFused* f, const SlotArrays& src, const float4* mpos, const int4
 
 int save_state(GcFused* f, StateCopy* c) {
     GC_TRY(alloc_copy(f, c));
-    return copy_state(f, f->a, f->mpos, f->mnthro, f->dstep, c->s, c->mpos, c->mnthro, c->dstep);
+    return copy_state(f, f->a, f->mpos, f->mplo, f->mnthro, f->dstep, c->s, c->mpos, c->mplo, c->mnthro, c->dstep);
 }
 
 int restore_state(GcFused* f, StateCopy* c) {
-    return copy_state(f, c->s, c->mpos, c->mnthro, c->dstep, f->a, f->mpos, f->mnthro, f->dstep);
+    return copy_state(f, c->s, c->mpos, c->mplo, c->mnthro, c->dstep, f->a, f->mpos, f->mplo, f->mnthro, f->dstep);
 }
 
 // Re-sort and rebuild outside a step, then recompute what the outputs show
@@ -2018,7 +2059,8 @@ int load_range(GcFused* f, unsigned id_base, int count, const float* pos, const 
     fk_load<<<gc_blocks(count, f->block), f->block, 0, st>>>(count, id_base, f->dsys, f->nsys, keep, dx, dv, dh, df,
                                                              dn, f->slot_of, f->a.pos, f->a.plo, f->a.vel, f->a.vh,
                                                              f->a.force, f->a.nthro,
-                                                             keep && f->ncell > 0 ? f->mpos : nullptr, f->mnthro);
+                                                             keep && f->ncell > 0 ? f->mpos : nullptr, f->mplo,
+                                                             f->mnthro);
     GC_CHECK_LAUNCH("fused: load");
     if (!from_device) GC_CUDA(cudaStreamSynchronize(st), "fused_load");   // the staging buffer is reused
     return GC_OK;
@@ -2194,6 +2236,7 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
     if (ok == GC_OK) ok = falloc(f, &f->drebuilds, 1);
     if (ok == GC_OK) ok = falloc(f, &f->dsys, nsys);
     if (ok == GC_OK && f->ncp > 0) ok = falloc(f, &f->mpos, f->ncp);
+    if (ok == GC_OK && f->ncp > 0) ok = falloc(f, &f->mplo, f->ncp);
     if (ok == GC_OK && f->ncp > 0) ok = falloc(f, &f->mnthro, f->ncp);
     if (ok == GC_OK && cudaMallocHost(&f->h, sizeof(GcFused::Pinned)) != cudaSuccess)
         ok = gc_fail(GC_ENOMEM, "fused: pinned words");
@@ -2358,14 +2401,14 @@ int gc_fused_setup(GcFused* f) {
     GcParams p = f->p;
     if (f->ncell > 0) {
         fk_gather_mpos<<<gc_blocks(f->ncp, 256), 256, 0, st>>>(f->ncp, f->dsys, f->msys, f->slot_of, f->a.pos,
-                                                              f->a.nthro, f->mpos, f->mnthro);
+                                                              f->a.nthro, f->a.plo, f->mpos, f->mplo, f->mnthro);
         GC_CHECK_LAUNCH("fused: membrane positions");
         fk_mgeo<<<f->ncell, 256, 0, st>>>(p, f->dsys, f->cellsys, f->ncell, f->ntri, f->tri, f->betri, f->mpos,
-                                         f->mnthro, f->tarea, f->tnorm, f->tcen, f->reftarea, f->carea, f->cvol,
+                                         f->mplo, f->mnthro, f->tarea, f->tnorm, f->tcen, f->reftarea, f->carea, f->cvol,
                                          f->crefarea, f->crefvol, 1, f->flags);
         GC_CHECK_LAUNCH("fused: set-up geometry");
         fk_mech_setup<<<gc_blocks(f->nedge, f->block), f->block, 0, st>>>(
-            p, f->dsys, f->msys, f->nedge, f->edge, f->mpos, f->mnthro, f->shear, f->bend, f->l0, f->lmax, f->perlen,
+            p, f->dsys, f->msys, f->nedge, f->edge, f->mpos, f->mplo, f->mnthro, f->shear, f->bend, f->l0, f->lmax, f->perlen,
             f->hpow, f->hbend, f->refang, f->flags);
         GC_CHECK_LAUNCH("fused: set-up mechanics");
         GC_TRY(launch_membranes(f, st, p));   // membrane outputs of the loaded state

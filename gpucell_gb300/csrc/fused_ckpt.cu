@@ -214,7 +214,7 @@ extern "C" int gc_fused_restore(GcFused* f, const char* path) {
     GC_CHECK_LAUNCH("restore: slots");
     if (f->ncell > 0) {
         fk_gather_mpos<<<gc_blocks(f->ncp, 256), 256, 0, st>>>(f->ncp, f->dsys, f->msys, f->slot_of, f->a.pos,
-                                                              f->a.nthro, f->mpos, f->mnthro);
+                                                              f->a.nthro, f->a.plo, f->mpos, f->mplo, f->mnthro);
         GC_CHECK_LAUNCH("restore: membrane positions");
     }
     GC_TRY(rebuild_from_ref(f));

@@ -32,7 +32,8 @@ namespace {
 __global__ void fk_import_ref(int n, unsigned nC, const int* __restrict__ sortpart, const float* __restrict__ coor,
                               const float* __restrict__ velrhop, const float* __restrict__ velhalf,
                               const float* __restrict__ force, const int* __restrict__ nthro, SlotArrays a,
-                              int* __restrict__ slot_of, float4* __restrict__ mpos, int4* __restrict__ mnthro,
+                              int* __restrict__ slot_of, float4* __restrict__ mpos, float4* __restrict__ mplo,
+                              int4* __restrict__ mnthro,
                               unsigned* flags) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
@@ -54,6 +55,7 @@ __global__ void fk_import_ref(int n, unsigned nC, const int* __restrict__ sortpa
     slot_of[id] = q;
     if ((unsigned)id >= nC && mpos) {
         mpos[id - nC] = x;
+        mplo[id - nC] = make_float4(0.f, 0.f, 0.f, 0.f);
         mnthro[id - nC] = t;
     }
 }
@@ -179,7 +181,7 @@ int engine_start(GcState& s) {
     if (rc == GC_OK) {
         fk_import_ref<<<gc_blocks(f->n, f->block), f->block, 0, f->st>>>(
             f->n, f->p.nC, r.sortpart, r.coor, r.velrhop, r.velhalf, r.force, r.nthro, f->a, f->slot_of,
-            f->ncell > 0 ? f->mpos : nullptr, f->mnthro, f->flags);
+            f->ncell > 0 ? f->mpos : nullptr, f->mplo, f->mnthro, f->flags);
         cudaError_t e = cudaGetLastError();
         gc_count_launch();
         if (e != cudaSuccess) rc = gc_cuda_fail(e, "fused engine: adopt state");

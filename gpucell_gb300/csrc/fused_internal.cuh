@@ -99,6 +99,7 @@ struct HostCells {
 struct StateCopy {
     SlotArrays s{};
     float4* mpos = nullptr;
+    float4* mplo = nullptr;
     int4* mnthro = nullptr;
     long long* dstep = nullptr;
     bool have = false;
@@ -180,6 +181,7 @@ struct GcFused {
     float4 *tnorm = nullptr, *tcen = nullptr;
     double *carea = nullptr, *cvol = nullptr, *crefarea = nullptr, *crefvol = nullptr;
     float4 *mpos = nullptr, *mforce = nullptr, *magg = nullptr;
+    float4* mplo = nullptr;      // low parts of mpos (the double-float positions of the membrane vertices)
     int4* mnthro = nullptr;
     float* parea = nullptr;
     int *mkeys = nullptr, *mvals = nullptr;
@@ -256,7 +258,8 @@ __global__ void __launch_bounds__(kMaxBS, GC_BUILD_MIN_BLOCKS) fk_build_list(int
 
 __global__ void fk_gather_mpos(int ncp, const SysInfo* __restrict__ sys, const int* __restrict__ msys,
                                const int* __restrict__ slot_of, const float4* __restrict__ pos,
-                               const int4* __restrict__ nthro, float4* __restrict__ mpos, int4* __restrict__ mnthro);
+                               const int4* __restrict__ nthro, const float4* __restrict__ plo,
+                               float4* __restrict__ mpos, float4* __restrict__ mplo, int4* __restrict__ mnthro);
 
 __global__ void fk_store_cells(int ncp, int m0, int ntri, int t0, const float4* __restrict__ mforce,
                                const float4* __restrict__ magg, const float* __restrict__ parea,

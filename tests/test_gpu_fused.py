@@ -150,3 +150,33 @@ def test_fused_tracks_oracle_noise_on(cuda_device):
     np.testing.assert_allclose(g["pos"], o.pos, atol=1e-5)
     _close_rel(g["vel"], o.vel, 1e-4)
     np.testing.assert_allclose(g["Area64"], o.area, rtol=1e-5)
+
+
+def test_fused_force_evaluation_matches_oracle(cuda_device):
+    """Forces of the fused step and of the FP64 oracle on the same positions
+    (a vanishing time step leaves the set-up state in place; noise off), on
+    a periodic suspension whose cells cross the box faces: within 1e-5 of
+    the largest force (measured 3.9e-6), and the membrane deformation force
+    of the undeformed cells, exactly zero, below 1e-3 (measured 1.1e-4; the
+    edge and triangle vectors are differences of double-float positions, so
+    a cell's geometry is the same wrapped into the box or not — with FP32
+    differences it was 3.2e-3)."""
+    import dataclasses
+    from gpucell_gb300.fused import FusedSystem
+    cfg = gen.suspension(nx=40, ny=40, nz=40, ncells=3, subdiv=3, seed=5)
+    cfg = dataclasses.replace(cfg, phys=dataclasses.replace(cfg.phys, dt=1e-20))
+    lo, hi = cfg.bbox[0::2], cfg.bbox[1::2]
+    m = cfg.coor[cfg.n_cell_start:]
+    assert ((m < lo) | (m >= hi)).any(), "no membrane vertex outside the box"
+    o = _oracle(cfg, noise=False)
+    o.step()
+    fs = FusedSystem(cfg, noise=False)
+    fs.step(1, 1)
+    g = fs.fetch()
+    fs.close()
+    mov = slice(cfg.n_b1 + cfg.n_b2, cfg.n)
+    d = np.linalg.norm(g["force"][mov].astype(np.float64) - o.force[mov], axis=1)
+    scale = np.linalg.norm(o.force[mov], axis=1).max()
+    print(f"\nforce error {d.max() / scale:.2e} of the largest force; |DefForce| at rest {np.abs(g['DefForce']).max():.2e}")
+    assert d.max() < 1e-5 * scale
+    assert np.abs(g["DefForce"]).max() < 1e-3
