@@ -116,6 +116,25 @@ def test_captured_steps_follow_host_steps(cuda_device, ensemble):
     assert capt.flags() == 0
 
 
+def test_captured_steps_with_aggregation_follow_host_steps(cuda_device):
+    """The Morse aggregation pass (its own sort, the cube-ordered copies and
+    the per-cube search) inside captured steps: a two-cell rouleau in Couette
+    flow follows the host-driven steps, aggregation forces included."""
+    from gpucell_gb300.fused import FusedSystem
+    cfg = gen.couette(nx=36, ny=18, nz=24, ncells=2, subdiv=2, cell_diameter=3.0, shear_rate=0.5, seed=31)
+    host, capt = FusedSystem(cfg, graph=False), FusedSystem(cfg, graph=True)
+    host.set_options(skin=0.12)
+    capt.set_options(skin=0.12)
+    for _ in range(3):
+        host.step(10, 1)
+        capt.step(10, 1)
+    got, want = capt.fetch(), host.fetch()
+    _compare(got, want)
+    assert np.abs(want["AggForce"]).max() > 0
+    np.testing.assert_allclose(got["AggForce"], want["AggForce"], rtol=0, atol=1e-5 * np.abs(want["AggForce"]).max())
+    assert capt.stats()["rebuilds"] >= 1 and capt.flags() == 0
+
+
 def test_captured_steps_count_launches(cuda_device):
     from gpucell_gb300 import _lib
     from gpucell_gb300.fused import FusedSystem
