@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--no-compact", dest="compact", action="store_false",
                     help="force pass iterates the skin lists instead of the per-step compact lists")
     ap.add_argument("--no-plain", dest="plain", action="store_false", help="skip the FP32 boundary-path timing")
+    ap.add_argument("--no-engine", dest="engine", action="store_false",
+                    help="skip the boundary entry points with the fused engine behind them")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--small", action="store_true", help="a 1/8-size suspension (for quick checks)")
@@ -179,12 +181,16 @@ FORCE_FP32_FLOP_PER_PARTICLE = 5.224e9 / 524288
 GB300_FP32_FLOP_PER_CYCLE = 152 * 128 * 2
 
 
-def measure_plain(cfg, dev, steps, warmup):
-    """The reference-structured FP32 step (one kernel per boundary entry
-    point), timed with CUDA events: the FP32 denominator."""
+def measure_plain(cfg, dev, steps, warmup, engine=False):
+    """The boundary entry points called in GPUCell's step order, timed with
+    CUDA events: with engine=False one kernel per entry point (the
+    reference-structured FP32 step, the FP32 denominator); with engine=True
+    the fused engine behind them (GPUCELL_ENGINE=fused: each call sequence
+    runs as one fused step and writes back every buffer the host reads)."""
     import torch
     from gpucell_gb300 import _lib
     from gpucell_gb300.host import ParticleSystem
+    _lib.call("gc_set_engine", 1 if engine else 0)
     ps = ParticleSystem(cfg, device=dev, noise=True)
     for _ in range(warmup):
         ps.update()
@@ -199,9 +205,14 @@ def measure_plain(cfg, dev, steps, warmup):
     ms = e0.elapsed_time(e1) / steps
     out = {"ms_per_step": ms, "value": cfg.n / (ms / 1e3), "steps": steps,
            "gpu_launches_per_step": (_lib.launch_count() - l0) / steps, "dtype": "fp32",
-           "path": "boundary entry points (gc_cupar_*/gc_cudiv_*), one kernel each"}
+           "path": "boundary entry points (gc_cupar_*/gc_cudiv_*), one kernel each" if not engine else
+                   "boundary entry points in GPUCell's order with GPUCELL_ENGINE=fused: one fused step per call "
+                   "sequence, every host-read buffer written back each step"}
+    if engine:
+        out["dtype"] = "fp32 pair physics; double-float positions; fp64 membrane sums"
     del ps
     torch.cuda.synchronize()
+    _lib.call("gc_set_engine", 0)
     return out
 
 
@@ -256,6 +267,7 @@ def run_ours(args):
     W = max(args.warmup, 3)
     K = args.steps
     plain = measure_plain(cfg, dev, steps=min(K, 10), warmup=3) if args.plain else None
+    engine = measure_plain(cfg, dev, steps=K, warmup=3, engine=True) if args.engine else None
 
     fs = FusedSystem(cfg, noise=args.noise, skin=args.skin, block=args.block, compact=args.compact,
                      graph=args.graph)
@@ -434,6 +446,10 @@ def run_ours(args):
     if plain:
         plain["speedup_of_fused"] = plain["ms_per_step"] / (t_ms / K)
         line["plain_fp32"] = plain
+    if engine:
+        if plain:
+            engine["speedup_over_plain"] = plain["ms_per_step"] / engine["ms_per_step"]
+        line["engine_fused"] = engine
     if ens:
         line["ensemble"] = ens
     if cpu:
