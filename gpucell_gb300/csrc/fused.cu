@@ -456,7 +456,8 @@ __global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, 
                     }
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
-                        float r2 = norm2_rn(pair_diff<W>(xi, xyz(xj[u]), B));
+                        const float3 dd = pair_diff<W>(xi, xyz(xj[u]), B);
+                        float r2 = fmaf(dd.x, dd.x, fmaf(dd.y, dd.y, dd.z * dd.z));
                         if (r2 < p.rc2) {
                             unsigned bit = 1u << (k0 - w0 + u);
                             if (fid(xj[u]) >= b2) {
