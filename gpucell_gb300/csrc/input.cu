@@ -15,6 +15,7 @@
 // the triangles of cells 0..i-1), src/Particle.cu:252-284, and the per-type
 // moduli are spread over edges and triangles as src/Particle.cu:355-375 does.
 #include <errno.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -27,6 +28,65 @@
 #include "gc_internal.cuh"
 
 namespace {
+
+// The decimal number in s[0, n) as strtod reads it, when that is m 10^e
+// with at most 19 significant digits m < 2^53 and |e| <= 22 (surrounded by
+// spaces only): m and 10^|e| are then exact doubles and one IEEE multiply
+// or divide rounds their product or quotient correctly, as strtod does
+// (Clinger 1990).  Returns false for anything else (more digits, larger
+// exponents, inf/nan/hex, trailing text), which goes to strtod.
+bool fast_decimal(const char* s, size_t n, double* out) {
+    static const double kP10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                                    1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+    size_t i = 0;
+    while (i < n && s[i] == ' ') ++i;
+    bool neg = false;
+    if (i < n && (s[i] == '+' || s[i] == '-')) neg = s[i++] == '-';
+    uint64_t m = 0;
+    int digits = 0, exp10 = 0, seen = 0;
+    bool point = false;
+    for (; i < n; ++i) {
+        char c = s[i];
+        if (c >= '0' && c <= '9') {
+            ++seen;
+            if (m == 0 && c == '0') {   // leading zeros carry no digit
+                if (point) --exp10;
+                continue;
+            }
+            if (digits == 19) return false;
+            m = m * 10u + (uint64_t)(c - '0');
+            ++digits;
+            if (point) --exp10;
+        } else if (c == '.' && !point) {
+            point = true;
+        } else {
+            break;
+        }
+    }
+    if (seen == 0) return false;
+    if (i < n && (s[i] == 'e' || s[i] == 'E')) {
+        ++i;
+        bool eneg = false;
+        if (i < n && (s[i] == '+' || s[i] == '-')) eneg = s[i++] == '-';
+        int e = 0, ed = 0;
+        for (; i < n && s[i] >= '0' && s[i] <= '9'; ++i) {
+            if (e < 10000) e = e * 10 + (s[i] - '0');
+            ++ed;
+        }
+        if (ed == 0) return false;
+        exp10 += eneg ? -e : e;
+    }
+    while (i < n && s[i] == ' ') ++i;
+    if (i != n) return false;
+    if (m >= (1ull << 53)) return false;
+    double v = (double)m;
+    if (m != 0) {
+        if (exp10 > 22 || exp10 < -22) return false;
+        v = exp10 >= 0 ? v * kP10[exp10] : v / kP10[-exp10];
+    }
+    *out = neg ? -v : v;
+    return true;
+}
 
 struct Text {
     std::string buf;
@@ -43,6 +103,15 @@ struct Text {
         size_t s = b + 20 * (size_t)k;
         size_t m = 0;
         while (m < 20 && s + m < e) {
+            tmp[m] = buf[s + m];
+            ++m;
+        }
+        while (m > 0 && (tmp[m - 1] == '\r' || tmp[m - 1] == '\t')) --m;   // line ends and tabs: strtod's business
+        double v;
+        if (m > 0 && fast_decimal(tmp, m, &v)) return v;
+        tmp[m] = '\0';
+        m = 0;
+        while (m < 20 && s + m < e) {   // the column as it was, for strtod
             tmp[m] = buf[s + m];
             ++m;
         }

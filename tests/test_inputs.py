@@ -103,3 +103,49 @@ def test_bad_files_are_refused(built_library, tmp_path):
     (tmp_path / "x.bin").write_bytes(b"GCINPUT1" + b"\0" * 20)
     with pytest.raises(_lib.GcError, match="truncated|corrupt|not a binary"):
         read_binary(str(tmp_path / "x.bin"))
+
+
+def _field_strings(seed=11, n=30000):
+    """Numbers as GPUCell's 20-character columns may hold them: printf
+    formats of many widths and precisions, magnitudes from 1e-40 to 1e38,
+    signs, leading spaces, integers, long mantissas and exponents beyond
+    the exact fast path, and inf/nan."""
+    rng = np.random.default_rng(seed)
+    mags = 10.0 ** rng.uniform(-40, 38, n)
+    vals = mags * rng.choice([-1.0, 1.0], n)
+    fmts = ["%.5e", "%.9g", "%.17g", "%f", "%.3E", "%+.7e", "%.12f", "%g", "%.0f", "%.1e", "%.19g"]
+    out = []
+    for k, v in enumerate(vals):
+        s = fmts[k % len(fmts)] % v
+        if len(s) > 19:
+            s = "%.9g" % v
+        out.append(s)
+    out += ["0", "-0", "0.0", "-0.000", "1", "-1", "123456789012345678", "1e22", "1e23", "9007199254740993",
+            "0.1", "0.30000000000000004", "1.7976931348623e308", "4.9e-324", "2.225073858507e-308",
+            "inf", "-inf", "nan", "1e-400", "1e400", "  3.5", "+2.5", "1.e5", ".5", "5.", "00012.5000"]
+    return out
+
+
+def test_decimal_fields_read_like_atof(built_library, tmp_path):
+    """Every 20-character field converts to the float32 of the correctly
+    rounded double, as the reference's atof followed by the assignment to a
+    float does (the loader takes an exact fast path for short decimals and
+    strtod for the rest)."""
+    cfg = gen.small_channel()
+    gen.write_reference_inputs(cfg, str(tmp_path))
+    strs = _field_strings()
+    n = (len(strs) + 2) // 3
+    strs += ["0"] * (3 * n - len(strs))
+    with open(tmp_path / "SDPDParCoor.txt", "w") as f:
+        f.write("nBound1 nBound2 nFluid\n")
+        f.write("%-20d%-20d%-20d\n" % (0, 0, n))
+        f.write("Bound1 x y z\nBound2 x y z\nFluid x y z\n")
+        for r in range(n):
+            f.write("".join("%-20s" % s for s in strs[3 * r:3 * r + 3]) + "\n")
+    got = read_inputs(str(tmp_path))["sdpd_coor"].reshape(-1)
+    assert max(len(s) for s in strs) <= 20   # a column holds 20 characters
+    with np.errstate(over="ignore"):
+        want = np.array([np.float32(float(s)) for s in strs], np.float32)
+    nan = np.isnan(want)
+    assert np.array_equal(np.isnan(got), nan)
+    assert np.array_equal(got[~nan].view(np.uint32), want[~nan].view(np.uint32))
