@@ -172,12 +172,12 @@ FORCE_TRAFFIC_4M = 2.845227264e9 + 0.127872512e9
 # 143.7; profiles/fk_force_fk_density_rbc_suspension_524k.md), and the SM
 # schedulers of a GB300 (152 SMs x 4), each issuing one warp instruction
 # per cycle.
-FORCE_WARP_INST_PER_PARTICLE = 345528243 / 524288
+FORCE_WARP_INST_PER_PARTICLE = 348382172 / 524288
 GB300_SCHEDULERS = 152 * 4
 # FP32 operations of fk_force per particle (FADD + FMUL + 2 FFMA, thread
 # level) from the same ncu capture: 5.224e9 over 524,288 particles; the
 # FP32 peak is 152 SMs x 128 lanes x 2 (FMA) per cycle.
-FORCE_FP32_FLOP_PER_PARTICLE = 5.224e9 / 524288
+FORCE_FP32_FLOP_PER_PARTICLE = 5.224e9 / 524288   # 9963 per particle
 GB300_FP32_FLOP_PER_CYCLE = 152 * 128 * 2
 
 
