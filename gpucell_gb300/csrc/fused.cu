@@ -318,7 +318,8 @@ __device__ __forceinline__ float slab_gap(float x, int c, int axis, const GcGrid
 __global__ void __launch_bounds__(kMaxBS, GC_BUILD_MIN_BLOCKS) fk_build_list(int n, const SysInfo* __restrict__ sys,
                                                      const int* __restrict__ sysid, const float4* __restrict__ pos,
                                                      const unsigned* __restrict__ start, int* __restrict__ nbr,
-                                                     int* __restrict__ cnt, int cap, float cut2, unsigned* flags) {
+                                                     int* __restrict__ cnt, int cap, float cut2, unsigned* flags,
+                                                     int* __restrict__ need) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 xi4 = pos[i];
@@ -384,8 +385,9 @@ __global__ void __launch_bounds__(kMaxBS, GC_BUILD_MIN_BLOCKS) fk_build_list(int
             }
         }
     }
-    if (k > cap) {
+    if (k > cap) {   // the list holds cap entries; the host grows it to the longest wanted
         raise_flag(flags, GC_FLAG_CELL_OVERFLOW);
+        atomicMax(need, k);
         k = cap;
     }
     cnt[i] = k;
@@ -1398,6 +1400,14 @@ float wrap_margin(const GcFused* f) { return 1.01f * f->p.rc + 2.f * f->skin; }
 // Re-sort and list build on the host-driven path (swaps the slot arrays;
 // grows the lists and rebuilds when a particle had more neighbours than the
 // lists hold).
+// List capacity after an overflow: the longest list the build wanted
+// (f->h->need, read back with the overflow flag) with a quarter and 16 to
+// spare, and at least at_least; a multiple of 8.
+int grown_capacity(const GcFused* f, int at_least) {
+    const int want = (int)(1.25 * f->h->need) + 16;
+    return ((want > at_least ? want : at_least) + 7) & ~7;
+}
+
 int rebuild_lists(GcFused* f) {
     const int n = f->n;
     const int nb = gc_blocks(n, f->block);
@@ -1413,15 +1423,18 @@ int rebuild_lists(GcFused* f) {
     float cut2 = cut * cut;
     for (int attempt = 0; attempt < 4; ++attempt) {
         GC_CUDA(cudaMemsetAsync(f->oflag, 0, sizeof(unsigned), st), "fused: flags");
+        GC_CUDA(cudaMemsetAsync(f->need, 0, sizeof(int), st), "fused: flags");
         fk_build_list<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->a.pos, f->sb.cnt, f->nbr, f->cnt, f->cap,
-                                              cut2, f->oflag);
+                                              cut2, f->oflag, f->need);
         GC_CHECK_LAUNCH("fused: build lists");
         GC_CUDA(cudaMemcpyAsync(&f->h->oflag, f->oflag, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "fused: flags");
+        GC_CUDA(cudaMemcpyAsync(&f->h->need, f->need, sizeof(int), cudaMemcpyDeviceToHost, st), "fused: flags");
         GC_CUDA(cudaStreamSynchronize(st), "fused: flags");
         if (!(f->h->oflag & GC_FLAG_CELL_OVERFLOW)) break;
         if (attempt == 3) return gc_fail(GC_EDEVICE, "fused: neighbour lists overflow %d entries", f->cap);
-        // a particle had more neighbours than the list holds: grow and rebuild
-        GC_TRY(alloc_list(f, f->cap * 2));
+        // a particle had more neighbours than the list holds: grow to the
+        // longest list wanted (with room) and rebuild
+        GC_TRY(alloc_list(f, grown_capacity(f, 2 * f->cap)));
     }
     f->rebuilds++;
     return GC_OK;
@@ -1619,7 +1632,7 @@ int launch_rebuild_body(GcFused* f, cudaStream_t st) {
     GC_CHECK_LAUNCH("fused: copy slots");
     float cut = f->p.rc + f->skin;
     fk_build_list<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->a.pos, f->sb.cnt, f->nbr, f->cnt, f->cap,
-                                          cut * cut, f->oflag);
+                                          cut * cut, f->oflag, f->need);
     GC_CHECK_LAUNCH("fused: build lists");
     return GC_OK;
 }
@@ -1811,10 +1824,12 @@ int graph_segment(GcFused* f, int nsteps, int drive) {
         GC_TRY(prepare_graph(f, drive));
         GC_TRY(save_state(f, &f->snap));
         GC_CUDA(cudaMemsetAsync(f->oflag, 0, sizeof(unsigned), f->st), "fused: flags");
+        GC_CUDA(cudaMemsetAsync(f->need, 0, sizeof(int), f->st), "fused: flags");
         for (int k = 0; k < nsteps; ++k)
             GC_CUDA(cudaGraphLaunch(f->gexec[drive], f->st), "fused: launch step graph");
         GC_CUDA(cudaMemcpyAsync(&f->h->oflag, f->oflag, sizeof(unsigned), cudaMemcpyDeviceToHost, f->st), "fused: flags");
         GC_CUDA(cudaMemcpyAsync(&f->h->drebuilds, f->drebuilds, 8, cudaMemcpyDeviceToHost, f->st), "fused: flags");
+        GC_CUDA(cudaMemcpyAsync(&f->h->need, f->need, sizeof(int), cudaMemcpyDeviceToHost, f->st), "fused: flags");
         GC_CUDA(cudaStreamSynchronize(f->st), "fused: step graphs");
         long long nreb = (long long)(f->h->drebuilds - f->drebuilds_seen);
         f->drebuilds_seen = f->h->drebuilds;
@@ -1829,7 +1844,7 @@ int graph_segment(GcFused* f, int nsteps, int drive) {
         // the lists and run them again
         GC_TRY(restore_state(f, &f->snap));
         f->step = step0;
-        GC_TRY(alloc_list(f, f->cap + f->cap / 2 + 8));
+        GC_TRY(alloc_list(f, grown_capacity(f, f->cap + f->cap / 2 + 8)));
         f->graph_dirty = true;
     }
     return gc_fail(GC_EDEVICE, "fused: neighbour lists keep overflowing in captured steps (capacity %d)", f->cap);
@@ -2230,6 +2245,7 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
     if (ok == GC_OK) ok = falloc(f, &f->rebuild, 1);
     if (ok == GC_OK) ok = falloc(f, &f->flags, 1);
     if (ok == GC_OK) ok = falloc(f, &f->oflag, 1);
+    if (ok == GC_OK) ok = falloc(f, &f->need, 1);
     if (ok == GC_OK) ok = falloc(f, &f->stat_sum, 1);
     if (ok == GC_OK) ok = falloc(f, &f->stat_max, 1);
     if (ok == GC_OK) ok = falloc(f, &f->dstep, 1);
@@ -2273,6 +2289,7 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
     }
     if (ok == GC_OK) {
         f->h->drebuilds = 0;
+        f->h->need = 0;
         if (cudaMemsetAsync(f->flags, 0, sizeof(unsigned), f->st) != cudaSuccess ||
             cudaMemsetAsync(f->drebuilds, 0, 8, f->st) != cudaSuccess ||
             cudaMemsetAsync(f->dstep, 0xff, 8, f->st) != cudaSuccess)   // -1

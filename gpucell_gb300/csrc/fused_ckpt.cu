@@ -115,13 +115,15 @@ int rebuild_from_ref(GcFused* f) {
     float cut = f->p.rc + f->skin;
     for (int attempt = 0; attempt < 4; ++attempt) {
         GC_CUDA(cudaMemsetAsync(f->oflag, 0, sizeof(unsigned), st), "restore: flags");
+        GC_CUDA(cudaMemsetAsync(f->need, 0, sizeof(int), st), "restore: flags");
         fk_build_list<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->refpos, f->sb.cnt, f->nbr, f->cnt, f->cap,
-                                              cut * cut, f->oflag);
+                                              cut * cut, f->oflag, f->need);
         GC_CHECK_LAUNCH("restore: build lists");
         GC_CUDA(cudaMemcpyAsync(&f->h->oflag, f->oflag, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "restore");
+        GC_CUDA(cudaMemcpyAsync(&f->h->need, f->need, sizeof(int), cudaMemcpyDeviceToHost, st), "restore");
         GC_CUDA(cudaStreamSynchronize(st), "restore");
         if (!(f->h->oflag & GC_FLAG_CELL_OVERFLOW)) return GC_OK;
-        GC_TRY(alloc_list(f, f->cap * 2));
+        GC_TRY(alloc_list(f, grown_capacity(f, 2 * f->cap)));
     }
     return gc_fail(GC_EDEVICE, "restore: neighbour lists overflow %d entries", f->cap);
 }

@@ -143,6 +143,7 @@ struct GcFused {
     int* rebuild = nullptr;
     unsigned* flags = nullptr;
     unsigned* oflag = nullptr;   // list overflow inside captured steps
+    int* need = nullptr;         // the longest list an overflowing build wanted
     unsigned long long* stat_sum = nullptr;
     int* stat_max = nullptr;
     long long* dstep = nullptr;  // device step counter (ensembles, captured steps)
@@ -152,6 +153,7 @@ struct GcFused {
     struct Pinned {
         int rebuild;
         unsigned oflag;
+        int need;
         unsigned long long drebuilds;
     }* h = nullptr;
     unsigned long long drebuilds_seen = 0;
@@ -230,6 +232,7 @@ int falloc(GcFused* f, T** p, size_t count) {
 int stage_bytes(GcFused* f, size_t bytes);
 void drop_graphs(GcFused* f);
 int alloc_list(GcFused* f, int cap);
+int grown_capacity(const GcFused* f, int at_least);
 int build_grids(GcFused* f);
 int sync_dstep(GcFused* f);
 int rebuild_lists(GcFused* f);
@@ -254,7 +257,8 @@ int store_cells_range(GcFused* f, int c0, int nc, int m0, int nv, int t0, int nt
 __global__ void __launch_bounds__(kMaxBS, GC_BUILD_MIN_BLOCKS) fk_build_list(int n, const SysInfo* __restrict__ sys,
                                                      const int* __restrict__ sysid, const float4* __restrict__ pos,
                                                      const unsigned* __restrict__ start, int* __restrict__ nbr,
-                                                     int* __restrict__ cnt, int cap, float cut2, unsigned* flags);
+                                                     int* __restrict__ cnt, int cap, float cut2, unsigned* flags,
+                                                     int* __restrict__ need);
 
 __global__ void fk_gather_mpos(int ncp, const SysInfo* __restrict__ sys, const int* __restrict__ msys,
                                const int* __restrict__ slot_of, const float4* __restrict__ pos,

@@ -180,3 +180,24 @@ def test_fused_force_evaluation_matches_oracle(cuda_device):
     print(f"\nforce error {d.max() / scale:.2e} of the largest force; |DefForce| at rest {np.abs(g['DefForce']).max():.2e}")
     assert d.max() < 1e-5 * scale
     assert np.abs(g["DefForce"]).max() < 1e-3
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_lists_grow_when_they_overflow(cuda_device, graph):
+    """A handle created with room for 16 list entries per particle (the
+    lists need ~140) grows its lists when a build overflows them and steps
+    exactly as a handle with the default capacity: only the stride of the
+    interleaved lists differs, not their entries or their order."""
+    from gpucell_gb300.fused import FusedSystem
+    cfg = gen.suspension(nx=24, ny=24, nz=24, ncells=1, subdiv=2, hematocrit=0.1, seed=3)
+    small = FusedSystem(cfg, noise=True, list_capacity=16, graph=graph)
+    ref = FusedSystem(cfg, noise=True, graph=graph)
+    small.step(30, 1)
+    ref.step(30, 1)
+    a, b = small.fetch(), ref.fetch()
+    assert small.stats()["capacity"] >= small.stats()["max_neighbors"] > 16
+    assert small.flags() == 0 and ref.flags() == 0
+    for k in ("pos", "vel", "force", "rho"):
+        assert np.array_equal(a[k], b[k]), k
+    small.close()
+    ref.close()
