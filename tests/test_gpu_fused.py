@@ -201,3 +201,28 @@ def test_lists_grow_when_they_overflow(cuda_device, graph):
         assert np.array_equal(a[k], b[k]), k
     small.close()
     ref.close()
+
+
+def test_load_positions_several_boxes_away(cuda_device):
+    """Positions loaded three box lengths off along each periodic axis (with
+    crossing counts three lower, the same unwrapped state) step like the
+    wrapped ones: the permutation wraps any number of lengths and counts them."""
+    from gpucell_gb300.fused import FusedSystem
+    cfg = gen.suspension(nx=24, ny=24, nz=24, ncells=1, subdiv=2, hematocrit=0.1, seed=3)
+    a = FusedSystem(cfg, noise=False)
+    a.step(5, 1)
+    s = a.fetch()
+    L = (cfg.bbox[1::2] - cfg.bbox[0::2]).astype(np.float32)
+    far = FusedSystem(cfg, noise=False)
+    far.load(s["pos"] + 3.0 * L, vel=s["vel"], velhalf=s["velhalf"], force=s["force"], nthro=s["nthro"] - 3)
+    near = FusedSystem(cfg, noise=False)
+    near.load(s["pos"], vel=s["vel"], velhalf=s["velhalf"], force=s["force"], nthro=s["nthro"])
+    far.step(5, 1)
+    near.step(5, 1)
+    g, h = far.fetch(), near.fetch()
+    assert far.flags() == 0 and near.flags() == 0
+    assert np.array_equal(g["nthro"], h["nthro"])
+    np.testing.assert_allclose(g["pos"], h["pos"], atol=2e-5)
+    np.testing.assert_allclose(g["vel"], h["vel"], atol=2e-3 * np.abs(h["vel"]).max())
+    for fs in (a, far, near):
+        fs.close()
