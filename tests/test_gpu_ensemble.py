@@ -174,3 +174,22 @@ def test_autotune_keeps_state_and_trajectory(cuda_device):
     assert cached["ms_per_step"] == 0.0
     assert {k: cached[k] for k in ("skin", "block", "compact", "graph")} == \
         {k: choice[k] for k in ("skin", "block", "compact", "graph")}
+
+
+def test_smallest_periodic_system_in_an_ensemble(cuda_device):
+    """A system in a box of five half-width cells along each periodic axis
+    (L = 3.0, 729 particles: the radius-2 stencil then covers every cell of
+    the box exactly once) beside a larger one steps as it does alone."""
+    from gpucell_gb300.fused import Ensemble, FusedSystem
+    tiny = gen.suspension(nx=9, ny=9, nz=9, ncells=0, seed=8, phys=gen.Physics(ext_force=0.02, seed=5))
+    big = gen.suspension(nx=30, ny=18, nz=18, ncells=2, subdiv=2, hematocrit=0.12, seed=4,
+                         phys=gen.Physics(ext_force=0.01, seed=77))
+    assert tiny.n == 729 and abs(float(tiny.bbox[1] - tiny.bbox[0]) - 3.0) < 1e-5
+    ens = Ensemble([big, tiny], noise=True)
+    alone = FusedSystem(tiny, noise=True)
+    ens.step(20, 1)
+    alone.step(20, 1)
+    _compare(ens.fetch(1), alone.fetch(), cells=False)
+    assert ens.flags() == 0 and alone.flags() == 0
+    ens.close()
+    alone.close()
