@@ -226,3 +226,47 @@ def test_load_positions_several_boxes_away(cuda_device):
     np.testing.assert_allclose(g["vel"], h["vel"], atol=2e-3 * np.abs(h["vel"]).max())
     for fs in (a, far, near):
         fs.close()
+
+
+def test_device_buffers_load_and_store_like_host_ones(cuda_device):
+    """gc_fused_store/store_cells/load with device pointers (to_device /
+    from_device = 1, no staging) give the arrays the host path gives, and a
+    state loaded from device buffers steps like the same state loaded from
+    the host."""
+    import ctypes as C
+    import torch
+    from gpucell_gb300 import _lib
+    from gpucell_gb300.fused import FusedSystem
+    cfg = gen.small_channel()
+    fs = FusedSystem(cfg, noise=True)
+    fs.step(3, 1)
+    host = fs.fetch()
+    n, dev = cfg.n, torch.device("cuda:0")
+    d = {k: torch.empty((n, 3), dtype=torch.float32, device=dev) for k in ("pos", "vel", "force", "velhalf")}
+    d["rho"], d["press"] = torch.empty(n, device=dev), torch.empty(n, device=dev)
+    d["nthro"] = torch.empty((n, 3), dtype=torch.int32, device=dev)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    _lib.call("gc_fused_store", fs.h, *[p(d[k]) for k in ("pos", "vel", "rho", "press", "force", "velhalf", "nthro")], 1)
+    torch.cuda.synchronize()
+    for k in ("pos", "vel", "rho", "press", "force", "velhalf", "nthro"):
+        assert np.array_equal(d[k].cpu().numpy(), host[k]), k
+    cells = {k: torch.empty(v.shape, dtype=torch.float32, device=dev)
+             for k, v in host.items() if k in ("Area", "Vol", "DefForce", "AggForce", "TriNorDir", "TriCenter", "ParArea")}
+    _lib.call("gc_fused_store_cells", fs.h, *[p(cells[k]) for k in ("Area", "Vol", "DefForce", "AggForce",
+                                                                     "TriNorDir", "TriCenter", "ParArea")], 1)
+    torch.cuda.synchronize()
+    for k, t in cells.items():
+        assert np.array_equal(t.cpu().numpy(), host[k]), k
+    fs.step(2, 1)                    # move on, then load the stored state back from the device buffers
+    _lib.call("gc_fused_load", fs.h, *[p(d[k]) for k in ("pos", "vel", "velhalf", "force", "nthro")], 1)
+    fs.step(4, 1)
+    got = fs.fetch()
+    ref = FusedSystem(cfg, noise=True)
+    ref.step(5, 1)                   # the same step indices key the same noise
+    ref.load(host["pos"], host["vel"], host["velhalf"], host["force"], host["nthro"])
+    ref.step(4, 1)
+    want = ref.fetch()
+    for k in ("pos", "vel", "force"):
+        assert np.array_equal(got[k], want[k]), k
+    fs.close()
+    ref.close()

@@ -99,3 +99,19 @@ def test_ensemble_system_writes_its_own_files(cuda_device, tmp_path):
     assert field.shape[0] == b.n_cell_start
     np.testing.assert_allclose(field[:, :3], got["pos"][:b.n_cell_start], rtol=1e-5, atol=1e-6)
     assert len(read_plt(os.path.join(d, "CellCoor", "3.plt"))) == b.ncell
+
+
+def test_system_without_cells_writes_its_files(cuda_device, tmp_path):
+    """A system without membranes writes the particle files (and no cell
+    files or series) without error."""
+    from gpucell_gb300.fused import FusedSystem
+    from gpucell_gb300.output import read_plt
+    cfg = gen.suspension(nx=16, ny=16, nz=16, ncells=0, seed=5)
+    fs = FusedSystem(cfg, noise=True)
+    fs.step(3, 1)
+    d = str(tmp_path / "Result")
+    fs.write_output(d, 3, 0.003, first=True)
+    zones = read_plt(os.path.join(d, "FluidCoor", "3.plt"))
+    assert sum(z["rows"].shape[0] for z in zones) == cfg.n
+    assert not os.path.exists(os.path.join(d, "CellCoor", "3.plt"))
+    fs.close()
