@@ -197,12 +197,9 @@ __host__ __device__ __forceinline__ Philox2 philox2x32_10(uint32_t c0, uint32_t 
 #pragma unroll
 #endif
     for (int r = 0; r < 10; ++r) {
-#ifdef __CUDA_ARCH__
-        uint32_t hi = __umulhi(0xD256D193u, c0), lo = 0xD256D193u * c0;
-#else
+        // one 32x32 -> 64-bit product gives both halves
         uint64_t pr = (uint64_t)0xD256D193u * c0;
         uint32_t hi = (uint32_t)(pr >> 32), lo = (uint32_t)pr;
-#endif
         c0 = hi ^ k ^ c1;
         c1 = lo;
         k += 0x9E3779B9u;
