@@ -190,18 +190,40 @@ extern "C" int gc_fused_restore(GcFused* f, const char* path) {
                     rc = gc_fail(GC_EINVAL, "restore: system %d differs from the checkpoint's", s);
         }
     }
+    if (rc == GC_OK) {   // the file holds exactly the arrays of this configuration
+        uint64_t want = sizeof(h) + sizeof(CkptSys) * (uint64_t)h.nsys;
+        for (const CkptArray& a : ckpt_arrays(f)) want += a.bytes;
+        const long here = ftell(fp);
+        const bool sized = here >= 0 && fseek(fp, 0, SEEK_END) == 0;
+        const long end = sized ? ftell(fp) : -1;
+        if (!sized || end < 0 || fseek(fp, here, SEEK_SET) != 0)
+            rc = gc_fail(GC_EINVAL, "restore: cannot read %s", path);
+        else if ((uint64_t)end != want)
+            rc = gc_fail(GC_EINVAL, "restore: %s holds %ld bytes, a checkpoint of this configuration %llu", path,
+                         end, (unsigned long long)want);
+    }
     if (rc == GC_OK && h.skin_rel != f->skin_rel) {   // the lists were built at the checkpoint's skin
+        const float skin_rel = f->skin_rel;
         f->skin_rel = h.skin_rel;
         f->skin = f->skin_rel * f->p.rc;
         rc = build_grids(f);
+        if (rc == GC_OK && h.K != f->K)
+            rc = gc_fail(GC_EINVAL, "restore: the cube grids differ from the checkpoint's");
+        if (rc != GC_OK) {   // refused: back to the handle's own skin and grids
+            f->skin_rel = skin_rel;
+            f->skin = f->skin_rel * f->p.rc;
+            const int back = build_grids(f);
+            if (back != GC_OK) rc = back;
+        }
+    } else if (rc == GC_OK && h.K != f->K) {
+        rc = gc_fail(GC_EINVAL, "restore: the cube grids differ from the checkpoint's");
     }
-    if (rc == GC_OK && h.K != f->K) rc = gc_fail(GC_EINVAL, "restore: the cube grids differ from the checkpoint's");
     std::vector<char> buf;
     for (const CkptArray& a : ckpt_arrays(f)) {
         if (rc != GC_OK) break;
         buf.resize(a.bytes);
-        if (fread(buf.data(), 1, a.bytes, fp) != a.bytes) {
-            rc = gc_fail(GC_EINVAL, "restore: %s is truncated", path);
+        if (fread(buf.data(), 1, a.bytes, fp) != a.bytes) {   // a read error: the length was checked
+            rc = gc_fail(GC_EINVAL, "restore: reading %s failed; the handle's state is undefined", path);
             break;
         }
         cudaError_t e = cudaMemcpyAsync(a.dev, buf.data(), a.bytes, cudaMemcpyHostToDevice, f->st);

@@ -248,7 +248,11 @@ int gc_fused_autotune(GcFused* f, int trial_steps, int drive_on, int flags, GcFu
  * geometry.  gc_fused_restore reads it into a handle created and set up as
  * for the original run (same systems, constants, boxes and membranes) and
  * rebuilds the lists exactly, so that host-driven steps continue bit for bit
- * as the original run would have.  Synchronise. */
+ * as the original run would have.  A file that is not a checkpoint, holds
+ * another configuration or has another length is refused (GC_EINVAL) before
+ * the handle changes; a read or device error after that leaves the handle's
+ * state undefined until the next successful restore or gc_fused_load.
+ * Synchronise. */
 int gc_fused_checkpoint(GcFused* f, const char* path);
 int gc_fused_restore(GcFused* f, const char* path);
 int gc_fused_destroy(GcFused* f);

@@ -7,8 +7,9 @@
   does, through list rebuilds, with the restored handle created at another
   skin (the checkpoint's skin is adopted); right after the restore the
   stored state equals the state at the checkpoint.
-* A checkpoint of another configuration, or a file that is not one, is
-  refused with an error.
+* A checkpoint of another configuration, a file that is not one, or one of
+  the wrong length is refused with an error, and a refused handle steps on
+  exactly as if the restore had not been asked for.
 """
 import numpy as np
 import pytest
@@ -106,3 +107,26 @@ def test_ensemble_with_aggregation_restarts_bit_for_bit(cuda_device, tmp_path):
     assert b.flags() == 0
     a.close()
     b.close()
+
+
+def test_refused_restore_leaves_the_handle_as_it_was(cuda_device, tmp_path):
+    from gpucell_gb300 import _lib
+    from gpucell_gb300.fused import FusedSystem
+    cfg = _cfg()
+    a = FusedSystem(cfg, noise=True, skin=0.03)
+    a.step(10, 1)
+    a.checkpoint(tmp_path / "a.ckpt")
+    data = (tmp_path / "a.ckpt").read_bytes()
+    (tmp_path / "short.ckpt").write_bytes(data[:-4])
+    (tmp_path / "long.ckpt").write_bytes(data + bytes(8))
+    b = FusedSystem(cfg, noise=True, skin=0.1)   # another skin: a refused file's is not adopted
+    twin = FusedSystem(cfg, noise=True, skin=0.1)
+    for bad in ("short.ckpt", "long.ckpt"):
+        with pytest.raises(_lib.GcError, match="bytes, a checkpoint of this configuration"):
+            b.restore(tmp_path / bad)
+    assert b.options()["skin"] == pytest.approx(0.1)
+    b.step(30, 1)
+    twin.step(30, 1)
+    assert b.stats()["rebuilds"] == twin.stats()["rebuilds"]
+    _same(b.fetch(), twin.fetch())
+    assert b.flags() == 0
