@@ -456,20 +456,20 @@ __global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, 
 #pragma unroll
                         for (int u = 0; u < 4; ++u) jq[u] = __ldg(lp + (size_t)(k0 + 4 + u) * 32);
                     }
+                    // without branches: W is formed for every entry and added
+                    // (as +0 when the entry does not count, which leaves the sum
+                    // as it is), so that no lane waits on another's branch
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
                         const float3 dd = pair_diff<W>(xi, xyz(xj[u]), B);
-                        float r2 = fmaf(dd.x, dd.x, fmaf(dd.y, dd.y, dd.z * dd.z));
-                        if (r2 < p.rc2) {
-                            unsigned bit = 1u << (k0 - w0 + u);
-                            if (fid(xj[u]) >= b2) {
-                                float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
-                                sum += wendland_w(r, p);
-                                if (r2 > 0.f) m |= bit;
-                            } else if (r2 < p.rep_r0sq && r2 > 0.f) {
-                                m |= bit;
-                            }
-                        }
+                        const float r2 = fmaf(dd.x, dd.x, fmaf(dd.y, dd.y, dd.z * dd.z));
+                        const bool in = r2 < p.rc2, apart = r2 > 0.f, sdpd = fid(xj[u]) >= b2;
+                        const float r = apart ? r2 * rsqrtf(r2) : 0.f;
+                        const float w = wendland_w(r, p);
+                        sum += in && sdpd ? w : 0.f;
+                        // acting: an SDPD partner within rc, or a Bound1 wall within the repulsion range
+                        const bool act = in && apart && (sdpd || r2 < p.rep_r0sq);
+                        m |= (unsigned)act << (k0 - w0 + u);
                     }
                 }
                 if (cmask) {
