@@ -42,7 +42,7 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skin", type=float, default=0.075)
@@ -125,6 +125,13 @@ class ClockSampler:
                                           "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        # the timed region starts once the first sample is in (at most 1.5 s)
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 1.5 and self.proc.poll() is None:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.02)
 
     def stop(self, gpu_index=0):
         if not self.proc:
