@@ -1,7 +1,9 @@
-"""The host-side checks bench.py applies to GPU results, against the FP64
-oracle: cell_geometry_fp64 (area and volume of every cell from stored FP32
-positions and crossing counts) equals the oracle's geometry pass on the same
-wrapped state, for cells that cross the periodic faces."""
+"""The host-side checks bench.py applies to GPU results: cell_geometry_fp64
+(area and volume of every cell from stored FP32 positions and crossing
+counts) equals the FP64 oracle's geometry pass on the same wrapped state, for
+cells that cross the periodic faces; the clock record is read from
+nvidia-smi's samples with their throttle reasons; the metric is named by the
+size it ran at."""
 import os
 import sys
 
@@ -33,3 +35,45 @@ def test_cell_geometry_matches_the_oracle():
     o.call("geo", 0)
     np.testing.assert_allclose(area, o.area, rtol=1e-12)
     np.testing.assert_allclose(vol, o.vol, rtol=1e-12)
+
+
+class _FakeSampler:
+    """Stands in for the nvidia-smi process the sampler started."""
+
+    def terminate(self):
+        pass
+
+    def wait(self, timeout=None):
+        return 0
+
+
+def test_clock_samples_are_read_with_their_throttle_reasons(tmp_path):
+    """The bench line's `clocks` record: SM clocks of the benchmarked GPU only,
+    unreadable samples skipped, every throttle reason that was active in any
+    sample reported (a run with hw_slowdown or a thermal slowdown is rejected
+    by whoever reads the line; sw_power_cap is kept and noted)."""
+    import bench
+    lines = [
+        "0, 2070, 2070, 900.1, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, 1980, 2070, 1400.0, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "1, 1200, 2070, 300.0, 0x0000000000000008, Active, Not Active, Not Active, Not Active",
+        "0, [N/A], 2070, 950.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, 2070, 2070, 950.0, 0x0000000000000040, Not Active, Active, Not Active, Not Active",
+    ]
+    s = bench.ClockSampler()
+    s.path = str(tmp_path / "clocks.csv")
+    with open(s.path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    s.fh = open(os.devnull, "w")
+    s.proc = _FakeSampler()
+    rec = s.stop(gpu_index=0)
+    assert rec == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "samples": 3,
+                   "reasons": ["hw_thermal_slowdown", "sw_power_cap"]}
+    assert not os.path.exists(s.path)
+    assert bench.ClockSampler().stop() is None   # never started: no record
+
+
+def test_metric_name_follows_the_workload_size():
+    import bench
+    assert bench.metric_name(4194304) == bench.METRIC
+    assert bench.metric_name(524288) == "particle-steps/s on 524288-particle RBC suspension"
