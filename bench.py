@@ -228,6 +228,27 @@ def measure_plain(cfg, dev, steps, warmup, engine=False):
     return out
 
 
+def rank_reducers(world, dev):
+    """The barrier and the max over ranks that bracket every timed region
+    (identities on one process).  Times are reduced as float64 tensors on
+    `dev`: the GPU under NCCL, the CPU under gloo."""
+    import torch
+    import torch.distributed as dist
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    return barrier, max_over_ranks
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -249,16 +270,7 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
 
-    def barrier():
-        if world > 1:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier, max_over_ranks = rank_reducers(world, dev)
 
     if args.rouleaux_run or args.constriction_run:
         if rank == 0:

@@ -4,7 +4,8 @@ The multi-process path runs as two `gloo` ranks on the CPU: each rank takes
 its LPT share of a drawn ensemble, computes a per-system result on the host
 (a checksum of the system's coordinates stands in for its trajectory), and
 the gather must return every system exactly once, equal to the serial
-computation.
+computation.  The bench's timing reduction (barrier, max over ranks) runs the
+same way.
 """
 import os
 import socket
@@ -82,3 +83,50 @@ def test_two_gloo_ranks_share_an_ensemble():
     assert [k for k, _ in merged] == list(range(6))
     assert [v for _, v in merged] == serial
     assert 0 < len(mine0) < 6
+
+
+def _rank_times(rank, world, port, q):
+    import sys
+
+    import torch
+    import torch.distributed as dist
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    import bench
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    barrier, max_over_ranks = bench.rank_reducers(world, torch.device("cpu"))
+    barrier()
+    t = max_over_ranks(10.0 + 5.0 * rank)   # rank 1 is the slower one
+    barrier()
+    q.put((rank, t))
+    dist.destroy_process_group()
+
+
+def test_bench_times_are_the_max_over_two_gloo_ranks():
+    """The bench brackets each timed region with a barrier and reports the
+    slowest rank's time, on every rank; one process reduces nothing."""
+    import sys
+
+    import torch
+    import torch.multiprocessing as mp
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    import bench
+    barrier, max_over_ranks = bench.rank_reducers(1, torch.device("cpu"))
+    barrier()
+    assert max_over_ranks(3.25) == 3.25
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_times, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = dict(q.get(timeout=300) for _ in range(2))
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    assert got == {0: 15.0, 1: 15.0}
