@@ -7,19 +7,26 @@
 // block is preceded by one header line.  They copy into arrays of fixed
 // size (2,000,000 wall + fluid particles and 4,000,000 membrane vertices,
 // triangles and edges, src/Particle.cu:31-32, 200-202) and read line by
-// line into a 200-character buffer.  Here each file is read whole, the line
-// starts are found in one pass, the numeric lines are converted by several
-// threads, and the arrays are sized from the counts in the files.  The
+// line into a 200-character buffer.  Here each file is mapped whole, its line
+// starts are found by all host threads, the numeric lines are converted by
+// all host threads (the cells' rows in chunks shared out across cells), and
+// the arrays are sized from the counts in the files.  The
 // topology gets the reference's per-cell offsets (vertices of cell i
 // follow those of cells 0..i-1; triangle indices in the edge records follow
 // the triangles of cells 0..i-1), src/Particle.cu:252-284, and the per-type
 // moduli are spread over edges and triangles as src/Particle.cu:355-375 does.
 #include <errno.h>
+#include <fcntl.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
+#include <algorithm>
+#include <atomic>
 #include <string>
 #include <thread>
 #include <type_traits>
@@ -88,9 +95,17 @@ bool fast_decimal(const char* s, size_t n, double* out) {
     return true;
 }
 
+// A text file mapped read-only, with the start of every line.
 struct Text {
-    std::string buf;
+    const char* buf = nullptr;
+    size_t size = 0;
     std::vector<size_t> line;   // start offset of every line
+    Text() = default;
+    Text(const Text&) = delete;
+    Text& operator=(const Text&) = delete;
+    ~Text() {
+        if (buf) munmap((void*)buf, size);
+    }
     size_t count() const { return line.size(); }
     // Column k (20 characters) of line r, converted like atof / atoi.
     double f(size_t r, int k) const { return atof_col(r, k); }
@@ -99,7 +114,7 @@ struct Text {
   private:
     double atof_col(size_t r, int k) const {
         char tmp[24];
-        size_t b = line[r], e = r + 1 < line.size() ? line[r + 1] - 1 : buf.size();
+        size_t b = line[r], e = r + 1 < line.size() ? line[r + 1] - 1 : size;
         size_t s = b + 20 * (size_t)k;
         size_t m = 0;
         while (m < 20 && s + m < e) {
@@ -120,35 +135,86 @@ struct Text {
     }
 };
 
+// fn(w) for w in [0, nt) on nt threads (the caller's among them)
+template <class F>
+void run_threads(int nt, F fn) {
+    std::vector<std::thread> pool;
+    for (int w = 1; w < nt; ++w) pool.emplace_back(fn, w);
+    fn(0);
+    for (auto& th : pool) th.join();
+}
+
+int host_threads() {
+    int nt = (int)std::thread::hardware_concurrency();
+    return nt < 1 ? 1 : nt;
+}
+
+// Maps a file and finds its line starts: the text is cut into one piece per
+// thread, each piece's newlines are found with memchr, and the pieces' line
+// starts are joined in order.  (Mapped, the text is neither copied nor
+// zero-filled first, and the threads that read it fault its pages in.)
 int load_text(const std::string& path, Text* t) {
-    FILE* fp = fopen(path.c_str(), "rb");
-    if (!fp) return gc_fail(GC_EINVAL, "input: cannot open %s", path.c_str());
-    fseek(fp, 0, SEEK_END);
-    long sz = ftell(fp);
-    fseek(fp, 0, SEEK_SET);
-    t->buf.resize(sz > 0 ? (size_t)sz : 0);
-    size_t got = sz > 0 ? fread(&t->buf[0], 1, (size_t)sz, fp) : 0;
-    fclose(fp);
-    if ((long)got != sz) return gc_fail(GC_EINVAL, "input: cannot read %s", path.c_str());
+    const int fd = open(path.c_str(), O_RDONLY);
+    if (fd < 0) return gc_fail(GC_EINVAL, "input: cannot open %s", path.c_str());
+    struct stat st;
+    if (fstat(fd, &st) != 0 || !S_ISREG(st.st_mode)) {
+        close(fd);
+        return gc_fail(GC_EINVAL, "input: %s is not a readable file", path.c_str());
+    }
+    t->size = (size_t)st.st_size;
+    if (t->size > 0) {
+        void* m = mmap(nullptr, t->size, PROT_READ, MAP_PRIVATE, fd, 0);
+        if (m == MAP_FAILED) {
+            t->size = 0;
+            close(fd);
+            return gc_fail(GC_EINVAL, "input: cannot read %s", path.c_str());
+        }
+        t->buf = (const char*)m;
+    }
+    close(fd);
+    const size_t n = t->size;
+    const char* b = t->buf;
+    const int nt = n >= ((size_t)1 << 22) ? host_threads() : 1;
+    std::vector<std::vector<size_t>> part(nt);
+    run_threads(nt, [&](int w) {
+        const char* p = b + n * w / nt;
+        const char* e = b + n * (w + 1) / nt;
+        while (p < e) {
+            const char* q = (const char*)memchr(p, '\n', (size_t)(e - p));
+            if (!q) break;
+            const size_t k = (size_t)(q - b);
+            if (k + 1 < n) part[w].push_back(k + 1);
+            p = q + 1;
+        }
+    });
+    size_t total = 1;
+    for (const auto& v : part) total += v.size();
     t->line.clear();
+    t->line.reserve(total);
     t->line.push_back(0);
-    for (size_t k = 0; k < t->buf.size(); ++k)
-        if (t->buf[k] == '\n' && k + 1 < t->buf.size()) t->line.push_back(k + 1);
+    for (const auto& v : part) t->line.insert(t->line.end(), v.begin(), v.end());
     return GC_OK;
 }
 
+// fn(r) for r in [0, count), cut into one contiguous range per thread
 template <class F>
 void parallel_rows(size_t count, F fn) {
-    int nt = (int)std::thread::hardware_concurrency();
-    if (nt < 1 || count < 50000) nt = 1;
-    std::vector<std::thread> pool;
-    auto work = [&](int w) {
+    const int nt = count < 50000 ? 1 : host_threads();
+    run_threads(nt, [&](int w) {
         size_t b = count * w / nt, e = count * (w + 1) / nt;
         for (size_t r = b; r < e; ++r) fn(r);
-    };
-    for (int w = 1; w < nt; ++w) pool.emplace_back(work, w);
-    work(0);
-    for (auto& th : pool) th.join();
+    });
+}
+
+// fn(i) for i in [0, count) taken in order by all threads from one counter
+// (tasks of uneven size)
+template <class F>
+void parallel_tasks(size_t count, F fn) {
+    const int nt = count < 2 ? 1 : host_threads();
+    std::atomic<size_t> next{0};
+    run_threads(nt, [&](int) {
+        for (size_t i = next++; i < count; i = next++) fn(i);
+    });
 }
 
 template <class T>
@@ -252,28 +318,52 @@ static int input_read(const char* dir, GcInputSet* out) {
     s.betri = alloc<int>(2 * (size_t)s.ncell);
     s.celltab = alloc<int>((size_t)s.ncp);
     {
-        long long b = 0, a = 0, eo = 0;   // vertex offset, triangle offset, edge offset
+        // each cell's vertex, triangle and edge offsets, then its rows in
+        // chunks that all threads share out (cells are many and small, or few
+        // and large)
+        std::vector<long long> vo(s.ncell), to(s.ncell), eo(s.ncell);
+        long long b = 0, a = 0, e = 0;
         for (int c = 0; c < s.ncell; ++c) {
-            const int nv = s.npar[c], nt = s.ntri_cell[c], ne = nt * 3 / 2;
-            const size_t rv = row_v[c], rt = row_t[c], re = row_e[c];
-            const long long b0 = b, a0 = a, e0 = eo;
-            parallel_rows((size_t)nv, [&](size_t k) {
-                for (int q = 0; q < 3; ++q) s.cell_coor[3 * (b0 + k) + q] = (float)cs.f(rv + k, q);
-                s.celltab[b0 + k] = c;
-            });
-            parallel_rows((size_t)nt, [&](size_t k) {
-                for (int q = 0; q < 3; ++q) s.tri[3 * (a0 + k) + q] = (int)cs.i(rt + k, q) + (int)b0;
-            });
-            parallel_rows((size_t)ne, [&](size_t k) {
-                for (int q = 0; q < 4; ++q) s.edge[6 * (e0 + k) + q] = (int)cs.i(re + k, q) + (int)b0;
-                for (int q = 4; q < 6; ++q) s.edge[6 * (e0 + k) + q] = (int)cs.i(re + k, q) + (int)a0;
-            });
-            s.betri[2 * c] = (int)a0;
-            s.betri[2 * c + 1] = (int)(a0 + nt - 1);
-            b += nv;
-            a += nt;
-            eo += ne;
+            vo[c] = b;
+            to[c] = a;
+            eo[c] = e;
+            s.betri[2 * c] = (int)a;
+            s.betri[2 * c + 1] = (int)(a + s.ntri_cell[c] - 1);
+            b += s.npar[c];
+            a += s.ntri_cell[c];
+            e += (long long)s.ntri_cell[c] * 3 / 2;
         }
+        struct Chunk {
+            int cell, kind;   // kind 0: vertices, 1: triangles, 2: edges
+            size_t k0, k1;
+        };
+        constexpr size_t kRows = 4096;
+        std::vector<Chunk> chunks;
+        for (int c = 0; c < s.ncell; ++c) {
+            const size_t rows[3] = {(size_t)s.npar[c], (size_t)s.ntri_cell[c], (size_t)s.ntri_cell[c] * 3 / 2};
+            for (int kind = 0; kind < 3; ++kind)
+                for (size_t k0 = 0; k0 < rows[kind]; k0 += kRows)
+                    chunks.push_back(Chunk{c, kind, k0, std::min(rows[kind], k0 + kRows)});
+        }
+        parallel_tasks(chunks.size(), [&](size_t i) {
+            const Chunk& ch = chunks[i];
+            const int c = ch.cell;
+            const long long b0 = vo[c], a0 = to[c], e0 = eo[c];
+            if (ch.kind == 0) {
+                for (size_t k = ch.k0; k < ch.k1; ++k) {
+                    for (int q = 0; q < 3; ++q) s.cell_coor[3 * (b0 + k) + q] = (float)cs.f(row_v[c] + k, q);
+                    s.celltab[b0 + k] = c;
+                }
+            } else if (ch.kind == 1) {
+                for (size_t k = ch.k0; k < ch.k1; ++k)
+                    for (int q = 0; q < 3; ++q) s.tri[3 * (a0 + k) + q] = (int)cs.i(row_t[c] + k, q) + (int)b0;
+            } else {
+                for (size_t k = ch.k0; k < ch.k1; ++k) {
+                    for (int q = 0; q < 4; ++q) s.edge[6 * (e0 + k) + q] = (int)cs.i(row_e[c] + k, q) + (int)b0;
+                    for (int q = 4; q < 6; ++q) s.edge[6 * (e0 + k) + q] = (int)cs.i(row_e[c] + k, q) + (int)a0;
+                }
+            }
+        });
     }
     // CELLPhyPara.txt (read when there are cells, as the reference does):
     // nType, then per quantity a header and one line per type
