@@ -844,7 +844,9 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     o = Oracle(cfg, noise=True, nthreads=threads)
     o.setup()
-    o.step()   # one warm-up step (page-in, thread start-up)
+    warm = 3   # warm-up steps (page-in, thread start-up), as for the GPU arm
+    for _ in range(warm):
+        o.step()
     steps = max(1, min(args.steps, 3))
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -858,7 +860,7 @@ def run_reference(args):
         "unit": "particle-steps/s",
         "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
         "steps": steps,
-        "warmup": 1,
+        "warmup": warm,
         "ms_per_step": dt / steps * 1e3,
         "higher_is_better": True,
         "scaling": "weak",
