@@ -97,6 +97,25 @@ def build_oracle(verbose: bool = False) -> str:
     return ORACLE_LIB
 
 
+def build_reference_io(verbose: bool = False) -> str | None:
+    """GPUCell's own input loaders and output writers, linked into
+    oracle/_ref/ref_io by oracle/ref_io.mk where the reference's sources are
+    present (the tests of the reader and writer compare against it); None
+    where they are not, or where `make` is missing."""
+    out = os.path.join(ORACLE_DIR, "_ref", "ref_io")
+    make = shutil.which("make")
+    if not make:
+        return None
+    res = subprocess.run([make, "-s", "-f", os.path.join("oracle", "ref_io.mk"), "NVCC=" + _nvcc()], cwd=ROOT,
+                         capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("oracle/ref_io.mk failed\n" + res.stdout + res.stderr)
+    if verbose and (res.stdout + res.stderr).strip():
+        print(res.stdout + res.stderr)
+    return out if os.path.exists(out) else None
+
+
 if __name__ == "__main__":
     print(build_library(verbose=True, force="--force" in sys.argv))
     print(build_oracle(verbose=True))
+    print(build_reference_io(verbose=True))
