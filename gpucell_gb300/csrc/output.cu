@@ -59,12 +59,15 @@ int mkdirs(const std::string& path) {
     return GC_OK;
 }
 
-// "%.5e" of a float without snprintf.  A finite float is k * 2^q exactly
-// (k < 2^24), so the six significant digits m = floor(|v| / 10^(X - 5)) and
-// the remainder are exact in 128-bit integers for 1e-15 <= |v| < 2^128; the
-// last digit is rounded to nearest with ties to even, as printf does with
-// the exact binary value.  Zeros are written directly; subnormals, values
-// below 1e-15, infinities and NaNs go to snprintf (returns false).
+// "%.5e" of a float without snprintf.  The six significant digits come
+// from one double division where that decides their rounding
+// (digits_double; checked against the exact path on every float from 1e-15
+// up), else exactly: a finite float is k * 2^q (k < 2^24), so
+// m = floor(|v| / 10^(X - 5)) and the remainder are exact in 128-bit
+// integers for 1e-15 <= |v| < 2^128, and the last digit is rounded to
+// nearest with ties to even, as printf does with the exact binary value.
+// Zeros are written directly; subnormals, values below 1e-15, infinities and
+// NaNs go to snprintf (returns false).
 typedef unsigned __int128 u128;
 
 struct Pow10Table {
@@ -94,6 +97,34 @@ inline void scaled_digits(uint32_t k, int q, int S, uint64_t& m, int& half) {
     half = r2 < D ? -1 : (r2 == D ? 0 : 1);
 }
 
+// The six rounded significant digits m (100000 <= m <= 1000000) and the
+// decimal exponent X of |f| by double arithmetic: t = |f| / 10^(X-5) is one
+// correctly rounded operation on exact operands (10^n is exact in double for
+// n <= 22), so for 10^5 <= t < 10^6 it is within 1.2e-10 of the exact
+// quotient, and rounding it to an integer gives the exact quotient's
+// rounding unless its fraction lies within 1e-6 of one half (or t lies at the
+// edge of the decade).  Returns false then, or when X is out of that range:
+// the caller takes the exact path.
+inline bool digits_double(double a, int ex, uint64_t& m, int& X) {
+    static const double kP10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                                    1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+    X = ((ex - 127) * 78913) >> 18;   // floor((ex - 127) log10 2): floor(log10 a) or one less
+    for (int it = 0; it < 3; ++it) {
+        const int S = X - 5;
+        if (S < -22 || S > 22) return false;
+        const double t = S >= 0 ? a / kP10[S] : a * kP10[-S];
+        if (t >= 1e6) { ++X; continue; }
+        if (t < 1e5) { --X; continue; }
+        if (t < 100000.001 || t > 999999.999) return false;
+        const uint64_t m0 = (uint64_t)t;
+        const double fr = t - (double)m0;   // exact: t < 2^20
+        if (fabs(fr - 0.5) < 1e-6) return false;
+        m = m0 + (fr > 0.5 ? 1u : 0u);
+        return true;
+    }
+    return false;
+}
+
 inline bool fast_e(float f, char* out, int& len) {
     uint32_t bits;
     memcpy(&bits, &f, 4);
@@ -111,19 +142,22 @@ inline bool fast_e(float f, char* out, int& len) {
     }
     const double a = fabs((double)f);
     if (a < 1e-15) return false;
-    const uint32_t k = frac | 0x800000u;
-    const int q = ex - 150;
-    int X = (int)floor(log10(a));
     uint64_t m = 0;
-    int half = -1;
-    for (int it = 0; it < 4; ++it) {
-        scaled_digits(k, q, X - 5, m, half);
-        if (m >= 1000000u) ++X;
-        else if (m < 100000u) --X;
-        else break;
+    int X = 0;
+    if (!digits_double(a, ex, m, X)) {   // the exact path
+        const uint32_t k = frac | 0x800000u;
+        const int q = ex - 150;
+        X = (int)floor(log10(a));
+        int half = -1;
+        for (int it = 0; it < 4; ++it) {
+            scaled_digits(k, q, X - 5, m, half);
+            if (m >= 1000000u) ++X;
+            else if (m < 100000u) --X;
+            else break;
+        }
+        if (m < 100000u || m >= 1000000u) return false;
+        if (half > 0 || (half == 0 && (m & 1u))) ++m;
     }
-    if (m < 100000u || m >= 1000000u) return false;
-    if (half > 0 || (half == 0 && (m & 1u))) ++m;
     if (m == 1000000u) { m = 100000u; ++X; }
     if (neg) *p++ = '-';
     *p++ = (char)('0' + m / 100000u);

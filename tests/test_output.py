@@ -142,13 +142,17 @@ def test_bad_frames_are_refused(built_library, tmp_path):
 def _hard_floats(seed=3):
     """Floats that stress a %.5e formatter: random bit patterns over the whole
     exponent range, decimal ties at the sixth digit (integers n*10+5 below
-    2^24 and their binary scalings), powers of ten and their neighbours, the
-    float extremes, subnormals, signed zeros, infinities and NaN."""
+    2^24 and their binary scalings) and the floats next to them, powers of
+    ten and their neighbours, log-uniform values over the range the double
+    path serves (1e-12 to 1e16), the float extremes, subnormals, signed
+    zeros, infinities and NaN."""
     rng = np.random.default_rng(seed)
     bits = rng.integers(0, 2**32, size=60000, dtype=np.uint64).astype(np.uint32)
     vals = [bits.view(np.float32)]
     ties = (rng.integers(100000, 1677721, size=4000) * 10 + 5).astype(np.float32)
     vals += [ties, ties * np.float32(2.0**-20), ties * np.float32(2.0**30), -ties]
+    vals += [np.nextafter(ties, np.float32(np.inf)), np.nextafter(ties, np.float32(0))]
+    vals.append((10.0 ** rng.uniform(-12, 16, size=100000)).astype(np.float32))
     p10 = np.array([10.0**e for e in range(-15, 39)], np.float64).astype(np.float32)
     vals += [p10, np.nextafter(p10, np.float32(np.inf)), np.nextafter(p10, np.float32(0)), -p10]
     fi = np.finfo(np.float32)
@@ -158,8 +162,9 @@ def _hard_floats(seed=3):
 
 
 def test_float_formatting_matches_printf(built_library, tmp_path):
-    """The writer formats floats itself (exact integer arithmetic for the six
-    digits); every value must come out as printf's %-20.5e would write it."""
+    """The writer formats floats itself (six digits by double arithmetic where
+    the rounding is certain, by exact integer arithmetic otherwise); every
+    value must come out as printf's %-20.5e would write it."""
     v = _hard_floats()
     n = v.size // 3 * 3
     pos = v[:n].reshape(-1, 3)
