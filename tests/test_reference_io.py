@@ -10,8 +10,9 @@ Particle::OutputPar (src/Particle.cu:712-1300) on host memory; no GPU.
 * gc_input_read reads the four input files as the reference's loaders do:
   every count, parameter, coordinate, topology index (with the per-cell
   offsets) and per-edge / per-triangle modulus, compared bit for bit, for a
-  walled channel with cells of two types, a periodic suspension and a
-  system without cells.
+  walled channel with cells of two types, a periodic suspension, a system
+  without cells, the channel's files with CRLF line ends, and its
+  coordinates in other spellings (%E, fixed point, explicit signs).
 * gc_output_write writes the files the reference's writers write, byte for
   byte, from the same host arrays with the particles in id order (SortPart
   the identity), for a first output step and an appended one; the per-cell
@@ -90,6 +91,31 @@ def _same_bits(a, b, what):
 
 
 CASES = ("channel_two_types", "suspension", "no_cells")
+LOAD_CASES = CASES + ("crlf", "respelled")
+
+
+def _respell(directory):
+    """The coordinates of SDPDParCoor.txt and CELLParStruct.txt in other
+    spellings of their values, one per column (%.7E, fixed with 8 decimals,
+    an explicit plus sign with %.9g): every field still fits its 20
+    characters."""
+    fmts = ("{:<20.7E}", "{:<20.8f}", "{:<+20.9g}")
+    for name in ("SDPDParCoor.txt", "CELLParStruct.txt"):
+        path = os.path.join(directory, name)
+        out = []
+        for line in open(path).read().split("\n"):
+            cols = [line[i:i + 20] for i in range(0, len(line), 20)]
+            if len(cols) == 3 and all("." in c or "e" in c for c in cols):
+                line = "".join(f.format(float(c)) for f, c in zip(fmts, cols))
+            out.append(line)
+        open(path, "w").write("\n".join(out))
+
+
+def _crlf(directory):
+    for name in os.listdir(directory):
+        path = os.path.join(directory, name)
+        data = open(path, "rb").read()
+        open(path, "wb").write(data.replace(b"\n", b"\r\n"))
 
 
 def _write_case(name, directory):
@@ -107,10 +133,14 @@ def _write_case(name, directory):
     return cfg
 
 
-@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("case", LOAD_CASES)
 def test_reader_reads_what_the_reference_loaders_read(built_library, tmp_path, case):
     d = tmp_path / "in"
-    _write_case(case, d)
+    _write_case("channel_two_types" if case in ("crlf", "respelled") else case, d)
+    if case == "crlf":
+        _crlf(d)
+    elif case == "respelled":
+        _respell(d)
     ref = _ref_load(d, tmp_path)
     ours = read_inputs(str(d))
     for k in ("n_b1", "n_b2", "n_fluid", "ncell", "ntri", "nedge", "ncp"):
