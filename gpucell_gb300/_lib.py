@@ -116,6 +116,7 @@ _SIGS = {
     "gc_get_step": [],
     "gc_set_stream": [_P],
     "gc_device_status": [_P],
+    "gc_scratch_bytes": [_P],
     "gc_shutdown": [],
     "gc_launch_count": [],
     "gc_cupar_ConstsDataUp": [_P],

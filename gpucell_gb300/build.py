@@ -26,6 +26,14 @@ ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "build", "liboracle.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def reference_src() -> str:
+    """The reference's src/ directory, read only by the development-time
+    recipes that pin the reader, writer and step driver against GPUCell's own
+    host code: $GPUCELL_REFERENCE/src, by default the development container's
+    read-only checkout.  It does not exist on the GPU machine."""
+    return os.path.join(os.environ.get("GPUCELL_REFERENCE", "/root/reference"), "src")
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
 
@@ -106,8 +114,8 @@ def build_reference_io(verbose: bool = False) -> str | None:
     make = shutil.which("make")
     if not make:
         return None
-    res = subprocess.run([make, "-s", "-f", os.path.join("oracle", "ref_io.mk"), "NVCC=" + _nvcc()], cwd=ROOT,
-                         capture_output=True, text=True)
+    res = subprocess.run([make, "-s", "-f", os.path.join("oracle", "ref_io.mk"), "NVCC=" + _nvcc(),
+                          "REF=" + reference_src()], cwd=ROOT, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("oracle/ref_io.mk failed\n" + res.stdout + res.stderr)
     if verbose and (res.stdout + res.stderr).strip():

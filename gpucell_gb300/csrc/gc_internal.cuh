@@ -322,6 +322,9 @@ int gc_cuda_fail(cudaError_t e, const char* what);
 // (with the error text set).
 void* gc_scratch(int slot, size_t bytes);
 unsigned* gc_flags_ptr();
+// Reads and clears the no-allocation sort's status word of the current
+// device into *flags (asynchronously, on st); nothing before its first call.
+int gc_noalloc_status_take(unsigned* flags, cudaStream_t st);
 // Fused engine behind the entry points (fused.cu).  gc_engine_step runs one
 // fused step on the recorded caller buffers and writes the caller-visible
 // state back; gc_engine_reset drops the engine.

@@ -477,8 +477,10 @@ constexpr size_t kNaCount = na_round(((size_t)GC_NOALLOC_SORT_MAX_KEYS + 1) * si
 constexpr size_t kNaArray = na_round((size_t)GC_NOALLOC_SORT_MAX_N * sizeof(int));
 constexpr size_t kNaBlocks = na_round(((size_t)GC_NOALLOC_SORT_MAX_KEYS / kScanTile + 2) * sizeof(unsigned));
 constexpr size_t kNaMaxKey = na_round(sizeof(int));
-// counts | rank | keys | values | input positions | scan block sums | max key
-constexpr size_t kNaBytes = kNaCount + 4 * kNaArray + kNaBlocks + kNaMaxKey;
+constexpr size_t kNaStatus = na_round(sizeof(unsigned));
+// counts | rank | keys | values | input positions | scan block sums | max key | status
+constexpr size_t kNaBytes = kNaCount + 4 * kNaArray + kNaBlocks + kNaMaxKey + kNaStatus;
+constexpr size_t kNaStatusOffset = kNaBytes - kNaStatus;
 
 static __device__ __align__(256) unsigned char g_noalloc_sort_scratch[kNaBytes];
 
@@ -487,13 +489,14 @@ unsigned char* g_na_base[kNaMaxDevices] = {};
 std::mutex g_na_mutex;
 
 // Device address of the scratch array on the current device (looked up on
-// the first call per device).
-int noalloc_base(unsigned char** out) {
+// the first call per device; with lookup = false, nullptr until then).
+int noalloc_base(unsigned char** out, bool lookup = true) {
     int dev = 0;
+    *out = nullptr;
     GC_CUDA(cudaGetDevice(&dev), "Sort_noalloc: current device");
     if (dev < 0 || dev >= kNaMaxDevices) return gc_fail(GC_EINVAL, "Sort_noalloc: device %d is out of range", dev);
     std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_base[dev]) {
+    if (!g_na_base[dev] && lookup) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_sort_scratch);
         if (e != cudaSuccess) return gc_cuda_fail(e, "Sort_noalloc: scratch address");
@@ -504,6 +507,20 @@ int noalloc_base(unsigned char** out) {
 }
 
 }  // namespace
+
+// The no-allocation sort's status word on the current device (a key outside
+// [0, K) raises GC_FLAG_BAD_INDEX there): ORed into *flags and cleared, on
+// stream st, without synchronising.  Nothing to do on a device where the sort
+// has not run.
+int gc_noalloc_status_take(unsigned* flags, cudaStream_t st) {
+    unsigned char* base = nullptr;
+    GC_TRY(noalloc_base(&base, false));
+    if (!base) return GC_OK;
+    unsigned* status = (unsigned*)(base + kNaStatusOffset);
+    GC_CUDA(cudaMemcpyAsync(flags, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "Sort_noalloc: status");
+    GC_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned), st), "Sort_noalloc: status");
+    return GC_OK;
+}
 
 extern "C" int gc_cudiv_Sort_noalloc(int n, int* keys, int* values) {
     if (n < 0) return gc_fail(GC_EINVAL, "Sort_noalloc: n < 0");
@@ -523,6 +540,10 @@ extern "C" int gc_cudiv_Sort_noalloc(int n, int* keys, int* values) {
     int* tsrc = (int*)(base + kNaCount + 3 * kNaArray);
     unsigned* bsum = (unsigned*)(base + kNaCount + 4 * kNaArray);
     int* maxkey = (int*)(base + kNaCount + 4 * kNaArray + kNaBlocks);
+    // a key outside [0, K) is clamped, as gc_cudiv_Sort does, and raises
+    // GC_FLAG_BAD_INDEX in this word (read by gc_device_status); the array is
+    // zero when the library loads and the word is cleared when it is read
+    unsigned* status = (unsigned*)(base + kNaStatusOffset);
     int K;
     if (s.grid_set) {
         K = s.grid.ncells;
@@ -545,6 +566,6 @@ extern "C" int gc_cudiv_Sort_noalloc(int n, int* keys, int* values) {
     b.tval = tval;
     b.tsrc = tsrc;
     b.bsum = bsum;
-    GC_TRY(sort_with(n, K, keys, values, b, nullptr, st));
+    GC_TRY(sort_with(n, K, keys, values, b, status, st));
     return GC_OK;
 }

@@ -252,10 +252,24 @@ int gc_device_status(unsigned* flags) {
     GcState& s = gc_state();
     if (!flags) return gc_fail(GC_EINVAL, "flags is NULL");
     *flags = 0;
-    if (!s.scratch[SCR_FLAGS]) return GC_OK;
-    GC_CUDA(cudaMemcpyAsync(flags, s.scratch[SCR_FLAGS], sizeof(unsigned), cudaMemcpyDeviceToHost, s.stream), "read flags");
-    GC_CUDA(cudaMemsetAsync(s.scratch[SCR_FLAGS], 0, sizeof(unsigned), s.stream), "clear flags");
+    unsigned main_word = 0, noalloc_word = 0;
+    if (s.scratch[SCR_FLAGS]) {
+        GC_CUDA(cudaMemcpyAsync(&main_word, s.scratch[SCR_FLAGS], sizeof(unsigned), cudaMemcpyDeviceToHost, s.stream),
+                "read flags");
+        GC_CUDA(cudaMemsetAsync(s.scratch[SCR_FLAGS], 0, sizeof(unsigned), s.stream), "clear flags");
+    }
+    GC_TRY(gc_noalloc_status_take(&noalloc_word, s.stream));
     GC_CUDA(cudaStreamSynchronize(s.stream), "read flags");
+    *flags = main_word | noalloc_word;
+    return GC_OK;
+}
+
+int gc_scratch_bytes(unsigned long long* bytes) {
+    if (!bytes) return gc_fail(GC_EINVAL, "bytes is NULL");
+    GcState& s = gc_state();
+    unsigned long long t = 0;
+    for (int i = 0; i < SCR_COUNT_; ++i) t += s.scratch[i] ? (unsigned long long)s.scratch_bytes[i] : 0ull;
+    *bytes = t;
     return GC_OK;
 }
 

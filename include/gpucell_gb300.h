@@ -78,9 +78,13 @@ int gc_set_step(long long step);
 long long gc_get_step(void);
 /* Stream used by every gc_* launch (a cudaStream_t; NULL = legacy default). */
 int gc_set_stream(void* stream);
-/* Reads and clears the device-side status flags (GC_FLAG_*).  Synchronises
- * the library's stream. */
+/* Reads and clears the device-side status flags (GC_FLAG_*), including those
+ * raised by gc_cudiv_Sort_noalloc on the current device.  Synchronises the
+ * library's stream. */
 int gc_device_status(unsigned* flags);
+/* Bytes of device scratch the library holds now (what gc_shutdown frees;
+ * the fixed array of gc_cudiv_Sort_noalloc is not counted). */
+int gc_scratch_bytes(unsigned long long* bytes);
 /* Number of kernels this library has launched since it was loaded. */
 unsigned long long gc_launch_count(void);
 /* Frees every scratch buffer the library allocated.  Safe to call twice;
@@ -142,14 +146,20 @@ int gc_cudiv_Sort(int n, int* keys, int* values);
  * device memory -- a host program that reserves the device memory it will
  * use up front, a process sharing the GPU under a fixed memory cap, or a loop
  * that must not stall on the device synchronisation of cudaFree.  Its
- * temporaries live in one fixed array of about 5.2 MB that every GPU loading
- * the library holds until the process exits; it calls no cudaMalloc or
- * cudaFree.  Limits: n <= GC_NOALLOC_SORT_MAX_N elements and keys in
- * [0, GC_NOALLOC_SORT_MAX_KEYS); larger inputs return GC_EINVAL.  The first
- * call on each device looks up the array's device address (do that call
- * before any stream capture).  All calls share the array: calls that may
- * overlap on the GPU (different streams, or different host threads) race and
- * must be serialised by the caller. */
+ * temporaries live in one fixed array of about 5.2 MB; it calls no
+ * cudaMalloc or cudaFree.  The array belongs to the library's code module,
+ * which CUDA loads lazily by default: the array is committed on a device
+ * when the first call there runs, and held until the process exits.  A
+ * caller that budgets its memory should make one small call on each device
+ * during set-up, before it reserves its own memory and before any stream
+ * capture (that first call also looks up the array's device address).
+ * Limits: n <= GC_NOALLOC_SORT_MAX_N elements and at most
+ * GC_NOALLOC_SORT_MAX_KEYS keys (the grid's cube count, or the largest key
+ * + 1 without a grid); larger inputs return GC_EINVAL.  A key outside
+ * [0, K) is clamped into range, as gc_cudiv_Sort does, and raises
+ * GC_FLAG_BAD_INDEX, which gc_device_status reports.  All calls share the
+ * array: calls that may overlap on the GPU (different streams, or different
+ * host threads) race and must be serialised by the caller. */
 #define GC_NOALLOC_SORT_MAX_N    262144
 #define GC_NOALLOC_SORT_MAX_KEYS 262144
 int gc_cudiv_Sort_noalloc(int n, int* keys, int* values);

@@ -8,9 +8,10 @@
 #                          of oracle/ref_calls_stubs.cu, driven by
 #                          oracle/ref_calls.cu
 # Test infrastructure only: run from the repository root,
-#   make -f oracle/ref_io.mk [REF=<reference>/src]
-# Without the reference's sources it builds nothing.
-REF ?= /root/reference/src
+#   make -f oracle/ref_io.mk REF=<reference>/src
+# (gpucell_gb300/build.py passes $GPUCELL_REFERENCE/src).  Without the
+# reference's sources it builds nothing.
+REF ?= $(GPUCELL_REFERENCE)/src
 NVCC ?= nvcc
 OUT := oracle/_ref
 LIB := gpucell_gb300/lib

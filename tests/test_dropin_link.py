@@ -12,7 +12,9 @@ import subprocess
 
 import pytest
 
-REF_SRC = "/root/reference/src"
+from gpucell_gb300.build import reference_src
+
+REF_SRC = reference_src()
 
 
 @pytest.mark.slow
