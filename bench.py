@@ -53,7 +53,15 @@ def parse():
     ap.add_argument("--no-engine", dest="engine", action="store_false",
                     help="skip the boundary entry points with the fused engine behind them")
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--cpu-steps", type=int, default=10,
+                    help="timed FP64 oracle steps of the CPU baseline (after one warm-up step)")
+    ap.add_argument("--ref-steps-cap", type=int, default=30,
+                    help="the reference arm times min(--steps, this) oracle steps")
+    ap.add_argument("--ens-seq-steps", type=int, default=10,
+                    help="steps per system of the sequential baselines of the ensemble")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="skip the short cfg3 (sheared suspension) and cfg4 (constriction) legs")
+    ap.add_argument("--config-steps", type=int, default=200, help="steps of the cfg3 and cfg4 legs")
     ap.add_argument("--small", action="store_true", help="a 1/8-size suspension (for quick checks)")
     ap.add_argument("--no-noise", dest="noise", action="store_false",
                     help="thermal noise off (for cost breakdowns; the reported workload has it on)")
@@ -67,7 +75,7 @@ def parse():
     ap.add_argument("--ens-systems", type=int, default=64)
     ap.add_argument("--ens-steps", type=int, default=20)
     ap.add_argument("--no-parity", dest="parity", action="store_false",
-                    help="skip the parity check against the FP64 oracle on a small channel")
+                    help="skip the parity checks against the FP64 oracle (the workload itself, and a small channel)")
     ap.add_argument("--no-output", dest="output", action="store_false",
                     help="skip timing one output step (GPUCell's output files)")
     ap.add_argument("--rouleaux-run", action="store_true",
@@ -170,27 +178,119 @@ def plain_bytes_per_step(cfg):
     return 352 * cfg.n + 16 * cfg.ntri + 32 * cfg.nedge + 28 * cfg.ncp
 
 
-# Dominant kernel of the fused step: fk_force.  Algorithmic bytes per
-# particle: its own position, predicted velocity, VelHalf (16 B each) and
-# (1/d, P/d^2) (8 B) read, force and velocity (16 B each) written, the list
-# length (4 B) and its neighbour-list entries (4 B each) read.
+# Per-particle byte counts of the fused step's kernels.  fk_force's share of
+# the plain step's algorithmic bytes: the fused force pass (44 B: position,
+# velocity, pressure and density read, force written) and the corrector of the
+# integration (28 B: VelHalf read, velocity written).
+FORCE_ALG_BYTES = 44 + 28
+# Bytes of the particle's own records fk_force moves: its position, predicted
+# velocity and VelHalf (16 B each) and (1/d, P/d^2) (8 B) read, force and
+# velocity (16 B each) written, the list length (4 B) read.  The neighbour
+# list entries it streams (4 B each) come on top: the Verlet lists are an
+# implementation overhead of the fused step, not algorithmic bytes.
 FORCE_STATE_BYTES = 16 * 3 + 8 + 16 * 2 + 4
-# DRAM bytes (read + write) of one fk_force launch on the 4.2M-particle
-# suspension, from ncu at full size (profiles/fused_step_rbc_suspension_4M_launches.md):
-# 2.845e9 read + 0.128e9 written, with 143.6 list entries per particle.
-FORCE_TRAFFIC_4M = 2.845227264e9 + 0.127872512e9
-# Warp instructions fk_force issues per particle (ncu smsp__inst_executed.sum
-# of one launch on the 524,288-particle suspension / particles, mean list
-# 143.7; profiles/fk_force_fk_density_rbc_suspension_524k.md), and the SM
-# schedulers of a GB300 (152 SMs x 4), each issuing one warp instruction
-# per cycle.
-FORCE_WARP_INST_PER_PARTICLE = 348382172 / 524288
+
+# Counters from one-kernel ncu captures of fk_force (they are constants of
+# the kernel's code, refreshed whenever it changes; the line says which
+# capture they come from):
+#   python bench.py --small --no-ensemble --cpu-steps 0 --no-plain --no-engine --no-output --no-parity
+#       --no-configs --steps 3 --warmup 3 --profile-steps 1 --e2e-steps 1   (plain run, exit 0), then
+#   ncu --set full --clock-control none -k regex:"fk_(force|density)" -s 6 -c 2 <the same command>
+# on the 524,288-particle suspension (warp instructions and FP32 operations
+# per particle, mean list 143.7), and
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none
+#       -k regex:"fk_force" -s 8 -c 2 python bench.py --no-ensemble --cpu-steps 0 --no-plain --no-output
+#       --no-parity --no-configs --steps 4 --warmup 3 --profile-steps 1 --e2e-steps 1
+# at full size (DRAM bytes of one launch, one pass).
+FORCE_COUNTERS = {
+    "kernel_version": "fk_force: one thread per particle over its compact list of acting entries",
+    "dram_bytes_per_launch_4M": 2.845227264e9 + 0.127872512e9,
+    "warp_inst_per_particle": 348382172 / 524288,
+    "fp32_flop_per_particle": 5.224e9 / 524288,
+}
+# SM schedulers of a GB300 (152 SMs x 4, one warp instruction per cycle
+# each) and its FP32 lanes (152 SMs x 128, an FMA counting 2).
 GB300_SCHEDULERS = 152 * 4
-# FP32 operations of fk_force per particle (FADD + FMUL + 2 FFMA, thread
-# level) from the same ncu capture: 5.224e9 over 524,288 particles; the
-# FP32 peak is 152 SMs x 128 lanes x 2 (FMA) per cycle.
-FORCE_FP32_FLOP_PER_PARTICLE = 5.224e9 / 524288   # 9963 per particle
 GB300_FP32_FLOP_PER_CYCLE = 152 * 128 * 2
+
+
+def rooflines(cfg, ms_per_step, force_ms, dens_ms, mean_nb, hbm, peak_kind, clocks, full_size):
+    """The roofline objects of the bench line.
+
+    `roofline`: the whole step against HBM, with the algorithmic bytes of the
+    plain FP32 step (plain_bytes_per_step: 352 B per particle + 16 per
+    triangle + 32 per edge + 28 per membrane vertex), so that frac =
+    particle-steps/s x B_alg / N / the measured HBM bandwidth.
+    `roofline_kernels`: fk_force with its share of those bytes (force 44 +
+    corrector 28 per particle), and the bytes it actually streams (its own
+    records plus 4 B per neighbour-list entry, the lists being overhead);
+    fk_density likewise.  `issue_roofline` / `fp32_roofline`: fk_force's
+    warp instructions and FP32 operations (ncu counters of its code) per
+    second against the GB300's issue and FP32 peaks, the roofs that bind it.
+    """
+    n = cfg.n
+    peak_src = f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
+    b_alg = plain_bytes_per_step(cfg)
+    step_gbs = b_alg / (ms_per_step / 1e3) / 1e9
+    roof = {
+        "kernel": "whole fused step",
+        "bound": "hbm",
+        "achieved": step_gbs,
+        "peak": hbm,
+        "unit": "GB/s",
+        "frac": step_gbs / hbm,
+        "peak_source": peak_src,
+        "traffic": None,
+        "bytes_per_step": b_alg,
+        "formula": f"B_alg = 352 N + 16 N_tri + 32 N_edge + 28 N_vert = 352*{n} + 16*{cfg.ntri} + 32*{cfg.nedge} "
+                   f"+ 28*{cfg.ncp} = {b_alg / 1e9:.4f} GB per step; frac = B_alg / (ms_per_step) / peak",
+        "note": "algorithmic bytes of the plain FP32 step per unit of work (neighbour state from cache, no lists); "
+                "the fused step is bound by instruction issue in its pair kernels (issue_roofline)",
+    }
+    f_alg = FORCE_ALG_BYTES * n
+    f_streamed = n * (FORCE_STATE_BYTES + 4 * mean_nb)
+    d_alg = 20 * n
+    d_streamed = n * (24 + 4 * mean_nb)
+    kern = {
+        "fk_force": {
+            "launch_ms": force_ms, "bound": "hbm", "unit": "GB/s", "peak": hbm, "peak_source": peak_src,
+            "alg_bytes_per_launch": f_alg, "achieved": f_alg / (force_ms / 1e3) / 1e9,
+            "frac": f_alg / (force_ms / 1e3) / 1e9 / hbm,
+            "streamed_bytes_per_launch": f_streamed,
+            "streamed_frac": f_streamed / (force_ms / 1e3) / 1e9 / hbm,
+            "traffic": FORCE_COUNTERS["dram_bytes_per_launch_4M"] if full_size else None,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at full size "
+                              f"({FORCE_COUNTERS['kernel_version']})",
+            "note": f"alg = {FORCE_ALG_BYTES} B per particle (force 44 + corrector 28); streamed = "
+                    f"{FORCE_STATE_BYTES} B per particle + 4 B per list entry (mean list {mean_nb:.1f}: overhead)",
+        },
+        "fk_density": {
+            "launch_ms": dens_ms, "bound": "hbm", "unit": "GB/s", "peak": hbm,
+            "alg_bytes_per_launch": d_alg, "achieved": d_alg / (dens_ms / 1e3) / 1e9,
+            "frac": d_alg / (dens_ms / 1e3) / 1e9 / hbm,
+            "streamed_bytes_per_launch": d_streamed,
+            "streamed_frac": d_streamed / (dens_ms / 1e3) / 1e9 / hbm,
+            "note": "alg = 20 B per particle (position read, density written); streamed = 24 B per particle + "
+                    "4 B per list entry",
+        },
+    }
+    mhz = clocks["sm_mhz"] if clocks else 2070.0
+    ipp, fpp = FORCE_COUNTERS["warp_inst_per_particle"], FORCE_COUNTERS["fp32_flop_per_particle"]
+    issue = {
+        "kernel": "fk_force", "bound": "instruction issue", "unit": "warp instructions/s",
+        "achieved": ipp * n / (force_ms / 1e3), "peak": GB300_SCHEDULERS * mhz * 1e6,
+        "frac": ipp * n / (force_ms / 1e3) / (GB300_SCHEDULERS * mhz * 1e6),
+        "note": f"{ipp:.0f} warp instructions per particle (ncu, 524k-particle suspension, "
+                f"{FORCE_COUNTERS['kernel_version']}); peak = 608 schedulers x the sampled SM clock",
+    }
+    fp32 = {
+        "kernel": "fk_force", "bound": "FP32 pipe", "unit": "TFLOP/s",
+        "achieved": fpp * n / (force_ms / 1e3) / 1e12, "peak": GB300_FP32_FLOP_PER_CYCLE * mhz * 1e6 / 1e12,
+        "frac": fpp * n / (force_ms / 1e3) / (GB300_FP32_FLOP_PER_CYCLE * mhz * 1e6),
+        "note": f"{fpp:.0f} FP32 operations per particle (FADD + FMUL + 2 FFMA, ncu); peak = 152 SMs x 128 lanes "
+                "x 2 x the sampled SM clock",
+    }
+    return roof, kern, issue, fp32
 
 
 def measure_plain(cfg, dev, steps, warmup, engine=False):
@@ -383,8 +483,8 @@ def run_ours(args):
     mean_nb = st1["mean_neighbors"]
     force_ms = prof["force_ms"] / max(prof["steps"], 1)
     dens_ms = prof["density_ms"] / max(prof["steps"], 1)
-    force_bytes = n * (FORCE_STATE_BYTES + 4 * mean_nb)
-    achieved = force_bytes / (force_ms / 1e3) / 1e9
+    roof, roof_kernels, issue_roof, fp32_roof = rooflines(cfg, t_ms / K, force_ms, dens_ms, mean_nb, hbm, peak_kind,
+                                                          clocks, full_size=(not args.small and n == 4194304))
 
     fs.close()
     ens = run_ensemble(args, dev, rank, world, barrier, max_over_ranks) if args.ensemble else None
@@ -392,8 +492,9 @@ def run_ours(args):
         if world > 1:
             dist.destroy_process_group()
         return
+    configs = run_config_legs(args) if args.configs and world == 1 else None
 
-    cpu, parity = cpu_leg(cfg, args.cpu_steps if world == 1 else 0, 100 if args.parity else 0)
+    cpu, parity = cpu_leg(cfg, args.cpu_steps if world == 1 else 0, args.parity, args)
     line = {
         "metric": metric_name(n),
         "value": value,
@@ -419,43 +520,10 @@ def run_ours(args):
                 "d2h_bytes_per_step": bo, "steps": KE,
                 "path": "C ABI gc_fused_load -> gc_fused_step -> gc_fused_store(_cells), pinned host buffers"},
         "gpu_launches": launches,
-        "roofline": {
-            "kernel": "fk_force (SDPD + repulsion + body force + membrane add + corrector)",
-            "bound": "hbm",
-            "achieved": achieved,
-            "peak": hbm,
-            "unit": "GB/s",
-            "frac": achieved / hbm,
-            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": FORCE_TRAFFIC_4M if (not args.small and n == 4194304) else None,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one fk_force launch, full size",
-            "bytes_per_launch": force_bytes,
-            "launch_ms": force_ms,
-            "note": f"bytes = {FORCE_STATE_BYTES} per particle + 4 per list entry (mean list {mean_nb:.1f}); "
-                    "the pair physics is FP32-issue bound",
-        },
-        "issue_roofline": {
-            "kernel": "fk_force",
-            "bound": "instruction issue",
-            "achieved": FORCE_WARP_INST_PER_PARTICLE * n / (force_ms / 1e3),
-            "peak": GB300_SCHEDULERS * (clocks["sm_mhz"] if clocks else 2070.0) * 1e6,
-            "unit": "warp instructions/s",
-            "frac": FORCE_WARP_INST_PER_PARTICLE * n / (force_ms / 1e3)
-                    / (GB300_SCHEDULERS * (clocks["sm_mhz"] if clocks else 2070.0) * 1e6),
-            "note": "instructions per particle from ncu on the 524k-particle suspension; peak = 608 schedulers x "
-                    "the sampled SM clock x 1 warp instruction per cycle",
-        },
-        "fp32_roofline": {
-            "kernel": "fk_force",
-            "bound": "FP32 pipe",
-            "achieved": FORCE_FP32_FLOP_PER_PARTICLE * n / (force_ms / 1e3) / 1e12,
-            "peak": GB300_FP32_FLOP_PER_CYCLE * (clocks["sm_mhz"] if clocks else 2070.0) * 1e6 / 1e12,
-            "unit": "TFLOP/s",
-            "frac": FORCE_FP32_FLOP_PER_PARTICLE * n / (force_ms / 1e3)
-                    / (GB300_FP32_FLOP_PER_CYCLE * (clocks["sm_mhz"] if clocks else 2070.0) * 1e6),
-            "note": "FP32 operations per particle (FADD + FMUL + 2 FFMA) from ncu on the 524k-particle suspension, "
-                    "~88 per acting pair; peak = 152 SMs x 128 lanes x 2 x the sampled SM clock",
-        },
+        "roofline": roof,
+        "roofline_kernels": roof_kernels,
+        "issue_roofline": issue_roof,
+        "fp32_roofline": fp32_roof,
         "kernels_ms_per_step": {"fk_force": force_ms, "fk_density": dens_ms},
         "output_step": out_info,
         "diagnostics_fp64": {"momentum": [float(x) for x in diag["momentum"]],
@@ -476,6 +544,8 @@ def run_ours(args):
         line["engine_fused"] = engine
     if ens:
         line["ensemble"] = ens
+    if configs:
+        line["configs"] = configs
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
@@ -678,11 +748,12 @@ def run_ensemble(args, dev, rank, world, barrier, max_over_ranks):
         return out
     # the same systems one after the other: FP32 boundary path, fused step
     seq_plain_ms = seq_fused_ms = 0.0
-    ps_steps, fs_steps = 2, K
+    ps_steps, fs_steps = max(1, args.ens_seq_steps), K
     seq_launches = 0
     for c in sub:
         ps = ParticleSystem(c, device=dev, noise=args.noise)
-        ps.update()
+        for _ in range(3):   # warm-up
+            ps.update()
         torch.cuda.synchronize()
         l1 = _lib.launch_count()
         ev0.record()
@@ -694,7 +765,7 @@ def run_ensemble(args, dev, rank, world, barrier, max_over_ranks):
         seq_launches += _lib.launch_count() - l1
         del ps
         fs = FusedSystem(c, noise=args.noise, skin=0.1, block=128, compact=True)
-        fs.step(2, 1)
+        fs.step(3, 1)
         torch.cuda.synchronize()
         ev0.record()
         fs.step(fs_steps, 1)
@@ -716,18 +787,71 @@ def run_ensemble(args, dev, rank, world, barrier, max_over_ranks):
     return out
 
 
-def cpu_leg(cfg, cpu_steps, parity_steps):
-    """The FP64 CPU oracle's leg of the bench (rank 0): `cpu_baseline` times
-    `cpu_steps` full oracle steps of the workload on the host cores; `parity`
-    steps a small walled channel `parity_steps` times with the oracle as the
-    checker beside the fused step.  The oracle is used nowhere else here."""
+def cpu_leg(cfg, cpu_steps, parity, args):
+    """The FP64 CPU oracle's leg of the bench (rank 0, after the timed GPU
+    work).  `cpu_baseline` times `cpu_steps` full oracle steps of the
+    workload on all host cores after one warm-up step, and a one-core sample.
+    With `parity`, the same oracle run doubles as the checker of the
+    workload itself: after its first five steps (the warm-up and four timed
+    ones, the clock stopped while it compares) it is compared with five
+    fused steps of the GPU from the same state (noise on, the same Philox
+    pair noise); a second oracle state evaluates the forces once on the
+    set-up positions (a vanishing time step, noise off) against the GPU's,
+    particle by particle; and a small walled channel is stepped 100 times by
+    both.  The oracle is used nowhere else here."""
     from gpucell_gb300.build import build_oracle
-    if cpu_steps <= 0 and parity_steps <= 0:
+    if cpu_steps <= 0 and not parity:
         return None, None
     build_oracle()
-    cpu = cpu_baseline(cfg, cpu_steps) if cpu_steps > 0 else None
-    par = parity_check(parity_steps) if parity_steps > 0 else None
-    return cpu, par
+    par = {}
+    if parity:
+        par = force_parity(cfg)
+    cpu, traj = cpu_baseline(cfg, cpu_steps, compare_after=5 if parity else 0)
+    if parity:
+        par["trajectory"] = traj
+        par["channel"] = parity_check(100)
+        par["workload"] = f"{cfg.n}-particle RBC suspension ({cfg.ncell} cells of {int(cfg.npar[0])} vertices)"
+        par["reference"] = "FP64 CPU oracle (oracle/oracle.c)"
+    return (cpu if cpu_steps > 0 else None), (par or None)
+
+
+def force_parity(cfg):
+    """Forces of one fused step on the set-up positions (time step 1e-20, so
+    the positions stay; noise off, since the random force grows as dt^-1/2)
+    against the FP64 oracle's, per particle: |dF_i| against 1e-5 |F_i| +
+    16 u S_i (u = 2^-24, S_i the sum of the magnitudes of the terms F_i adds
+    up), with the median, 99th percentile and largest relative errors."""
+    import dataclasses
+
+    from gpucell_gb300.fused import FusedSystem
+    from oracle.binding import Oracle, force_error_stats
+    c0 = dataclasses.replace(cfg, phys=dataclasses.replace(cfg.phys, dt=1e-20))
+    o = Oracle(c0, noise=False, nthreads=os.cpu_count() or 1)
+    o.setup()
+    o.step()
+    scale = o.force_scale()
+    fs = FusedSystem(c0, noise=False)
+    fs.step(1, 1)
+    g = fs.fetch()
+    fs.close()
+    mov = slice(cfg.n_b1 + cfg.n_b2, cfg.n)
+    cs = cfg.n_cell_start - (cfg.n_b1 + cfg.n_b2)
+    out = {"force_evaluation": {}, "force_given_gpu_density": {}}
+    parts = (("all", slice(None)), ("fluid", slice(0, cs)), ("membrane", slice(cs, None)))
+    for name, sl in parts:
+        out["force_evaluation"][name] = force_error_stats(g["force"][mov][sl], o.force[mov][sl], scale[mov][sl])
+    o.forces_from_density(g["rho"])
+    scale = o.force_scale(31)
+    for name, sl in parts:
+        out["force_given_gpu_density"][name] = force_error_stats(g["force"][mov][sl], o.force[mov][sl],
+                                                                 scale[mov][sl])
+    out["force_evaluation"]["what"] = ("one force evaluation on identical positions, noise off, against the oracle's "
+                                       "own FP64 densities: per particle |dF_i| <= 1e-5 |F_i| + 16 u S_i, the pressure "
+                                       "term counted at c^2 rho in S_i (worst_ratio <= 1 passes)")
+    out["force_given_gpu_density"]["what"] = ("the same forces against the oracle's FP64 forces from the GPU's FP32 "
+                                              "densities, the pressure term counted at |P| in S_i")
+    del o
+    return out
 
 
 def parity_check(steps=100):
@@ -762,22 +886,31 @@ def parity_check(steps=100):
             "max_position_error": float(np.abs(g["pos"] - o.pos).max()),
             "velocity_profile_error": float(np.abs(pg - po).max() / np.abs(po).max()),
             "area_error": float(abs(g["Area64"][0] / o.area[0] - 1)),
-            "volume_error": float(abs(g["Vol64"][0] / o.vol[0] - 1)),
-            "reference": "FP64 CPU oracle (oracle/oracle.c)"}
+            "volume_error": float(abs(g["Vol64"][0] / o.vol[0] - 1))}
 
 
-def cpu_baseline(cfg, steps):
+def cpu_baseline(cfg, steps, compare_after=0):
     """FP64 CPU restatement of the method on all host cores, on `steps` full
-    steps of the same workload after one warm-up step."""
+    steps of the same workload after one warm-up step.  With
+    `compare_after` = k, the oracle's state after its first k steps is
+    compared with k fused GPU steps from the same set-up (outside the timed
+    spans); returns (baseline, comparison)."""
+    import numpy as np
     from oracle.binding import Oracle
     threads = os.cpu_count() or 1
     o = Oracle(cfg, noise=True, nthreads=threads)
     o.setup()
     o.step()   # warm-up (page-in, thread start-up)
-    t0 = time.perf_counter()
-    for _ in range(steps):
+    done, dt, traj = 1, 0.0, None
+    while done - 1 < steps or (compare_after and traj is None):
+        if compare_after and done == compare_after and traj is None:
+            traj = trajectory_parity(cfg, o, compare_after)
+            continue
+        t0 = time.perf_counter()
         o.step()
-    dt = time.perf_counter() - t0
+        dt += time.perf_counter() - t0
+        done += 1
+    timed = done - 1
     del o
     # one core, on a bounded sample: one step of a 1/16-size suspension with
     # cells of the same size at about the same hematocrit (262,144
@@ -789,12 +922,56 @@ def cpu_baseline(cfg, steps):
     t1 = time.perf_counter()
     o1.step()
     dt1 = time.perf_counter() - t1
-    return {"value": cfg.n * steps / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} full step(s) of the {cfg.n}-particle workload after one warm-up step, FP64, OpenMP",
+    base = {"value": cfg.n * timed / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "steps": timed,
+            "sample": f"{timed} full steps of the {cfg.n}-particle workload after one warm-up step, FP64, OpenMP",
             "cpu_model": cpu_model(),
             "one_core": {"value": small.n / dt1, "unit": "particle-steps/s",
                          "sample": f"one step of a {small.n}-particle suspension ({small.ncell} cells of "
                                    f"{int(small.npar[0])} vertices), FP64, 1 thread"}}
+    _ = np
+    return base, traj
+
+
+def trajectory_parity(cfg, o, k):
+    """k fused GPU steps (noise on) from the set-up against the oracle `o`
+    after its first k steps: largest position error (minimum image), largest
+    velocity error relative to the largest speed component, and the largest
+    per-cell relative area and volume errors (FP64 on both sides)."""
+    import numpy as np
+    from gpucell_gb300.fused import FusedSystem
+    fs = FusedSystem(cfg, noise=True, skin=0.075)
+    fs.step(k, 1)
+    g = fs.fetch()
+    fs.close()
+    d = g["pos"].astype(np.float64) - o.pos
+    for a in range(3):
+        if (cfg.pmask >> a) & 1:
+            L = float(cfg.bbox[2 * a + 1] - cfg.bbox[2 * a])
+            d[:, a] -= L * np.rint(d[:, a] / L)
+    vs = float(np.abs(o.vel).max())
+    out = {"steps": k, "noise": "on",
+           "max_position_error": float(np.abs(d).max()),
+           "max_velocity_error_rel": float(np.abs(g["vel"] - o.vel).max() / vs), "max_speed_component": vs}
+    if cfg.ncell:
+        out["max_area_error"] = float(np.abs(g["Area64"] / o.area - 1).max())
+        out["max_volume_error"] = float(np.abs(g["Vol64"] / o.vol - 1).max())
+    return out
+
+
+def run_config_legs(args):
+    """Short legs of the other configurations, so that every bench line
+    carries them: the sheared suspension with Morse aggregation (cfg3) at
+    the three shear rates, and the 2:1 constriction (cfg4) with its FP64
+    area/volume check, `config_steps` steps each."""
+    import copy
+    a = copy.copy(args)
+    a.rouleaux_steps = a.constriction_steps = max(1, args.config_steps)
+    a.rouleaux_every = a.check_every = max(1, args.config_steps // 2)
+    out = {"sheared_suspension": run_rouleaux(a), "constriction": run_constriction(a)}
+    for leg in out["sheared_suspension"]["runs"]:
+        leg.pop("series_columns", None)
+    return out
 
 
 def cell_diameter(cfg):
@@ -848,7 +1025,7 @@ def run_reference(args):
     warm = 3   # warm-up steps (page-in, thread start-up), as for the GPU arm
     for _ in range(warm):
         o.step()
-    steps = max(1, min(args.steps, 3))
+    steps = max(1, min(args.steps, args.ref_steps_cap))
     t0 = time.perf_counter()
     for _ in range(steps):
         o.step()
@@ -870,8 +1047,8 @@ def run_reference(args):
         "data": "synthetic (seeded generator, no dataset)",
         "config": dict(wdesc, particles=cfg.n),
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{steps} full step(s) of the {cfg.n}-particle workload (capped at 3 of the "
-                                   f"{args.steps} requested), FP64, OpenMP"},
+                         "sample": f"{steps} full step(s) of the {cfg.n}-particle workload ({args.steps} requested, "
+                                   f"capped at {args.ref_steps_cap}), FP64, OpenMP"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "GPUCell's GPU kernels are not in the reference and it has no CPU path; this arm is the FP64 "
                 "CPU restatement of the method (oracle/oracle.c)",

@@ -59,6 +59,8 @@ def load():
             getattr(lib, name).restype = C.c_int
         lib.or_geo.argtypes = [S, C.c_int]
         lib.or_neighbor_stats.argtypes = [S, _I, C.POINTER(C.c_uint64)]
+        lib.or_force_scale.argtypes = [S, C.c_int, _D]
+        lib.or_force_scale.restype = C.c_int
         lib.or_membrane_energy.argtypes = [S]
         lib.or_membrane_energy.restype = C.c_double
         lib.or_morse_energy.argtypes = [S]
@@ -154,6 +156,32 @@ class Oracle:
         self.lib.or_neighbor_stats(C.byref(self.st), _ip(cnt), h.ctypes.data_as(C.POINTER(C.c_uint64)))
         return cnt, h
 
+    SCALE_SDPD, SCALE_REP, SCALE_BODY, SCALE_MEMB, SCALE_MORSE, SCALE_EOS, SCALE_ALL = 1, 2, 4, 8, 16, 32, 63
+
+    def force_scale(self, parts=63):
+        """Per particle, the sum of the magnitudes of the terms its force adds
+        up (the parts selected by the SCALE_* bits), on the current state: the
+        scale of FP32 rounding in the force."""
+        out = np.zeros(self.cfg.n)
+        rc = self.lib.or_force_scale(C.byref(self.st), int(parts), _dp(out))
+        if rc != 0:
+            raise RuntimeError(f"or_force_scale failed ({rc})")
+        return out
+
+    def forces_from_density(self, rho):
+        """Re-evaluates every force of the current state in FP64 from the given
+        densities (for instance a GPU's FP32 ones): EOS, SDPD, wall repulsion,
+        body force, membrane geometry and forces, aggregation.  Compared with
+        the GPU's forces this isolates the force pass from the rounding of the
+        density sum, which P = c^2 (rho - rho0) amplifies."""
+        self.set(rho=rho)
+        for name in ("eos", "sdpd_force", "rep_force", "ext_force"):
+            self.call(name)
+        if self.cfg.ncell:
+            self.call("geo", 0)
+            self.call("def_force")
+            self.call("agg_force")
+
     def membrane_energy(self):
         return self.lib.or_membrane_energy(C.byref(self.st))
 
@@ -194,3 +222,50 @@ def philox(ctr, key):
     o = (C.c_uint32 * 4)()
     lib.or_philox4x32_10(c, k, o)
     return list(o)
+
+
+# FP32 unit roundoff
+U32 = 2.0 ** -24
+
+
+def force_error_stats(got, want, scale, rtol=1e-5, k=16.0):
+    """Per-particle comparison of forces (rows of 3) with the oracle's.
+
+    Each particle i must satisfy |dF_i| <= rtol |F_i| + k u S_i, where u is
+    FP32's unit roundoff and S_i the sum of the magnitudes of the terms F_i
+    adds up (Oracle.force_scale): relative error rtol wherever the net force
+    is not a cancellation of much larger terms, and a few roundings of the
+    terms where it is.  Returns the median, 99th percentile and largest
+    relative error |dF_i| / |F_i|, the fraction of particles within rtol
+    relative, and the worst particle against the bound (ratio <= 1 passes)."""
+    got = np.asarray(got, np.float64).reshape(-1, 3)
+    want = np.asarray(want, np.float64).reshape(-1, 3)
+    scale = np.asarray(scale, np.float64).reshape(-1)
+    d = np.linalg.norm(got - want, axis=1)
+    fn = np.linalg.norm(want, axis=1)
+    ok = fn > 0
+    rel = d[ok] / fn[ok]
+    bound = rtol * fn + k * U32 * scale
+    ratio = np.where(bound > 0, d / np.where(bound > 0, bound, 1.0), np.where(d > 0, np.inf, 0.0))
+    w = int(np.argmax(ratio)) if ratio.size else -1
+    return {
+        "particles": int(d.size),
+        "median_rel": float(np.median(rel)) if rel.size else 0.0,
+        "p99_rel": float(np.percentile(rel, 99)) if rel.size else 0.0,
+        "max_rel": float(rel.max()) if rel.size else 0.0,
+        "frac_within_rtol": float((rel <= rtol).mean()) if rel.size else 1.0,
+        "rtol": rtol, "k_roundoff": k,
+        "worst_ratio": float(ratio[w]) if w >= 0 else 0.0,
+        "worst": {"index": w, "dF": float(d[w]), "F": float(fn[w]), "scale": float(scale[w])} if w >= 0 else None,
+    }
+
+
+def assert_forces_close(got, want, scale, rtol=1e-5, k=16.0, what="force"):
+    """force_error_stats, asserting that every particle is within its bound;
+    the message names the worst particle."""
+    s = force_error_stats(got, want, scale, rtol, k)
+    assert s["worst_ratio"] <= 1.0, (
+        f"{what}: particle {s['worst']['index']} has |dF| = {s['worst']['dF']:.3e} against |F| = "
+        f"{s['worst']['F']:.3e} and term scale {s['worst']['scale']:.3e} (bound {rtol:g} |F| + {k:g} u S); "
+        f"median rel {s['median_rel']:.2e}, p99 {s['p99_rel']:.2e}")
+    return s

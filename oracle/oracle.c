@@ -799,6 +799,155 @@ double or_morse_energy(const or_state* s) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Force scale: per particle, the sum of the magnitudes of every term its    */
+/* force adds up (SDPD conservative, dissipative and random pair terms, wall */
+/* repulsion, body force, each spring, bending, area and volume term of a    */
+/* membrane vertex, each Morse pair), on the state as it is; a term that is  */
+/* itself a difference of larger quantities (the pressure c^2 (rho - rho0),  */
+/* the WLC and POW parts of a spring, the area and volume penalties near     */
+/* rest) counts with the size of those quantities.  The rounding error of an */
+/* FP32 evaluation of the force is a small multiple of FP32's unit roundoff  */
+/* times this scale, whatever the cancellation in the net.                   */
+/* ------------------------------------------------------------------------ */
+
+int or_force_scale(const or_state* s, int parts, double* scale) {
+    long n = s->c.nTotalPar;
+    for (long i = 0; i < n; ++i) scale[i] = 0.0;
+    bins_t b;
+    if (bins_build(&b, s, s->c.CutRadius, NULL)) return -1;
+    float rc2 = rc2_f(s);
+    double m = s->c.Mass, eta = s->c.ShearVis, zeta = s->c.BulkVis;
+    double A = 5.0 * eta / 3.0 - zeta, B = 5.0 * (zeta + eta / 3.0);
+    double sA = sqrt(A > 0 ? A : 0), sAB = sqrt(A + B > 0 ? A + B : 0);
+    int noise = s->noise_on && s->c.Temp > 0.f;
+    double pref = noise ? 2.0 * s->c.Temp / s->c.TimeStep : 0.0;
+    float r0f = (float)(s->c.CutRadius / 3.0);
+    float r0sq = r0f * r0f;
+    double r0 = s->c.CutRadius / 3.0, D = (double)s->c.SoundSpeed1 * s->c.SoundSpeed1;
+    set_threads(s);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long i = 0; i < n; ++i) {
+        if (!is_mobile(s, (unsigned)i)) continue;
+        double di = s->rho[i] / m;
+        /* the size of P_i / d_i^2 for rounding: P = c^2 (rho - rho0) is the
+         * difference of two terms of size c^2 rho, and rho is a sum of FP32
+         * kernel values, so its rounding error reaches P as c^2 rho u */
+        const int eos = (parts & OR_SCALE_EOS) != 0;
+        double ci = is_memb(s, (unsigned)i) ? s->c.SoundSpeed2 : s->c.SoundSpeed1;
+        double pi = (fabs(s->press[i]) + (eos ? ci * ci * s->rho[i] : 0.0)) / (di * di);
+        v3 vi = ld3(s->vel, i);
+        double acc = (parts & OR_SCALE_BODY) && s->drive_on ? fabs((double)s->c.ConstExtForce) : 0.0;
+        if (!(parts & (OR_SCALE_SDPD | OR_SCALE_REP))) {
+            scale[i] = acc;
+            continue;
+        }
+        FOR_CANDIDATES(&b, s, i, j, {
+            if (j == i) continue;
+            float r2f = r2_f32(s, i, j);
+            if (is_b1(s, (unsigned)j)) {
+                if (!(parts & OR_SCALE_REP) || r2f >= r0sq || r2f <= 0.f) continue;
+                v3 d = disp(s, i, j);
+                double r2 = dot(d, d), q2 = r0 * r0 / r2, q4 = q2 * q2, q12 = q4 * q4 * q4;
+                acc += fabs(D * (q12 - q4) / r2) * sqrt(r2);
+                continue;
+            }
+            if (!(parts & OR_SCALE_SDPD) || !is_sdpd(s, (unsigned)j) || r2f >= rc2) continue;
+            v3 d = disp(s, i, j);
+            double r = nrm(d), F = wend_f(s, r);
+            double dj = s->rho[j] / m;
+            /* Bound2 density is DenInit exactly: its pressure has no rounding */
+            double cj = is_memb(s, (unsigned)j) ? s->c.SoundSpeed2 : s->c.SoundSpeed1;
+            double pj = (fabs(s->press[j]) + (eos && is_mobile(s, (unsigned)j) ? cj * cj * s->rho[j] : 0.0)) / (dj * dj);
+            acc += fabs((pi + pj) * F) * r;
+            if (r <= 0.0) continue;
+            v3 e = scl(1.0 / r, d), vij = sub(vi, ld3(s->vel, j));
+            double ev = dot(e, vij), fdd = F / (di * dj);
+            acc += fabs(fdd) * (fabs(A) * nrm(vij) + fabs(B * ev));
+            if (noise && fdd > 0.0) {
+                double xi[3];
+                or_pair_noise(s, (unsigned)i, (unsigned)j, xi);
+                v3 x = mk(xi[0], xi[1], xi[2]);
+                acc += sqrt(pref * fdd) * (sA * nrm(x) + fabs((sAB - sA) * dot(e, x)));
+            }
+        });
+        scale[i] = acc;
+    }
+    bins_free(&b);
+    long nc = s->c.nCellStart, ncp = s->c.nCellPar;
+    if (s->ncell <= 0) return 0;
+    /* membrane terms, each added to its vertices as a magnitude */
+    for (int e = 0; e < s->nedge && (parts & OR_SCALE_MEMB); ++e) {
+        const int* E = s->edge + 6 * e;
+        v3 x1 = unwrapped(s, memb_id(s, E[0]));
+        v3 bb = sub(unwrapped(s, memb_id(s, E[1])), x1);
+        v3 c = sub(unwrapped(s, memb_id(s, E[2])), x1);
+        v3 d = sub(unwrapped(s, memb_id(s, E[3])), x1);
+        double r = nrm(bb);
+        /* the WLC and POW terms of the spring separately (they cancel at rest) */
+        double p = s->perlen[e];
+        if (p > 0 && r > 0) {
+            double x = r / s->maxrefedgelen[e];
+            if (x > 0.99) x = 0.99;
+            double u = 1.0 - x;
+            double t = fabs((s->c.Temp / p) * (1.0 / (4.0 * u * u) - 0.25 + x)) + fabs(s->hpow[e] / pow(r, OR_POWM));
+            scale[nc + E[0] - 1] += t;
+            scale[nc + E[1] - 1] += t;
+        }
+        double kb = s->hbending[e];
+        if (kb != 0.0) {
+            dih_t Dh = dihedral(c, mk(0, 0, 0), bb, d);
+            double dE = fabs(kb) * (fabs(Dh.s) + fabs(Dh.c));
+            scale[nc + E[2] - 1] += dE * nrm(Dh.gi);
+            scale[nc + E[0] - 1] += dE * nrm(Dh.gj);
+            scale[nc + E[1] - 1] += dE * nrm(Dh.gk);
+            scale[nc + E[3] - 1] += dE * nrm(Dh.gl);
+        }
+    }
+    for (int c = 0; c < s->ncell && (parts & OR_SCALE_MEMB); ++c) {
+        for (int t = s->betri[2 * c]; t <= s->betri[2 * c + 1]; ++t) {
+            const int* T = s->tri + 3 * t;
+            v3 x1 = unwrapped(s, memb_id(s, T[0]));
+            v3 x2 = sub(unwrapped(s, memb_id(s, T[1])), x1);
+            v3 x3 = sub(unwrapped(s, memb_id(s, T[2])), x1);
+            v3 xi = crs(x2, x3);
+            double len = nrm(xi);
+            if (!(len > 0)) continue;
+            /* each of the area and volume coefficients is a difference of
+             * nearly equal terms near rest: their rounding scales with the
+             * larger term, k |A| / A0 */
+            double cA = fabs(s->hgarea[t]) * s->area[c] / s->refarea[c] + fabs(s->hlarea[t]) * 0.5 * len / s->reftriarea[t];
+            double cV = fabs(s->hvol[t]) * fabs(s->vol[c]) / fabs(s->refvol[c]) / 6.0;
+            v3 nh = scl(1.0 / len, xi);
+            double g[3] = {0.5 * nrm(crs(nh, sub(x3, x2))), 0.5 * nrm(x3), 0.5 * nrm(x2)};
+            for (int k = 0; k < 3; ++k) scale[nc + T[k] - 1] += cV * len + cA * g[k];
+        }
+    }
+    if ((parts & OR_SCALE_MORSE) && s->c.surEnergy != 0.f && s->c.MaxCut > 0.f && ncp > 0) {
+        bins_t mb;
+        if (bins_build(&mb, s, s->c.MaxCut, memb_member)) return -1;
+        float mc2 = s->c.MaxCut * s->c.MaxCut;
+        double De = s->c.surEnergy, beta = s->c.scaFac, rz = s->c.zeroLen;
+#pragma omp parallel for schedule(dynamic, 64)
+        for (long v = 0; v < ncp; ++v) {
+            long i = nc + v;
+            int ci = s->celltab[v];
+            double acc = 0.0;
+            FOR_CANDIDATES(&mb, s, i, j, {
+                long w = j - nc;
+                if (s->celltab[w] == ci) continue;
+                float r2f = r2_f32(s, i, j);
+                if (r2f >= mc2 || r2f <= 0.f) continue;
+                double r = nrm(disp(s, i, j)), ex = exp(beta * (rz - r));
+                acc += 2.0 * De * fabs(beta) * (ex * ex + ex) * 0.5 * (s->pararea[v] + s->pararea[w]);
+            });
+            scale[i] += acc;
+        }
+        bins_free(&mb);
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Full step, Particle::UpdatePar order (src/Particle.cu:1310-1329)          */
 /* ------------------------------------------------------------------------ */
 

@@ -98,6 +98,19 @@ int or_correct(or_state* s);         /* K19 */
  * without the neighbour sort (the oracle keeps original order). */
 int or_step(or_state* s);
 
+/* Per particle (n values): the sum of the magnitudes of the terms its force
+ * adds up, on the state as it is (for the rounding scale of a per-particle
+ * force comparison; see oracle.c), for the parts selected by `parts`. */
+#define OR_SCALE_SDPD  1   /* SDPD pair terms: conservative, dissipative, random */
+#define OR_SCALE_REP   2   /* Bound1 wall repulsion */
+#define OR_SCALE_BODY  4   /* body force (with drive_on) */
+#define OR_SCALE_MEMB  8   /* membrane springs, bending, area, volume */
+#define OR_SCALE_MORSE 16  /* Morse aggregation */
+#define OR_SCALE_EOS   32  /* the pressure term counted at the size of c^2 rho (the rounding of an FP32
+                              density reaches P = c^2 (rho - rho0) at that size); without it at |P| */
+#define OR_SCALE_ALL   63
+int or_force_scale(const or_state* s, int parts, double* scale);
+
 /* Energies for finite-difference checks of the conservative forces. */
 double or_membrane_energy(const or_state* s);   /* springs + bending + area + volume */
 double or_morse_energy(const or_state* s);      /* aggregation */

@@ -77,3 +77,22 @@ def test_metric_name_follows_the_workload_size():
     import bench
     assert bench.metric_name(4194304) == bench.METRIC
     assert bench.metric_name(524288) == "particle-steps/s on 524288-particle RBC suspension"
+
+
+def test_roofline_follows_the_algorithmic_byte_formula():
+    """roofline.frac of the bench line is particle-steps/s x B_alg / N / the
+    HBM peak, with B_alg = 352 N + 16 N_tri + 32 N_edge + 28 N_vert (1.556 GB
+    per step on the 4.2M-particle suspension)."""
+    import types
+    import bench
+    cfg = types.SimpleNamespace(n=4194304, ntri=1024000, nedge=1536000, ncp=512400)
+    b_alg = bench.plain_bytes_per_step(cfg)
+    assert abs(b_alg / 1e9 - 1.556) < 1e-3
+    ms = 4.78
+    roof, kern, issue, fp32 = bench.rooflines(cfg, ms, 2.87, 1.1, 143.0, 6789.3, "measured", None, True)
+    value = cfg.n / (ms / 1e3)
+    assert abs(roof["frac"] - value * b_alg / cfg.n / 1e9 / 6789.3) < 1e-12
+    assert roof["bound"] == "hbm" and roof["unit"] == "GB/s" and roof["peak"] == 6789.3
+    assert abs(kern["fk_force"]["alg_bytes_per_launch"] - 72 * cfg.n) < 1
+    assert kern["fk_force"]["streamed_bytes_per_launch"] > kern["fk_force"]["alg_bytes_per_launch"]
+    assert 0 < issue["frac"] < 2 and 0 < fp32["frac"] < 2

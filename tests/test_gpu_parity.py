@@ -5,7 +5,10 @@ the reference's slot-ordered layout) and into the oracle (original order),
 runs one entry point on both and compares.  Tolerances, stated per test:
   * neighbour sets: bit-exact (count and id checksum per particle);
   * sums of positive terms (density, areas, volumes): 2e-6 relative;
-  * forces: max |dF| <= 1e-5 * max |F| (FP32 sums of ~100 pair terms);
+  * forces, per particle: |dF_i| <= 1e-5 |F_i| + 16 u S_i, with u FP32's unit
+    roundoff and S_i the sum of the magnitudes of the terms F_i adds up (from
+    the oracle): 1e-5 relative unless the net force cancels much larger
+    terms, then a few FP32 roundings of those terms;
   * elementwise integrator stages: 1e-6 relative to the data's scale.
 """
 import ctypes as C
@@ -55,10 +58,12 @@ def _sync_oracle(ps, o):
     return g
 
 
-def _force_close(got, want, tol=1e-5):
-    scale = np.abs(want).max()
-    err = np.abs(got - want).max()
-    assert err <= tol * scale, f"max |dF| = {err:g}, scale {scale:g}"
+def _force_close(got, want, scale, rtol=1e-5, what="force"):
+    from oracle.binding import assert_forces_close
+    s = assert_forces_close(got, want, scale, rtol=rtol, what=what)
+    print(f"\n{what}: median rel {s['median_rel']:.2e}, p99 {s['p99_rel']:.2e}, max {s['max_rel']:.2e}, "
+          f"{100 * s['frac_within_rtol']:.2f} % within {rtol:g}, worst/bound {s['worst_ratio']:.2f}")
+    return s
 
 
 @pytest.fixture(scope="module")
@@ -178,7 +183,7 @@ def test_sdpd_force(cuda_device, channel_cfg, noise):
     ps.sdpd_force()
     g = ps.fetch()
     o.call("sdpd_force")
-    _force_close(g["force"], o.force)
+    _force_close(g["force"], o.force, o.force_scale(o.SCALE_SDPD), what="SDPD force")
 
 
 def test_repulsion_and_body_force(cuda_device, channel_cfg):
@@ -198,12 +203,13 @@ def test_repulsion_and_body_force(cuda_device, channel_cfg):
     ps.rep_force()
     g = ps.fetch()
     o.call("rep_force")
-    _force_close(g["force"], o.force)
+    f0 = np.linalg.norm(st["force"], axis=1)     # the repulsion adds to the forces already there
+    _force_close(g["force"], o.force, f0 + o.force_scale(o.SCALE_REP), what="repulsion")
     assert np.abs(g["force"] - st["force"]).max() > 0
     ps.ext_force(1)
     g = ps.fetch()
     o.call("ext_force")
-    _force_close(g["force"], o.force)
+    _force_close(g["force"], o.force, f0 + o.force_scale(o.SCALE_REP | o.SCALE_BODY), what="repulsion + body force")
 
 
 def test_membrane_setup(cuda_device, channel_cfg):
@@ -235,8 +241,10 @@ def test_geometry_and_deformation_force(cuda_device, channel_cfg):
     np.testing.assert_allclose(g["TriNorDir"], o.trinormal, atol=1e-5)
     np.testing.assert_allclose(g["TriCenter"], o.tricenter, atol=1e-5)
     np.testing.assert_allclose(g["ParArea"], o.pararea, rtol=1e-5)
-    _force_close(g["DefForce"], o.defforce, tol=2e-5)
-    _force_close(g["force"], o.force, tol=2e-5)
+    sc = o.force_scale(o.SCALE_MEMB)
+    cs = channel_cfg.n_cell_start
+    _force_close(g["DefForce"], o.defforce, sc[cs:], what="deformation force")
+    _force_close(g["force"], o.force, sc, what="force")
 
 
 def test_aggregation_force(cuda_device, two_cell_cfg):
@@ -249,8 +257,10 @@ def test_aggregation_force(cuda_device, two_cell_cfg):
     o.call("geo", 0)
     o.call("agg_force")
     assert np.abs(o.aggforce).max() > 0
-    _force_close(g["AggForce"], o.aggforce)
-    _force_close(g["force"], o.force)
+    sc = o.force_scale(o.SCALE_MORSE)
+    cs = two_cell_cfg.n_cell_start
+    _force_close(g["AggForce"], o.aggforce, sc[cs:], what="aggregation force")
+    _force_close(g["force"], o.force, sc, what="force")
 
 
 def test_full_steps_track_the_oracle(cuda_device, channel_cfg):

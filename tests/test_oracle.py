@@ -234,3 +234,33 @@ def test_noise_on_steps_stay_finite_and_hot():
         o.step()
         assert np.isfinite(o.pos).all() and np.isfinite(o.vel).all() and np.isfinite(o.force).all()
     assert (o.vel ** 2).sum(axis=1).mean() > 0.1   # the noise heats the fluid
+
+
+@pytest.mark.parametrize("noise", [False, True])
+def test_force_scale_bounds_every_force(oracle_lib, noise):
+    """The per-particle scale of the force comparisons (the sum of the
+    magnitudes of the terms a force adds up) is at least the force itself,
+    part by part and in total (triangle inequality), on a walled channel
+    with a cell and on a periodic suspension with Morse aggregation."""
+    import dataclasses
+    from oracle.binding import Oracle
+    phys = dataclasses.replace(gen.Physics(), sur_energy=5.0, max_cut=1.2, zero_len=0.3, sca_fac=4.0)
+    for cfg in (gen.small_channel(), gen.suspension(nx=24, ny=24, nz=24, ncells=2, subdiv=2, hematocrit=0.15,
+                                                    seed=3, phys=phys)):
+        o = Oracle(cfg, noise=noise)
+        o.setup()
+        o.step()
+        o.step()
+        f = np.linalg.norm(o.force, axis=1)
+        s = o.force_scale()
+        mov = np.arange(cfg.n) >= cfg.n_b1 + cfg.n_b2
+        assert (s[mov] >= f[mov] * (1 - 1e-12)).all()
+        assert (s[~mov] == 0).all()
+        cs = cfg.n_cell_start
+        sm = o.force_scale(o.SCALE_MEMB)[cs:]
+        assert (sm >= np.linalg.norm(o.defforce, axis=1) * (1 - 1e-12)).all()
+        if cfg.phys.sur_energy:
+            sa = o.force_scale(o.SCALE_MORSE)[cs:]
+            assert (sa >= np.linalg.norm(o.aggforce, axis=1) * (1 - 1e-12)).all()
+        assert np.allclose(s, sum(o.force_scale(p) for p in (1 | 32, 2, 4, 8, 16)))
+        assert (o.force_scale(31) <= s).all()
