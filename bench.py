@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skin", type=float, default=0.075)
     ap.add_argument("--block", type=int, default=128)
+    ap.add_argument("--tiles", action="store_true",
+                    help="pair tiles (each pair once, both sides from one evaluation) instead of per-particle lists")
     ap.add_argument("--no-compact", dest="compact", action="store_false",
                     help="force pass iterates the skin lists instead of the per-step compact lists")
     ap.add_argument("--no-plain", dest="plain", action="store_false", help="skip the FP32 boundary-path timing")
@@ -189,6 +191,9 @@ FORCE_ALG_BYTES = 44 + 28
 # list entries it streams (4 B each) come on top: the Verlet lists are an
 # implementation overhead of the fused step, not algorithmic bytes.
 FORCE_STATE_BYTES = 16 * 3 + 8 + 16 * 2 + 4
+# Partial sums of the pair tiles per particle, written by the pair pass and
+# read back by its finish: 14 directions x 3 floats (force), x 1 (density).
+TILE_PARTIAL_BYTES = {"force": 2 * 14 * 12, "density": 2 * 14 * 4}
 
 # Counters from one-kernel ncu captures of fk_force (they are constants of
 # the kernel's code, refreshed whenever it changes; the line says which
@@ -214,7 +219,7 @@ GB300_SCHEDULERS = 152 * 4
 GB300_FP32_FLOP_PER_CYCLE = 152 * 128 * 2
 
 
-def rooflines(cfg, ms_per_step, force_ms, dens_ms, mean_nb, hbm, peak_kind, clocks, full_size):
+def rooflines(cfg, ms_per_step, force_ms, dens_ms, mean_nb, hbm, peak_kind, clocks, full_size, tiles=False):
     """The roofline objects of the bench line.
 
     `roofline`: the whole step against HBM, with the algorithmic bytes of the
@@ -248,9 +253,21 @@ def rooflines(cfg, ms_per_step, force_ms, dens_ms, mean_nb, hbm, peak_kind, cloc
                 "the fused step is bound by instruction issue in its pair kernels (issue_roofline)",
     }
     f_alg = FORCE_ALG_BYTES * n
-    f_streamed = n * (FORCE_STATE_BYTES + 4 * mean_nb)
     d_alg = 20 * n
-    d_streamed = n * (24 + 4 * mean_nb)
+    if tiles:
+        # pair tiles: one 4-byte entry per candidate pair (mean_nb / 2 per
+        # particle), 14 partial-sum planes written and read back by the finish
+        f_streamed = n * (FORCE_STATE_BYTES + TILE_PARTIAL_BYTES["force"] + 4 * mean_nb / 2)
+        d_streamed = n * (24 + TILE_PARTIAL_BYTES["density"] + 4 * mean_nb / 2)
+        f_note = (f"streamed = {FORCE_STATE_BYTES} B of the particle's records + {TILE_PARTIAL_BYTES['force']} B of "
+                  f"partial sums per particle + 4 B per candidate pair ({mean_nb / 2:.1f} per particle)")
+        d_note = (f"streamed = 24 + {TILE_PARTIAL_BYTES['density']} B of partial sums per particle + 4 B per "
+                  "candidate pair")
+    else:
+        f_streamed = n * (FORCE_STATE_BYTES + 4 * mean_nb)
+        d_streamed = n * (24 + 4 * mean_nb)
+        f_note = f"streamed = {FORCE_STATE_BYTES} B per particle + 4 B per list entry (mean list {mean_nb:.1f})"
+        d_note = "streamed = 24 B per particle + 4 B per list entry"
     kern = {
         "fk_force": {
             "launch_ms": force_ms, "bound": "hbm", "unit": "GB/s", "peak": hbm, "peak_source": peak_src,
@@ -261,8 +278,7 @@ def rooflines(cfg, ms_per_step, force_ms, dens_ms, mean_nb, hbm, peak_kind, cloc
             "traffic": FORCE_COUNTERS["dram_bytes_per_launch_4M"] if full_size else None,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at full size "
                               f"({FORCE_COUNTERS['kernel_version']})",
-            "note": f"alg = {FORCE_ALG_BYTES} B per particle (force 44 + corrector 28); streamed = "
-                    f"{FORCE_STATE_BYTES} B per particle + 4 B per list entry (mean list {mean_nb:.1f}: overhead)",
+            "note": f"alg = {FORCE_ALG_BYTES} B per particle (force 44 + corrector 28); {f_note} (overhead)",
         },
         "fk_density": {
             "launch_ms": dens_ms, "bound": "hbm", "unit": "GB/s", "peak": hbm,
@@ -270,8 +286,7 @@ def rooflines(cfg, ms_per_step, force_ms, dens_ms, mean_nb, hbm, peak_kind, cloc
             "frac": d_alg / (dens_ms / 1e3) / 1e9 / hbm,
             "streamed_bytes_per_launch": d_streamed,
             "streamed_frac": d_streamed / (dens_ms / 1e3) / 1e9 / hbm,
-            "note": "alg = 20 B per particle (position read, density written); streamed = 24 B per particle + "
-                    "4 B per list entry",
+            "note": f"alg = 20 B per particle (position read, density written); {d_note}",
         },
     }
     mhz = clocks["sm_mhz"] if clocks else 2070.0
@@ -394,7 +409,7 @@ def run_ours(args):
     engine = measure_plain(cfg, dev, steps=K, warmup=3, engine=True) if args.engine else None
 
     fs = FusedSystem(cfg, noise=args.noise, skin=args.skin, block=args.block, compact=args.compact,
-                     graph=args.graph)
+                     graph=args.graph, tiles=args.tiles)
     fs.step(W, 1)
     tuned = fs.autotune(trial_steps=args.tune_steps) if args.tune else None
     fs.step(2, 1)   # settle (captures the step graph when one is used)
@@ -484,7 +499,8 @@ def run_ours(args):
     force_ms = prof["force_ms"] / max(prof["steps"], 1)
     dens_ms = prof["density_ms"] / max(prof["steps"], 1)
     roof, roof_kernels, issue_roof, fp32_roof = rooflines(cfg, t_ms / K, force_ms, dens_ms, mean_nb, hbm, peak_kind,
-                                                          clocks, full_size=(not args.small and n == 4194304))
+                                                          clocks, full_size=(not args.small and n == 4194304),
+                                                          tiles=opts["tiles"])
 
     fs.close()
     ens = run_ensemble(args, dev, rank, world, barrier, max_over_ranks) if args.ensemble else None
@@ -508,12 +524,15 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "fp32 pair physics; double-float (fp32 pair) positions; fp64 membrane area/volume sums",
         "data": "synthetic (seeded generator, no dataset)",
-        "variant": "fused step: Verlet lists with skin, fused passes (gc_fused_*)",
+        "variant": ("fused step, pair tiles: each pair once per pass, both sides from one evaluation "
+                    "(gc_fused_*)") if opts["tiles"] else
+                   "fused step: per-particle Verlet lists with skin, fused passes (gc_fused_*)",
         "config": dict(wdesc, particles=n, membrane_vertices=cfg.ncp, triangles=cfg.ntri, edges=cfg.nedge,
                        parallelism=f"replicas x{world}" if world > 1 else "single GPU",
                        l2="working set (>1 GB: state + neighbour lists) is larger than L2; no flush",
                        noise="on" if args.noise else "off", skin=opts["skin"], block=opts["block"],
-                       compact_lists=opts["compact"], captured_steps=opts["graph"],
+                       pair_tiles=opts["tiles"], compact_lists=None if opts["tiles"] else opts["compact"],
+                       captured_steps=opts["graph"],
                        autotuned=tuned),
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": bi,
@@ -531,7 +550,7 @@ def run_ours(args):
                              "max_speed": diag["max_speed"], "mean_fluid_density": diag["mean_fluid_density"],
                              "note": "after the timed steps, reduced on the GPU in FP64 (gc_ensemble_diagnostics)"},
         "parity": parity,
-        "lists": {"rebuilds_in_timed_steps": st1["rebuilds"] - st0["rebuilds"], "mean_length": mean_nb,
+        "lists": {"rebuilds_in_timed_steps": st1["rebuilds"] - st0["rebuilds"], "mean_neighbors": mean_nb,
                   "max_length": st1["max_neighbors"], "capacity": st1["capacity"]},
         "device_flags": flags,
     }
@@ -840,7 +859,7 @@ def force_parity(cfg):
     parts = (("all", slice(None)), ("fluid", slice(0, cs)), ("membrane", slice(cs, None)))
     for name, sl in parts:
         out["force_evaluation"][name] = force_error_stats(g["force"][mov][sl], o.force[mov][sl], scale[mov][sl])
-    o.forces_from_density(g["rho"])
+    o.forces_from_density(g["rho"], g["press"])
     scale = o.force_scale(31)
     for name, sl in parts:
         out["force_given_gpu_density"][name] = force_error_stats(g["force"][mov][sl], o.force[mov][sl],
@@ -849,7 +868,7 @@ def force_parity(cfg):
                                        "own FP64 densities: per particle |dF_i| <= 1e-5 |F_i| + 16 u S_i, the pressure "
                                        "term counted at c^2 rho in S_i (worst_ratio <= 1 passes)")
     out["force_given_gpu_density"]["what"] = ("the same forces against the oracle's FP64 forces from the GPU's FP32 "
-                                              "densities, the pressure term counted at |P| in S_i")
+                                              "densities and pressures, the pressure term counted at |P| in S_i")
     del o
     return out
 

@@ -17,6 +17,7 @@ GC_FLAG_NONFINITE = 1
 GC_FLAG_BAD_INDEX = 2
 GC_FLAG_CELL_OVERFLOW = 4
 GC_FLAG_STRETCH = 8
+GC_FLAG_TILE_FULL = 16
 
 
 class Structconst(C.Structure):
@@ -54,7 +55,7 @@ class GcFusedOptions(C.Structure):
     """ctypes mirror of GcFusedOptions (include/gpucell_gb300.h)."""
 
     _fields_ = [("skin", C.c_float), ("block", C.c_int), ("list_capacity", C.c_int), ("compact", C.c_int),
-                ("graph", C.c_int), ("reserved", C.c_int * 3)]
+                ("graph", C.c_int), ("tiles", C.c_int), ("reserved", C.c_int * 2)]
 
 
 assert C.sizeof(GcFusedOptions) == 32

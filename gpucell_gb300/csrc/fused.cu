@@ -55,50 +55,6 @@ namespace gcf {
 
 
 
-__device__ __forceinline__ int stype(unsigned id, const SysInfo& S) {
-    return id < S.b2 ? PT_B1 : (id < S.fl ? PT_B2 : (id < S.cs ? PT_FLUID : PT_MEMB));
-}
-
-// System of the given global id (binary search over the id ranges).
-__device__ __forceinline__ int find_sys(const SysInfo* sys, int nsys, unsigned id) {
-    int lo = 0, hi = nsys - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (sys[mid].id0 <= id) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
-// Box constants of the per-step kernels.
-struct Box {
-    float L[3], invL[3];
-    int pmask;
-};
-
-__device__ __forceinline__ Box box_of(const SysInfo& S) {
-    Box b;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        b.L[a] = S.g.L[a];
-        b.invL[a] = S.invL[a];
-    }
-    b.pmask = S.g.pmask;
-    return b;
-}
-
-// Minimum image of a list pair.  A listed pair is either far closer than
-// L/2 or close to L apart along a periodic axis, so d - L rint(d/L) makes
-// the same shift as the conditional form of the boundary kernels and
-// rounds the same way (one subtraction of L), i.e. the same FP32 value.
-__device__ __forceinline__ float3 pair_image(float3 a, float3 b, const Box& B) {
-    float3 d = f3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
-    if (B.pmask & 1) d.x = fmaf(-B.L[0], rintf(d.x * B.invL[0]), d.x);
-    if (B.pmask & 2) d.y = fmaf(-B.L[1], rintf(d.y * B.invL[1]), d.y);
-    if (B.pmask & 4) d.z = fmaf(-B.L[2], rintf(d.z * B.invL[2]), d.z);
-    return d;
-}
-
 // Pair difference without the image shift: exact for a particle farther
 // than rc + 2 skin from every periodic face (its listed partners, which have
 // moved at most skin/2 each since the lists were built, are then less than
@@ -118,13 +74,6 @@ __device__ __forceinline__ bool near_face(float3 x, const GcGrid& g, float margi
     if (g.pmask & 4) w |= (x.z - g.lo[2] < margin) || (g.hi[2] - x.z <= margin);
     return w;
 }
-
-// The per-step kernels exist in two forms.  ENS = false: one system, given
-// by value in the kernel parameters (constant bank, no per-thread loads).
-// ENS = true: the system of each slot comes from the per-slot index and the
-// device table (ensembles, and captured steps, whose noise keys are derived
-// on the device).
-#define GC_SYS_OF(S, i) const SysInfo& S = ENS ? sys[sysid ? sysid[i] : 0] : s0
 
 // ---------------------------------------------------------------------------
 // Step prologue on the device: advance the step counter, derive every
@@ -321,7 +270,7 @@ __global__ void __launch_bounds__(kMaxBS, GC_BUILD_MIN_BLOCKS) fk_build_list(int
                                                      const int* __restrict__ sysid, const float4* __restrict__ pos,
                                                      const unsigned* __restrict__ start, int* __restrict__ nbr,
                                                      int* __restrict__ cnt, int cap, float cut2, unsigned* flags,
-                                                     int* __restrict__ need) {
+                                                     int* __restrict__ need, int walls_only) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 xi4 = pos[i];
@@ -329,6 +278,10 @@ __global__ void __launch_bounds__(kMaxBS, GC_BUILD_MIN_BLOCKS) fk_build_list(int
     unsigned id = fid(xi4);
     const SysInfo& S = sys[sysid ? sysid[i] : 0];
     int t = stype(id, S);
+    if (walls_only && t != PT_B2) {   // the pair tiles cover the other slots
+        cnt[i] = 0;
+        return;
+    }
     int k = 0;
     const GcGrid& g = S.g;
     const unsigned fl = S.fl;
@@ -1342,6 +1295,21 @@ int ensure_agg_sort_bufs(GcFused* f) {
 // Per-system list grids (cubes at least rc + skin wide) and aggregation
 // grids, their global cube offsets, and the device copy of the table.
 int build_grids(GcFused* f) {
+    if (!f->lists) {
+        // the pair tiles need at least three cubes of rc + skin along every
+        // periodic axis; a smaller box takes per-particle lists over
+        // half-width cells instead
+        for (int s = 0; s < f->nsys; ++s) {
+            const GcSystemDesc& d = f->desc[s];
+            const float cut = d.consts.CutRadius + f->skin;
+            for (int a = 0; a < 3; ++a)
+                if ((d.periodic_mask >> a) & 1) {
+                    const double L = (double)d.bbox[2 * a + 1] - (double)d.bbox[2 * a];
+                    if (floor(L / ((double)cut * (1.0 + 1e-4))) < 3.0) f->lists = true;
+                }
+        }
+        if (f->lists) drop_graphs(f);
+    }
     int K = 0, Kagg = 0;
     for (int s = 0; s < f->nsys; ++s) {
         SysInfo& S = f->hsys[s];
@@ -1350,7 +1318,7 @@ int build_grids(GcFused* f) {
         // 3x3x3 cubes) wherever every periodic axis has at least 5 of them
         const float cut = d.consts.CutRadius + f->skin;
         S.lr = 2;
-        if (gc_build_grid(d.bbox, 0.5f * cut, d.periodic_mask, &S.g) != GC_OK ||
+        if (!f->lists || gc_build_grid(d.bbox, 0.5f * cut, d.periodic_mask, &S.g) != GC_OK ||
             ((d.periodic_mask & 1) && S.g.n[0] < 5) || ((d.periodic_mask & 2) && S.g.n[1] < 5) ||
             ((d.periodic_mask & 4) && S.g.n[2] < 5)) {
             S.lr = 1;
@@ -1384,6 +1352,7 @@ int build_grids(GcFused* f) {
                 "fused: system table");
     GC_TRY(ensure_sort_bufs(f));
     GC_TRY(ensure_agg_sort_bufs(f));
+    GC_TRY(tiles_grid(f));
     drop_graphs(f);
     return GC_OK;
 }
@@ -1413,6 +1382,17 @@ int grown_capacity(const GcFused* f, int at_least) {
     return ((want > at_least ? want : at_least) + 7) & ~7;
 }
 
+// Turns a handle from pair tiles to per-particle lists (a cube holds more
+// particles than the tiles take): half-width cells where they fit, lists
+// for every slot.
+int switch_to_lists(GcFused* f) {
+    f->lists = true;
+    GC_TRY(build_grids(f));
+    GC_TRY(alloc_list(f, f->cap));
+    drop_graphs(f);
+    return GC_OK;
+}
+
 int rebuild_lists(GcFused* f) {
     const int n = f->n;
     const int nb = gc_blocks(n, f->block);
@@ -1424,13 +1404,26 @@ int rebuild_lists(GcFused* f) {
     GC_CHECK_LAUNCH("fused: permute");
     std::swap(f->a, f->b);
     drop_graphs(f);   // captured steps are bound to the old slot arrays
+    if (!f->lists) {
+        GC_TRY(wall_lists(f, st, f->a.pos, true));
+        GC_CUDA(cudaMemsetAsync(f->oflag, 0, sizeof(unsigned), st), "fused: flags");
+        GC_TRY(tiles_build(f, st, f->a.pos, true));
+        if (f->h->oflag & GC_FLAG_TILE_FULL) {
+            // a cube holds more particles than the tiles take: per-particle
+            // lists from now on (another grid, so sort again)
+            GC_TRY(switch_to_lists(f));
+            return rebuild_lists(f);
+        }
+        f->rebuilds++;
+        return GC_OK;
+    }
     float cut = f->p.rc + f->skin;
     float cut2 = cut * cut;
     for (int attempt = 0; attempt < 4; ++attempt) {
         GC_CUDA(cudaMemsetAsync(f->oflag, 0, sizeof(unsigned), st), "fused: flags");
         GC_CUDA(cudaMemsetAsync(f->need, 0, sizeof(int), st), "fused: flags");
         fk_build_list<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->a.pos, f->sb.cnt, f->nbr, f->cnt, f->cap,
-                                              cut2, f->oflag, f->need);
+                                              cut2, f->oflag, f->need, 0);
         GC_CHECK_LAUNCH("fused: build lists");
         GC_CUDA(cudaMemcpyAsync(&f->h->oflag, f->oflag, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "fused: flags");
         GC_CUDA(cudaMemcpyAsync(&f->h->need, f->need, sizeof(int), cudaMemcpyDeviceToHost, st), "fused: flags");
@@ -1478,6 +1471,7 @@ int launch_integrate(GcFused* f, cudaStream_t st, const GcParams& p) {
 }
 
 int launch_density(GcFused* f, cudaStream_t st, const GcParams& p, bool mark) {
+    if (!f->lists) return launch_tile_density(f, st, p, false);
     const int n = f->n, nb = gc_blocks(n, f->block);
     unsigned* cm = mark && f->compact ? f->cmask : nullptr;
     int* cc = mark && f->compact ? f->ccnt : nullptr;
@@ -1547,6 +1541,7 @@ void force_launch(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
 }
 
 int launch_force(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
+    if (!f->lists) return launch_tile_force(f, st, p, drive, false);
     if (f->compact) force_launch<true>(f, st, p, drive);
     else force_launch<false>(f, st, p, drive);
     GC_CHECK_LAUNCH("fused: force");
@@ -1635,9 +1630,13 @@ int launch_rebuild_body(GcFused* f, cudaStream_t st) {
     GC_CHECK_LAUNCH("fused: permute");
     fk_copy_slots<<<nb, f->block, 0, st>>>(n, f->b, f->a);
     GC_CHECK_LAUNCH("fused: copy slots");
+    if (!f->lists) {
+        GC_TRY(wall_lists(f, st, f->a.pos, false));
+        return tiles_build(f, st, f->a.pos, false);
+    }
     float cut = f->p.rc + f->skin;
     fk_build_list<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->a.pos, f->sb.cnt, f->nbr, f->cnt, f->cap,
-                                          cut * cut, f->oflag, f->need);
+                                          cut * cut, f->oflag, f->need, 0);
     GC_CHECK_LAUNCH("fused: build lists");
     return GC_OK;
 }
@@ -1788,6 +1787,14 @@ int refresh(GcFused* f) {
 int prepare_graph(GcFused* f, int drive) {
     if (f->graph_dirty) {
         GC_TRY(rebuild_lists(f));
+        if (!f->lists) {
+            // room in the pair lists for the rebuilds inside captured steps
+            const size_t want = (size_t)(1.25 * f->h->tchunks) + 256;
+            if (want > f->tent_chunks) {
+                GC_TRY(tiles_alloc_entries(f, want));
+                GC_TRY(rebuild_lists(f));
+            }
+        }
         // capacity for captured steps: the longest list now plus a margin
         GC_CUDA(cudaMemsetAsync(f->stat_max, 0, sizeof(int), f->st), "fused: stats");
         GC_CUDA(cudaMemsetAsync(f->stat_sum, 0, sizeof(unsigned long long), f->st), "fused: stats");
@@ -1839,17 +1846,28 @@ int graph_segment(GcFused* f, int nsteps, int drive) {
         long long nreb = (long long)(f->h->drebuilds - f->drebuilds_seen);
         f->drebuilds_seen = f->h->drebuilds;
         gc_add_launches(f->kernels_step * nsteps + f->kernels_rebuild * nreb);
-        if (!(f->h->oflag & GC_FLAG_CELL_OVERFLOW)) {
+        if (!(f->h->oflag & (GC_FLAG_CELL_OVERFLOW | GC_FLAG_TILE_FULL))) {
             f->step = step0 + nsteps;
             f->steps += nsteps;
             f->rebuilds += nreb;
             return GC_OK;
         }
         // a list overflowed: go back to the state before these steps, grow
-        // the lists and run them again
+        // the lists (or, with a cube too full for the pair tiles, turn to
+        // per-particle lists) and run them again
         GC_TRY(restore_state(f, &f->snap));
         f->step = step0;
-        GC_TRY(alloc_list(f, grown_capacity(f, f->cap + f->cap / 2 + 8)));
+        if (f->h->oflag & GC_FLAG_TILE_FULL) {
+            GC_TRY(switch_to_lists(f));
+        } else if (!f->lists) {
+            unsigned need = 0;
+            GC_CUDA(cudaMemcpy(&need, f->toff + (size_t)f->K * kTilePairs, sizeof(unsigned), cudaMemcpyDeviceToHost),
+                    "fused: tiles");
+            GC_TRY(tiles_alloc_entries(f, (size_t)(1.25 * (need > f->tent_chunks ? need : f->tent_chunks)) + 256));
+            if (f->h->need > 0) GC_TRY(alloc_list(f, grown_capacity(f, f->cap + f->cap / 2 + 8)));
+        } else {
+            GC_TRY(alloc_list(f, grown_capacity(f, f->cap + f->cap / 2 + 8)));
+        }
         f->graph_dirty = true;
     }
     return gc_fail(GC_EDEVICE, "fused: neighbour lists keep overflowing in captured steps (capacity %d)", f->cap);
@@ -2044,6 +2062,7 @@ int apply_options(GcFused* f, const GcFusedOptions* opt) {
     if (opt->block) f->block = opt->block;
     f->compact = opt->compact != 0;
     f->graph = opt->graph != 0;
+    f->lists = opt->tiles == 0;
     return GC_OK;
 }
 
@@ -2279,6 +2298,7 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
         }
         double cutr = f->p.rc + f->skin;
         int capn = (int)(2.0 * 4.18879 * cutr * cutr * cutr * dens) + 32;
+        if (!f->lists && !any_bound2(f)) capn = 8;   // the pair tiles need lists only for Bound2 walls
         if (opt && opt->list_capacity > 0) capn = opt->list_capacity;
         capn = (capn + 7) & ~7;
         ok = alloc_list(f, capn);
@@ -2296,6 +2316,7 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
         f->h->drebuilds = 0;
         f->h->need = 0;
         if (cudaMemsetAsync(f->flags, 0, sizeof(unsigned), f->st) != cudaSuccess ||
+            cudaMemsetAsync(f->cnt, 0, (size_t)n * sizeof(int), f->st) != cudaSuccess ||   // lists of no slot yet
             cudaMemsetAsync(f->drebuilds, 0, 8, f->st) != cudaSuccess ||
             cudaMemsetAsync(f->dstep, 0xff, 8, f->st) != cudaSuccess)   // -1
             ok = gc_fail(GC_ECUDA, "fused: clear counters");
@@ -2506,6 +2527,14 @@ int gc_fused_stats(GcFused* f, long long* rebuilds, long long* steps, int* list_
     if (rebuilds) *rebuilds = f->rebuilds;
     if (steps) *steps = f->steps;
     if (list_capacity) *list_capacity = f->cap;
+    if (!f->lists && mean_neighbors) {
+        // pair tiles: each candidate pair counts for both of its particles
+        unsigned long long pairs = 0;
+        GC_CUDA(cudaMemcpyAsync(&pairs, f->tpairs, 8, cudaMemcpyDeviceToHost, f->st), "stats");
+        GC_CUDA(cudaStreamSynchronize(f->st), "stats");
+        *mean_neighbors = 2.0 * (double)pairs / (f->n > 0 ? f->n : 1);
+        mean_neighbors = nullptr;
+    }
     if (mean_neighbors || max_neighbors) {
         GC_CUDA(cudaMemsetAsync(f->stat_sum, 0, sizeof(unsigned long long), f->st), "stats");
         GC_CUDA(cudaMemsetAsync(f->stat_max, 0, sizeof(int), f->st), "stats");
@@ -2517,7 +2546,7 @@ int gc_fused_stats(GcFused* f, long long* rebuilds, long long* steps, int* list_
         GC_CUDA(cudaMemcpyAsync(&m, f->stat_max, 4, cudaMemcpyDeviceToHost, f->st), "stats");
         GC_CUDA(cudaStreamSynchronize(f->st), "stats");
         if (mean_neighbors) *mean_neighbors = (double)s / (f->n > 0 ? f->n : 1);
-        if (max_neighbors) *max_neighbors = m;
+        if (max_neighbors) *max_neighbors = m;   // with pair tiles: the walls' lists
     }
     return GC_OK;
 }
@@ -2564,6 +2593,7 @@ int gc_fused_get_options(GcFused* f, GcFusedOptions* opt) {
     opt->list_capacity = f->cap;
     opt->compact = f->compact ? 1 : 0;
     opt->graph = f->graph ? 1 : 0;
+    opt->tiles = f->lists ? 0 : 1;
     return GC_OK;
 }
 
@@ -2571,11 +2601,12 @@ int gc_fused_set_options(GcFused* f, const GcFusedOptions* opt) {
     if (!f || !opt) return gc_fail(GC_EINVAL, "fused_set_options: NULL argument");
     float old_skin = f->skin_rel;
     bool old_compact = f->compact;
+    bool old_lists = f->lists;
     int old_block = f->block;
     GC_TRY(apply_options(f, opt));
     f->skin = f->skin_rel * f->p.rc;
     f->ens = f->nsys > 1 || f->graph;
-    bool regrid = f->skin_rel != old_skin;
+    bool regrid = f->skin_rel != old_skin || f->lists != old_lists;
     if (regrid) GC_TRY(build_grids(f));
     int cap = f->cap;
     if (opt->list_capacity > cap) cap = (opt->list_capacity + 7) & ~7;
@@ -2585,6 +2616,8 @@ int gc_fused_set_options(GcFused* f, const GcFusedOptions* opt) {
     }
     GC_TRY(alloc_list(f, cap));
     if (f->compact != old_compact || f->block != old_block) drop_graphs(f);
+    if (f->lists && !old_lists && cap < 16) cap = 64;   // every slot lists again (grown on overflow)
+    if (f->lists != old_lists) GC_TRY(alloc_list(f, cap));
     if (f->setup_done) {
         GC_TRY(sync_dstep(f));
         if (regrid || f->compact != old_compact || opt->list_capacity > 0) GC_TRY(refresh(f));
@@ -2611,6 +2644,9 @@ int gc_fused_destroy(GcFused* f) {
     for (void* q : f->allocs) cudaFree(q);
     if (f->nbr) cudaFree(f->nbr);
     if (f->cmask) cudaFree(f->cmask);
+    for (void* q : {(void*)f->cube_sys, (void*)f->bmask, (void*)f->tnb, (void*)f->toff, (void*)f->tscan,
+                    (void*)f->tent, (void*)f->pd, (void*)f->pf, (void*)f->tpairs})
+        if (q) cudaFree(q);
     if (f->sortmem) cudaFree(f->sortmem);
     if (f->stage) cudaFree(f->stage);
     if (f->h) cudaFreeHost(f->h);

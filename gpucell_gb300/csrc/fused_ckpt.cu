@@ -112,12 +112,21 @@ int rebuild_from_ref(GcFused* f) {
     fk_iota<<<nb, f->block, 0, st>>>(n, f->vals);
     GC_CHECK_LAUNCH("restore: identity");
     GC_TRY(gc_counting_sort_bufs(n, f->K, f->keys, f->vals, f->sb, f->flags, st));
+    if (!f->lists) {
+        GC_TRY(wall_lists(f, st, f->refpos, true));
+        GC_CUDA(cudaMemsetAsync(f->oflag, 0, sizeof(unsigned), st), "restore: flags");
+        GC_TRY(tiles_build(f, st, f->refpos, true));
+        if (f->h->oflag & GC_FLAG_TILE_FULL)
+            return gc_fail(GC_EDEVICE, "restore: a cube holds more particles than the pair tiles take; restore into "
+                                       "a handle with per-particle lists (GcFusedOptions.tiles = 0)");
+        return GC_OK;
+    }
     float cut = f->p.rc + f->skin;
     for (int attempt = 0; attempt < 4; ++attempt) {
         GC_CUDA(cudaMemsetAsync(f->oflag, 0, sizeof(unsigned), st), "restore: flags");
         GC_CUDA(cudaMemsetAsync(f->need, 0, sizeof(int), st), "restore: flags");
         fk_build_list<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->refpos, f->sb.cnt, f->nbr, f->cnt, f->cap,
-                                              cut * cut, f->oflag, f->need);
+                                              cut * cut, f->oflag, f->need, 0);
         GC_CHECK_LAUNCH("restore: build lists");
         GC_CUDA(cudaMemcpyAsync(&f->h->oflag, f->oflag, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "restore");
         GC_CUDA(cudaMemcpyAsync(&f->h->need, f->need, sizeof(int), cudaMemcpyDeviceToHost, st), "restore");

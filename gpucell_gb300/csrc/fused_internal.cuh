@@ -18,6 +18,14 @@ namespace gcf {
 constexpr int kBS = 128;      // default threads per block
 constexpr int kMaxBS = 256;   // largest block the particle kernels accept
 
+// Pair tiles (the half-stencil passes, fused_tiles.cu): particles are sorted
+// by cubes at least rc + skin wide; each cube pairs with itself and its 13
+// forward neighbours, and one warp takes a home cube and its 14 pairs.
+constexpr int kTilePairs = 14;
+constexpr int kTileMax = 96;       // particles per cube the tiles accept (local indices fit a byte)
+constexpr int kTileWarps = 4;      // warps per block of the tile kernels
+constexpr unsigned kTilePad = 0xFFFFFFFFu;   // padding entry of a pair list
+
 __device__ __forceinline__ unsigned fid(float4 x) { return __float_as_uint(x.w); }
 __device__ __forceinline__ float3 xyz(float4 a) { return f3(a.x, a.y, a.z); }
 
@@ -73,6 +81,59 @@ struct SysInfo {
     GcGrid g;                        // list grid over the box
     GcGrid mg;                       // aggregation grid: cubes at least MaxCut wide
 };
+
+// Particle type, system lookup, box constants and the minimum image of a
+// listed pair, shared by the list and the tile passes.
+__device__ __forceinline__ int stype(unsigned id, const SysInfo& S) {
+    return id < S.b2 ? PT_B1 : (id < S.fl ? PT_B2 : (id < S.cs ? PT_FLUID : PT_MEMB));
+}
+
+// System of the given global id (binary search over the id ranges).
+__device__ __forceinline__ int find_sys(const SysInfo* sys, int nsys, unsigned id) {
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (sys[mid].id0 <= id) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Box constants of the per-step kernels.
+struct Box {
+    float L[3], invL[3];
+    int pmask;
+};
+
+__device__ __forceinline__ Box box_of(const SysInfo& S) {
+    Box b;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        b.L[a] = S.g.L[a];
+        b.invL[a] = S.invL[a];
+    }
+    b.pmask = S.g.pmask;
+    return b;
+}
+
+// Minimum image of a list pair.  A listed pair is either far closer than
+// L/2 or close to L apart along a periodic axis, so d - L rint(d/L) makes
+// the same shift as the conditional form of the boundary kernels and
+// rounds the same way (one subtraction of L), i.e. the same FP32 value.
+__device__ __forceinline__ float3 pair_image(float3 a, float3 b, const Box& B) {
+    float3 d = f3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+    if (B.pmask & 1) d.x = fmaf(-B.L[0], rintf(d.x * B.invL[0]), d.x);
+    if (B.pmask & 2) d.y = fmaf(-B.L[1], rintf(d.y * B.invL[1]), d.y);
+    if (B.pmask & 4) d.z = fmaf(-B.L[2], rintf(d.z * B.invL[2]), d.z);
+    return d;
+}
+
+// The per-step kernels exist in two forms.  ENS = false: one system, given
+// by value in the kernel parameters (constant bank, no per-thread loads).
+// ENS = true: the system of each slot comes from the per-slot index and the
+// device table (ensembles, and captured steps, whose noise keys are derived
+// on the device).
+#define GC_SYS_OF(S, i) const SysInfo& S = ENS ? sys[sysid ? sysid[i] : 0] : s0
 
 // Positions are double-float: pos holds the FP32 position (what the pair,
 // membrane and list kernels read) and plo the FP32 remainder x - pos, so that
@@ -141,6 +202,21 @@ struct GcFused {
     int* ccnt = nullptr;         // number of acting entries
     int mw = 0;                  // mask words per slot
     int* rebuild = nullptr;
+    // pair tiles (GcFusedOptions.tiles): lists per pair of neighbouring
+    // cubes built at each rebuild, partial sums per pair direction, finish
+    // passes; otherwise per-particle Verlet lists for every slot
+    bool lists = true;
+    int tK = 0;                     // cubes the per-cube tile arrays hold
+    int* cube_sys = nullptr;        // system of each cube
+    unsigned short* bmask = nullptr;   // per cube: pair directions whose backward neighbour exists
+    int* tnb = nullptr;             // K x 14: neighbour cube of each pair (bit 30: minimum image), -1: none
+    unsigned* toff = nullptr;       // K x 14 + 1: chunks of 32 entries per pair, then their exclusive scan
+    unsigned* tscan = nullptr;      // block sums of that scan
+    unsigned* tent = nullptr;       // pair entries (a | b << 8, kTilePad between lists)
+    size_t tent_chunks = 0;         // capacity in chunks of 32 entries
+    float* pd = nullptr;            // 14 x n density partial sums
+    float* pf = nullptr;            // 14 x 3 x n force partial sums (x, y, z planes)
+    unsigned long long* tpairs = nullptr;   // candidate pairs of the latest build
     unsigned* flags = nullptr;
     unsigned* oflag = nullptr;   // list overflow inside captured steps
     int* need = nullptr;         // the longest list an overflowing build wanted
@@ -155,6 +231,8 @@ struct GcFused {
         unsigned oflag;
         int need;
         unsigned long long drebuilds;
+        unsigned tchunks;            // chunks the latest tile build needs
+        unsigned long long tpairs;
     }* h = nullptr;
     unsigned long long drebuilds_seen = 0;
     // counting-sort temporaries (owned, so a captured step can use them)
@@ -229,6 +307,17 @@ int falloc(GcFused* f, T** p, size_t count) {
     return GC_OK;
 }
 
+// pair tiles (fused_tiles.cu)
+int tiles_grid(GcFused* f);
+int tiles_build(GcFused* f, cudaStream_t st, const float4* bpos, bool host);
+int tiles_alloc_entries(GcFused* f, size_t chunks);
+int launch_tile_density(GcFused* f, cudaStream_t st, const GcParams& p, bool mark);
+int launch_tile_force(GcFused* f, cudaStream_t st, const GcParams& p, int drive, bool mark);
+int wall_lists(GcFused* f, cudaStream_t st, const float4* bpos, bool host);
+bool any_bound2(const GcFused* f);
+void prof_mark(GcFused* f, cudaStream_t st);
+struct SysInfo;
+
 int stage_bytes(GcFused* f, size_t bytes);
 void drop_graphs(GcFused* f);
 int alloc_list(GcFused* f, int cap);
@@ -258,7 +347,7 @@ __global__ void __launch_bounds__(kMaxBS, GC_BUILD_MIN_BLOCKS) fk_build_list(int
                                                      const int* __restrict__ sysid, const float4* __restrict__ pos,
                                                      const unsigned* __restrict__ start, int* __restrict__ nbr,
                                                      int* __restrict__ cnt, int cap, float cut2, unsigned* flags,
-                                                     int* __restrict__ need);
+                                                     int* __restrict__ need, int walls_only);
 
 __global__ void fk_gather_mpos(int ncp, const SysInfo* __restrict__ sys, const int* __restrict__ msys,
                                const int* __restrict__ slot_of, const float4* __restrict__ pos,

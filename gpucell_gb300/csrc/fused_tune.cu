@@ -23,17 +23,18 @@ using namespace gcf;
 // (beyond the summation order the chosen settings imply).  The search is
 // coordinate-wise: skin (the cube size rc + skin of the list grid and the
 // list length), then threads per block, then per-step compaction of the
-// acting entries, then captured steps.  Choices are cached per size class
-// (ensemble or single system, particle count, density, membranes present,
-// noise) for the life of the process.
+// acting entries (list passes only), then captured steps.  Choices are
+// cached per size class (ensemble or single system, particle count,
+// density, membranes present, noise, pair tiles or lists) for the life of
+// the process.
 // ---------------------------------------------------------------------------
 namespace {
 
 struct TuneKey {
-    int nsys_class, n_class, dens_class, cells, noise;
+    int nsys_class, n_class, dens_class, cells, noise, lists;
     bool operator<(const TuneKey& o) const {
-        return std::tie(nsys_class, n_class, dens_class, cells, noise) <
-               std::tie(o.nsys_class, o.n_class, o.dens_class, o.cells, o.noise);
+        return std::tie(nsys_class, n_class, dens_class, cells, noise, lists) <
+               std::tie(o.nsys_class, o.n_class, o.dens_class, o.cells, o.noise, o.lists);
     }
 };
 
@@ -50,6 +51,7 @@ TuneKey tune_key(GcFused* f) {
     k.dens_class = (int)lround(8.0 * log2(dens * f->p.rc * f->p.rc * f->p.rc + 1e-30));
     k.cells = f->ncell > 0;
     k.noise = f->p.noise_pref > 0.f;
+    k.lists = f->lists;
     return k;
 }
 
@@ -119,7 +121,7 @@ extern "C" int gc_fused_autotune(GcFused* f, int trial_steps, int drive_on, int 
         double ms = trial(f, o, trial_steps, drive, e0, e1);
         if (ms < best_ms) { best_ms = ms; best = o; }
     }
-    for (int c = 0; c < 2; ++c) {
+    for (int c = 0; c < 2 && f->lists; ++c) {   // compaction is a setting of the list passes
         GcFusedOptions o = best;
         o.compact = c;
         if (o.compact == best.compact) continue;

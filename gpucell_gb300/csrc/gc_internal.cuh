@@ -354,6 +354,10 @@ void gc_sort_bufs_carve(void* base, int n, int K, GcSortBufs* b);
 // scratch, so it can be captured into a CUDA graph).
 int gc_counting_sort_bufs(int n, int K, int* keys, int* vals, const GcSortBufs& b, unsigned* flags,
                           cudaStream_t st);
+// Device-wide exclusive scan of buf[0..n) in place, buf[n] = total; bsum
+// holds gc_scan_blocks(n) block sums (n up to 4096^2).
+size_t gc_scan_blocks(int n);
+int gc_scan_exclusive(unsigned* buf, int n, unsigned* bsum, cudaStream_t st);
 // Start of every key's range (K + 1 entries) after the latest counting sort.
 const unsigned* gc_sort_starts();
 // (Re)builds the grid from the caller's device bbox pointer.

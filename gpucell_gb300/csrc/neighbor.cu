@@ -319,6 +319,13 @@ int gc_counting_sort_bufs(int n, int K, int* keys, int* vals, const GcSortBufs& 
     return sort_with(n, K, keys, vals, b, flags, st);
 }
 
+size_t gc_scan_blocks(int n) { return (size_t)(n / kScanTile + 2); }
+
+int gc_scan_exclusive(unsigned* buf, int n, unsigned* bsum, cudaStream_t st) {
+    if (n <= 0) return GC_OK;
+    return scan_exclusive_with(buf, n, bsum, st);
+}
+
 extern "C" {
 
 // K4 -- src/ConfigDomain.cuh:11, src/Particle.cu:668.  The cube geometry is

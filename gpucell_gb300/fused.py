@@ -26,9 +26,9 @@ def _ptr(a):
     return C.c_void_p(a.data_ptr())
 
 
-def _options(skin, block, list_capacity, compact, graph):
+def _options(skin, block, list_capacity, compact, graph, tiles=False):
     return _lib.GcFusedOptions(skin=skin, block=block, list_capacity=list_capacity, compact=1 if compact else 0,
-                               graph=1 if graph else 0)
+                               graph=1 if graph else 0, tiles=1 if tiles else 0)
 
 
 def _cell_arrays(cfg: Config):
@@ -87,12 +87,12 @@ class _Handle:
         o = _lib.GcFusedOptions()
         _lib.call("gc_fused_get_options", self.h, C.byref(o))
         return dict(skin=round(float(o.skin), 6), block=o.block, list_capacity=o.list_capacity,
-                    compact=bool(o.compact), graph=bool(o.graph))
+                    compact=bool(o.compact), graph=bool(o.graph), tiles=bool(o.tiles))
 
-    def set_options(self, skin=0.0, block=0, list_capacity=0, compact=None, graph=None):
+    def set_options(self, skin=0.0, block=0, list_capacity=0, compact=None, graph=None, tiles=None):
         cur = self.options()
         o = _options(skin, block, list_capacity, cur["compact"] if compact is None else compact,
-                     cur["graph"] if graph is None else graph)
+                     cur["graph"] if graph is None else graph, cur["tiles"] if tiles is None else tiles)
         _lib.call("gc_fused_set_options", self.h, C.byref(o))
 
     def autotune(self, trial_steps=30, drive_on=1, use_cache=False) -> dict:
@@ -101,7 +101,7 @@ class _Handle:
         _lib.call("gc_fused_autotune", self.h, int(trial_steps), int(drive_on),
                   _lib.GC_TUNE_CACHE if use_cache else 0, C.byref(o), C.byref(ms))
         return dict(skin=round(float(o.skin), 6), block=o.block, compact=bool(o.compact), graph=bool(o.graph),
-                    ms_per_step=ms.value)
+                    tiles=bool(o.tiles), ms_per_step=ms.value)
 
     def write_output(self, directory, step_data, time, first=False, sys=0, threads=0):
         """GPUCell's output files for one output step (see gpucell_gb300.output)."""
@@ -156,12 +156,13 @@ class _Handle:
 
 
 class FusedSystem(_Handle):
-    def __init__(self, cfg: Config, noise=True, skin=0.1, block=128, list_capacity=0, compact=True, graph=False):
+    def __init__(self, cfg: Config, noise=True, skin=0.1, block=128, list_capacity=0, compact=True, graph=False,
+                 tiles=False):
         self.cfg = cfg
         self.lib = _lib.load()
         self.h = C.c_void_p()
         consts = _lib.Structconst(**cfg.consts())
-        opt = _options(skin, block, list_capacity, compact, graph)
+        opt = _options(skin, block, list_capacity, compact, graph, tiles)
         bbox = np.ascontiguousarray(cfg.bbox, np.float32)
         _lib.call("gc_fused_create", C.byref(consts), _ptr(bbox), cfg.pmask, 1 if noise else 0, C.byref(opt),
                   C.byref(self.h))
@@ -205,7 +206,7 @@ class Ensemble(_Handle):
     """
 
     def __init__(self, cfgs: Sequence[Config], noise=True, skin=0.1, block=128, list_capacity=0, compact=True,
-                 graph=False):
+                 graph=False, tiles=False):
         self.cfgs = list(cfgs)
         self.lib = _lib.load()
         self.h = C.c_void_p()
@@ -214,7 +215,7 @@ class Ensemble(_Handle):
             d.consts = _lib.Structconst(**cfg.consts())
             d.bbox[:] = [float(x) for x in cfg.bbox]
             d.periodic_mask = cfg.pmask
-        opt = _options(skin, block, list_capacity, compact, graph)
+        opt = _options(skin, block, list_capacity, compact, graph, tiles)
         _lib.call("gc_ensemble_create", len(self.cfgs), descs, 1 if noise else 0, C.byref(opt), C.byref(self.h))
         self._keep = []
         for s, cfg in enumerate(self.cfgs):

@@ -43,6 +43,8 @@ extern "C" {
 #define GC_FLAG_BAD_INDEX     2u   /* a topology index pointed outside its array */
 #define GC_FLAG_CELL_OVERFLOW 4u   /* a grid cell held more particles than a sweep stages */
 #define GC_FLAG_STRETCH       8u   /* a membrane edge reached its maximum length */
+#define GC_FLAG_TILE_FULL    16u   /* a cube held more particles than the pair tiles take (the handle
+                                      turns to per-particle lists) */
 
 /* ---- library controls (no counterpart in the reference) ---------------- */
 
@@ -193,7 +195,13 @@ typedef struct {
                              pass iterates only those */
     int graph;            /* 1: each step runs as one captured CUDA graph; the list rebuild is a conditional
                              node decided on the device, and gc_fused_step synchronises once per call */
-    int reserved[3];
+    int tiles;            /* 0 (default): per-particle Verlet lists, every pair evaluated from both ends;
+                             1: pair tiles -- particles sorted by cubes at least rc + skin wide, one list
+                             per pair of neighbouring cubes (each particle pair once), the density and force
+                             passes evaluate every pair once and give each side its share.  A handle with
+                             tiles turns to lists by itself when a cube holds more than 96 particles or a
+                             periodic axis has fewer than three cubes */
+    int reserved[2];
 } GcFusedOptions;
 /* bbox6 (host) as src/main.cuh:12; periodic_mask as gc_set_periodic. */
 int gc_fused_create(const Structconst* consts, const float* bbox6, int periodic_mask, int noise_on,

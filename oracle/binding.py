@@ -168,14 +168,19 @@ class Oracle:
             raise RuntimeError(f"or_force_scale failed ({rc})")
         return out
 
-    def forces_from_density(self, rho):
+    def forces_from_density(self, rho, press=None):
         """Re-evaluates every force of the current state in FP64 from the given
-        densities (for instance a GPU's FP32 ones): EOS, SDPD, wall repulsion,
-        body force, membrane geometry and forces, aggregation.  Compared with
-        the GPU's forces this isolates the force pass from the rounding of the
-        density sum, which P = c^2 (rho - rho0) amplifies."""
+        densities and pressures (for instance a GPU's FP32 ones; without
+        pressures, the EOS makes them): SDPD, wall repulsion, body force,
+        membrane geometry and forces, aggregation.  Compared with the GPU's
+        forces this isolates the force pass from the rounding of the density
+        sum, which P = c^2 (rho - rho0) amplifies."""
         self.set(rho=rho)
-        for name in ("eos", "sdpd_force", "rep_force", "ext_force"):
+        if press is None:
+            self.call("eos")
+        else:
+            self.set(press=press)
+        for name in ("sdpd_force", "rep_force", "ext_force"):
             self.call(name)
         if self.cfg.ncell:
             self.call("geo", 0)

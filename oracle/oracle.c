@@ -816,7 +816,7 @@ int or_force_scale(const or_state* s, int parts, double* scale) {
     bins_t b;
     if (bins_build(&b, s, s->c.CutRadius, NULL)) return -1;
     float rc2 = rc2_f(s);
-    double m = s->c.Mass, eta = s->c.ShearVis, zeta = s->c.BulkVis;
+    double m = s->c.Mass, eta = s->c.ShearVis, zeta = s->c.BulkVis, rc = s->c.CutRadius;
     double A = 5.0 * eta / 3.0 - zeta, B = 5.0 * (zeta + eta / 3.0);
     double sA = sqrt(A > 0 ? A : 0), sAB = sqrt(A + B > 0 ? A + B : 0);
     int noise = s->noise_on && s->c.Temp > 0.f;
@@ -824,6 +824,32 @@ int or_force_scale(const or_state* s, int parts, double* scale) {
     float r0f = (float)(s->c.CutRadius / 3.0);
     float r0sq = r0f * r0f;
     double r0 = s->c.CutRadius / 3.0, D = (double)s->c.SoundSpeed1 * s->c.SoundSpeed1;
+    const double fnorm = 210.0 / (OR_PI * rc * rc * rc * rc * rc), wnorm = 21.0 / (2.0 * OR_PI * rc * rc * rc);
+    const int eos = (parts & OR_SCALE_EOS) != 0;
+    /* with the EOS bit: per particle, the rounding scale of its number
+     * density, W(0) + sum_j (W_ij + |W'_ij| r_ij) -- each kernel value and its
+     * sensitivity to the rounding of r */
+    double* dscale = NULL;
+    if (eos && (parts & OR_SCALE_SDPD)) {
+        dscale = (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+        if (!dscale) {
+            bins_free(&b);
+            return -1;
+        }
+        set_threads(s);
+#pragma omp parallel for schedule(dynamic, 256)
+        for (long i = 0; i < n; ++i) {
+            if (!is_mobile(s, (unsigned)i)) continue;
+            double acc = wend_w(s, 0.0);
+            FOR_CANDIDATES(&b, s, i, j, {
+                if (j == i || !is_sdpd(s, (unsigned)j)) continue;
+                if (r2_f32(s, i, j) >= rc2) continue;
+                double r = nrm(disp(s, i, j)), q = r / rc, t = 1.0 - q;
+                acc += wend_w(s, r) + wnorm * 20.0 * q * q * t * t * t;
+            });
+            dscale[i] = acc;
+        }
+    }
     set_threads(s);
 #pragma omp parallel for schedule(dynamic, 256)
     for (long i = 0; i < n; ++i) {
@@ -831,10 +857,10 @@ int or_force_scale(const or_state* s, int parts, double* scale) {
         double di = s->rho[i] / m;
         /* the size of P_i / d_i^2 for rounding: P = c^2 (rho - rho0) is the
          * difference of two terms of size c^2 rho, and rho is a sum of FP32
-         * kernel values, so its rounding error reaches P as c^2 rho u */
-        const int eos = (parts & OR_SCALE_EOS) != 0;
+         * kernel values, so its rounding error reaches P as c^2 m (its
+         * rounding scale) u */
         double ci = is_memb(s, (unsigned)i) ? s->c.SoundSpeed2 : s->c.SoundSpeed1;
-        double pi = (fabs(s->press[i]) + (eos ? ci * ci * s->rho[i] : 0.0)) / (di * di);
+        double pi = (fabs(s->press[i]) + (dscale ? ci * ci * m * dscale[i] : 0.0)) / (di * di);
         v3 vi = ld3(s->vel, i);
         double acc = (parts & OR_SCALE_BODY) && s->drive_on ? fabs((double)s->c.ConstExtForce) : 0.0;
         if (!(parts & (OR_SCALE_SDPD | OR_SCALE_REP))) {
@@ -848,30 +874,39 @@ int or_force_scale(const or_state* s, int parts, double* scale) {
                 if (!(parts & OR_SCALE_REP) || r2f >= r0sq || r2f <= 0.f) continue;
                 v3 d = disp(s, i, j);
                 double r2 = dot(d, d), q2 = r0 * r0 / r2, q4 = q2 * q2, q12 = q4 * q4 * q4;
-                acc += fabs(D * (q12 - q4) / r2) * sqrt(r2);
+                /* the term and its sensitivity to r: |d/dr (r f(r))| r <= (12 q^12 + 4 q^4) D / r */
+                acc += D * (fabs(q12 - q4) + 12.0 * q12 + 4.0 * q4) / sqrt(r2);
                 continue;
             }
             if (!(parts & OR_SCALE_SDPD) || !is_sdpd(s, (unsigned)j) || r2f >= rc2) continue;
             v3 d = disp(s, i, j);
-            double r = nrm(d), F = wend_f(s, r);
+            double r = nrm(d), q = r / rc, t = 1.0 - q;
             double dj = s->rho[j] / m;
             /* Bound2 density is DenInit exactly: its pressure has no rounding */
             double cj = is_memb(s, (unsigned)j) ? s->c.SoundSpeed2 : s->c.SoundSpeed1;
-            double pj = (fabs(s->press[j]) + (eos && is_mobile(s, (unsigned)j) ? cj * cj * s->rho[j] : 0.0)) / (dj * dj);
-            acc += fabs((pi + pj) * F) * r;
+            double pj = (fabs(s->press[j]) + (dscale && is_mobile(s, (unsigned)j) ? cj * cj * m * dscale[j] : 0.0)) /
+                        (dj * dj);
+            /* F = fnorm (1 - q)^3 with its sensitivity to the rounding of r:
+             * |F| + |F'| r = fnorm (1 - q)^2 (1 + 2 q) */
+            double Fc = fnorm * t * t * (1.0 + 2.0 * q);
+            acc += (pi + pj) * Fc * r;
             if (r <= 0.0) continue;
-            v3 e = scl(1.0 / r, d), vij = sub(vi, ld3(s->vel, j));
-            double ev = dot(e, vij), fdd = F / (di * dj);
-            acc += fabs(fdd) * (fabs(A) * nrm(vij) + fabs(B * ev));
-            if (noise && fdd > 0.0) {
+            v3 vij = sub(vi, ld3(s->vel, j));
+            double fddc = Fc / (di * dj);
+            acc += fddc * (fabs(A) * nrm(vij) + fabs(B) * nrm(vij));
+            if (noise && t > 0.0) {
                 double xi[3];
                 or_pair_noise(s, (unsigned)i, (unsigned)j, xi);
                 v3 x = mk(xi[0], xi[1], xi[2]);
-                acc += sqrt(pref * fdd) * (sA * nrm(x) + fabs((sAB - sA) * dot(e, x)));
+                /* the amplitude sqrt(pref F / (d_i d_j)) ~ (1 - q)^(3/2) with its sensitivity
+                 * to the rounding of r: sqrt(pref fnorm (1 - q) / (d_i d_j)) (1 + q/2) */
+                double qc = sqrt(pref * fnorm * t / (di * dj)) * (1.0 + 0.5 * q);
+                acc += qc * (sA * nrm(x) + fabs(sAB - sA) * nrm(x));
             }
         });
         scale[i] = acc;
     }
+    free(dscale);
     bins_free(&b);
     long nc = s->c.nCellStart, ncp = s->c.nCellPar;
     if (s->ncell <= 0) return 0;

@@ -29,11 +29,16 @@ def _close_rel(got, want, tol):
     assert err <= tol * scale, f"max err {err:g} vs scale {scale:g}"
 
 
-@pytest.mark.parametrize("compact", [True, False])
-def test_fused_tracks_oracle_noise_off(cuda_device, compact):
+# the per-particle lists (default) with and without the per-step compaction
+# of the acting entries, and the pair tiles
+MODES = {"lists_compact": dict(compact=True), "lists": dict(compact=False), "tiles": dict(tiles=True)}
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+def test_fused_tracks_oracle_noise_off(cuda_device, mode):
     from gpucell_gb300.fused import FusedSystem
     cfg = gen.small_channel()
-    fs = FusedSystem(cfg, noise=False, compact=compact)
+    fs = FusedSystem(cfg, noise=False, **MODES[mode])
     o = _oracle(cfg, False)
     for _ in range(3):
         fs.step(1, 1)
@@ -47,13 +52,13 @@ def test_fused_tracks_oracle_noise_off(cuda_device, compact):
     assert fs.flags() == 0
 
 
-@pytest.mark.parametrize("compact", [True, False])
-def test_fused_matches_boundary_path_with_noise(cuda_device, compact):
+@pytest.mark.parametrize("mode", list(MODES))
+def test_fused_matches_boundary_path_with_noise(cuda_device, mode):
     from gpucell_gb300.fused import FusedSystem
     from gpucell_gb300.host import ParticleSystem
     cfg = gen.small_channel()
     ps = ParticleSystem(cfg, noise=True)
-    fs = FusedSystem(cfg, noise=True, compact=compact)
+    fs = FusedSystem(cfg, noise=True, **MODES[mode])
     for _ in range(2):
         ps.update()
         fs.step(1, 1)
@@ -159,7 +164,7 @@ def test_fused_force_evaluation_matches_oracle(cuda_device):
     |dF_i| <= 1e-5 |F_i| + 16 u S_i (u FP32's unit roundoff, S_i the sum of
     the magnitudes of the terms F_i adds up, the pressure counted at c^2 rho
     since it amplifies the density's rounding); against the oracle's forces
-    from the GPU's own densities, the same bound with the pressure counted at
+    from the GPU's own densities and pressures, the same bound with the pressure counted at
     |P|; and the membrane deformation force
     of the undeformed cells, exactly zero, below 1e-3 (measured 1.1e-4; the
     edge and triangle vectors are differences of double-float positions, so
@@ -181,9 +186,9 @@ def test_fused_force_evaluation_matches_oracle(cuda_device):
     mov = slice(cfg.n_b1 + cfg.n_b2, cfg.n)
     from oracle.binding import force_error_stats
     s = force_error_stats(g["force"][mov], o.force[mov], o.force_scale()[mov], rtol=1e-5)
-    # the same forces re-evaluated by the oracle from the GPU's FP32 densities:
+    # the same forces re-evaluated by the oracle from the GPU's FP32 densities and pressures:
     # the pressure's amplification of the density rounding drops out
-    o.forces_from_density(g["rho"])
+    o.forces_from_density(g["rho"], g["press"])
     t = force_error_stats(g["force"][mov], o.force[mov], o.force_scale(31)[mov], rtol=1e-5)
     for name, x in (("own density", s), ("GPU density", t)):
         print(f"\nforce ({name}): median rel {x['median_rel']:.2e}, p99 {x['p99_rel']:.2e}, max {x['max_rel']:.2e}, "

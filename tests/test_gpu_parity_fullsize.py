@@ -12,7 +12,7 @@ step checked is Particle::UpdatePar, src/Particle.cu:1310-1329).
     P = c^2 (rho - rho0) turns the FP32 rounding of the density sum into an
     error of size c^2 rho u, so against the oracle's own densities its term
     counts at that size; against the oracle's forces from the GPU's
-    densities, at |P|.  The median, 99th percentile and largest relative
+    densities and pressures, at |P|.  The median, 99th percentile and largest relative
     error |dF_i| / |F_i| and the fraction of particles within 1e-5 are
     printed for both.
   - five steps with the thermal noise on (both sides draw the same Philox
@@ -73,7 +73,7 @@ def test_force_evaluation_at_full_size(cuda_device, cfg2):
     res = {}
     for label, sc in (("own density", scale), ("GPU density", None)):
         if sc is None:
-            o.forces_from_density(g["rho"])
+            o.forces_from_density(g["rho"], g["press"])
             sc = o.force_scale(31)
         f, w, sm = g["force"][mov], o.force[mov], sc[mov]
         res[label] = [(name, force_error_stats(f[sl], w[sl], sm[sl], rtol=1e-5))
