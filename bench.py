@@ -61,6 +61,9 @@ def parse():
                     help="the reference arm times min(--steps, this) oracle steps")
     ap.add_argument("--ens-seq-steps", type=int, default=10,
                     help="steps per system of the sequential baselines of the ensemble")
+    ap.add_argument("--no-variants", dest="variants", action="store_false",
+                    help="skip timing the precision variants (plain FP32 positions, FP16 neighbour velocities) "
+                         "and the pair tiles on the same workload")
     ap.add_argument("--no-configs", dest="configs", action="store_false",
                     help="skip the short cfg3 (sheared suspension) and cfg4 (constriction) legs")
     ap.add_argument("--config-steps", type=int, default=200, help="steps of the cfg3 and cfg4 legs")
@@ -503,6 +506,7 @@ def run_ours(args):
                                                           tiles=opts["tiles"])
 
     fs.close()
+    variants = time_variants(cfg, args, min(K, 30)) if args.variants and world == 1 else None
     ens = run_ensemble(args, dev, rank, world, barrier, max_over_ranks) if args.ensemble else None
     if rank != 0:
         if world > 1:
@@ -561,6 +565,10 @@ def run_ours(args):
         if plain:
             engine["speedup_over_plain"] = plain["ms_per_step"] / engine["ms_per_step"]
         line["engine_fused"] = engine
+    if variants:
+        for v in variants.values():
+            v["slowdown_vs_default"] = v["ms_per_step"] / (t_ms / K)
+        line["variants"] = variants
     if ens:
         line["ensemble"] = ens
     if configs:
@@ -829,9 +837,66 @@ def cpu_leg(cfg, cpu_steps, parity, args):
     if parity:
         par["trajectory"] = traj
         par["channel"] = parity_check(100)
+        par["precision_variants"] = precision_parity()
         par["workload"] = f"{cfg.n}-particle RBC suspension ({cfg.ncell} cells of {int(cfg.npar[0])} vertices)"
         par["reference"] = "FP64 CPU oracle (oracle/oracle.c)"
     return (cpu if cpu_steps > 0 else None), (par or None)
+
+
+def precision_parity(steps=300):
+    """The precision variants against the FP64 oracle: the largest position
+    error of a walled channel with a cell after `steps` steps (noise off)
+    with double-float and with plain FP32 positions; and the per-particle
+    force error of one force evaluation on a stepped periodic suspension with
+    FP32 and with FP16-packed neighbour velocities."""
+    import dataclasses
+
+    import numpy as np
+    from gpucell_gb300 import generator
+    from gpucell_gb300.fused import FusedSystem
+    from oracle.binding import Oracle, force_error_stats
+    cfg = generator.small_channel()
+    o = Oracle(cfg, noise=False, nthreads=os.cpu_count() or 1)
+    o.setup()
+    for _ in range(steps):
+        o.step()
+    drift = {}
+    for name, fp32 in (("double_float", False), ("fp32", True)):
+        fs = FusedSystem(cfg, noise=False, fp32_positions=fp32)
+        fs.step(steps, 1)
+        d = fs.fetch()["pos"].astype(np.float64) - o.pos
+        fs.close()
+        for a in range(3):
+            if (cfg.pmask >> a) & 1:
+                L = float(cfg.bbox[2 * a + 1] - cfg.bbox[2 * a])
+                d[:, a] -= L * np.rint(d[:, a] / L)
+        drift[name] = float(np.abs(d).max())
+    sus = generator.suspension(nx=32, ny=24, nz=24, ncells=2, subdiv=2, hematocrit=0.12, seed=6)
+    warm = FusedSystem(sus, noise=True)
+    warm.step(20, 1)
+    s = warm.fetch()
+    warm.close()
+    c0 = dataclasses.replace(sus, phys=dataclasses.replace(sus.phys, dt=1e-20))
+    o = Oracle(c0, noise=False, nthreads=os.cpu_count() or 1)
+    o.setup()
+    o.set(pos=s["pos"], vel=s["vel"], velhalf=s["velhalf"], force=s["force"], nthro=s["nthro"])
+    o.step()
+    mov = slice(sus.n_b1 + sus.n_b2, sus.n)
+    scale = o.force_scale()[mov]
+    ferr = {}
+    for name, half in (("fp32", False), ("fp16", True)):
+        fs = FusedSystem(c0, noise=False, half_velocity=half)
+        fs.load(s["pos"], s["vel"], s["velhalf"], s["force"], s["nthro"])
+        fs.step(1, 1)
+        g = fs.fetch()
+        fs.close()
+        st = force_error_stats(g["force"][mov], o.force[mov], scale)
+        ferr[name] = {k: st[k] for k in ("median_rel", "p99_rel", "max_rel", "frac_within_rtol", "worst_ratio")}
+    return {"position_error_after_steps": drift, "steps": steps,
+            "position_workload": f"walled channel, {cfg.n} particles, one {cfg.ncp}-vertex cell, noise off",
+            "neighbour_velocity_force_error": ferr,
+            "force_workload": f"periodic suspension, {sus.n} particles, {sus.ncell} cells, velocities of 20 noisy "
+                              "steps, one force evaluation"}
 
 
 def force_parity(cfg):
@@ -975,6 +1040,40 @@ def trajectory_parity(cfg, o, k):
     if cfg.ncell:
         out["max_area_error"] = float(np.abs(g["Area64"] / o.area - 1).max())
         out["max_volume_error"] = float(np.abs(g["Vol64"] / o.vol - 1).max())
+    return out
+
+
+def time_variants(cfg, args, steps):
+    """The same workload, timed like the headline step (CUDA events on the
+    library's stream, after 5 warm-up steps), with one setting changed:
+    plain FP32 positions instead of double-float ones (the precision A/B of
+    the step: same passes, same lists), FP16-packed neighbour velocities in
+    the force gathers (an experiment), and the pair tiles (each pair
+    evaluated once, instead of per-particle lists)."""
+    import torch
+    from gpucell_gb300.fused import FusedSystem
+    out = {}
+    for name, kw in (("fp32_positions", dict(fp32_positions=True)), ("half_velocity", dict(half_velocity=True)),
+                     ("pair_tiles", dict(tiles=True))):
+        fs = FusedSystem(cfg, noise=args.noise, skin=args.skin, block=args.block, compact=args.compact, **kw)
+        fs.step(5, 1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fs.step(steps, 1)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        fs.profile(True)
+        fs.step(2, 1)
+        prof = fs.profile_read()
+        fs.profile(False)
+        o = fs.options()
+        out[name] = {"ms_per_step": ms, "value": cfg.n / (ms / 1e3), "steps": steps, "device_flags": fs.flags(),
+                     "force_ms": prof["force_ms"] / max(prof["steps"], 1),
+                     "density_ms": prof["density_ms"] / max(prof["steps"], 1),
+                     "tiles": o["tiles"], "fp32_positions": o["fp32_positions"], "half_velocity": o["half_velocity"]}
+        fs.close()
     return out
 
 

@@ -55,7 +55,8 @@ class GcFusedOptions(C.Structure):
     """ctypes mirror of GcFusedOptions (include/gpucell_gb300.h)."""
 
     _fields_ = [("skin", C.c_float), ("block", C.c_int), ("list_capacity", C.c_int), ("compact", C.c_int),
-                ("graph", C.c_int), ("tiles", C.c_int), ("reserved", C.c_int * 2)]
+                ("graph", C.c_int), ("tiles", C.c_int), ("fp32_positions", C.c_int),
+                ("half_velocity", C.c_int)]
 
 
 assert C.sizeof(GcFusedOptions) == 32

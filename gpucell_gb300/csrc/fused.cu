@@ -36,6 +36,7 @@
 //     synchronises once per gc_fused_step call instead of once per step.
 #include "fused_internal.cuh"
 
+#include <cuda_fp16.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -108,7 +109,7 @@ __global__ void fk_integrate(int n, GcParams p, SysInfo s0, const SysInfo* __res
                              float4* __restrict__ vh, float4* __restrict__ vpred, const float4* __restrict__ force,
                              float4* __restrict__ plo, const float4* __restrict__ refpos, int4* __restrict__ nthro,
                              float half_skin2, int* __restrict__ rebuild, float4* __restrict__ mpos,
-                             float4* __restrict__ mplo, int4* __restrict__ mnthro, unsigned* flags) {
+                             float4* __restrict__ mplo, int4* __restrict__ mnthro, unsigned* flags, int ddpos) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool far = false;
     if (i < n) {
@@ -120,9 +121,9 @@ __global__ void fk_integrate(int n, GcParams p, SysInfo s0, const SysInfo* __res
             float h = 0.5f * p.dt * p.dt * p.inv_mass;
             // the displacement in FP32, added to the double-float position
             float4 lo = plo[i];
-            dd_add(x.x, lo.x, p.dt * v.x + h * f.x);
-            dd_add(x.y, lo.y, p.dt * v.y + h * f.y);
-            dd_add(x.z, lo.z, p.dt * v.z + h * f.z);
+            pos_add(x.x, lo.x, p.dt * v.x + h * f.x, ddpos);
+            pos_add(x.y, lo.y, p.dt * v.y + h * f.y, ddpos);
+            pos_add(x.z, lo.z, p.dt * v.z + h * f.z, ddpos);
             if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) raise_flag(flags, GC_FLAG_NONFINITE);
             int4 t = nthro[i];
             bool crossed = false;
@@ -133,8 +134,8 @@ __global__ void fk_integrate(int n, GcParams p, SysInfo s0, const SysInfo* __res
             for (int a = 0; a < 3; ++a) {
                 if (!(S.g.pmask & (1 << a))) continue;
                 float c = *xs[a];
-                if (c >= S.g.hi[a]) { dd_add(*xs[a], *ls[a], -S.g.L[a]); *ts[a] += 1; crossed = true; }
-                else if (c < S.g.lo[a]) { dd_add(*xs[a], *ls[a], S.g.L[a]); *ts[a] -= 1; crossed = true; }
+                if (c >= S.g.hi[a]) { pos_add(*xs[a], *ls[a], -S.g.L[a], ddpos); *ts[a] += 1; crossed = true; }
+                else if (c < S.g.lo[a]) { pos_add(*xs[a], *ls[a], S.g.L[a], ddpos); *ts[a] -= 1; crossed = true; }
             }
             if (crossed) nthro[i] = t;
             pos[i] = x;
@@ -174,7 +175,7 @@ __global__ void fk_cellkey(int n, const SysInfo* __restrict__ sys, const int* __
 // its box on periodic axes (counting the crossings), so that the list build
 // can use one image shift per row of cubes.
 __global__ void fk_permute(int n, const SysInfo* __restrict__ sys, const int* __restrict__ perm, SlotArrays src,
-                           SlotArrays dst, float4* __restrict__ refpos, int* __restrict__ slot_of) {
+                           SlotArrays dst, float4* __restrict__ refpos, int* __restrict__ slot_of, int ddpos) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     int o = perm[q];
@@ -192,9 +193,9 @@ __global__ void fk_permute(int n, const SysInfo* __restrict__ sys, const int* __
         if (!isfinite(c)) continue;
         int w = (int)floorf((c - g.lo[a]) / g.L[a]);
         if (w != 0) {
-            dd_add(*xs[a], *ls[a], -(float)w * g.L[a]);
-            if (*xs[a] >= g.hi[a]) { dd_add(*xs[a], *ls[a], -g.L[a]); ++w; }
-            else if (*xs[a] < g.lo[a]) { dd_add(*xs[a], *ls[a], g.L[a]); --w; }
+            pos_add(*xs[a], *ls[a], -(float)w * g.L[a], ddpos);
+            if (*xs[a] >= g.hi[a]) { pos_add(*xs[a], *ls[a], -g.L[a], ddpos); ++w; }
+            else if (*xs[a] < g.lo[a]) { pos_add(*xs[a], *ls[a], g.L[a], ddpos); --w; }
             *ts[a] += w;
         }
     }
@@ -486,13 +487,30 @@ constexpr int kForceAhead = GC_FORCE_AHEAD;   // groups of list indices loaded a
 #endif
 constexpr int force_min_blocks(bool ens) { return GC_FORCE_MIN_BLOCKS - (ens ? 1 : 0); }
 
-template <bool COMPACT, bool ENS>
+// The predicted velocity of a neighbour packed to FP16 (x, y | z, 0): 8 bytes
+// per gather instead of 16 (GcFusedOptions.half_velocity, an experiment).
+__device__ __forceinline__ float4 unpack_vel(uint2 u) {
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+    return make_float4(a.x, a.y, b.x, 0.f);
+}
+
+__global__ void fk_pack_vel(int n, const float4* __restrict__ v, uint2* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 x = v[i];
+    const __half2 a = __floats2half2_rn(x.x, x.y), b = __floats2half2_rn(x.z, 0.f);
+    out[i] = make_uint2(*reinterpret_cast<const unsigned*>(&a), *reinterpret_cast<const unsigned*>(&b));
+}
+
+template <bool COMPACT, bool ENS, bool HALFV>
 __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
     fk_force(int n, GcParams p, SysInfo s0, const SysInfo* __restrict__ sys, const int* __restrict__ sysid,
              const unsigned* __restrict__ nkey, const float4* __restrict__ pos, const float4* __restrict__ vpred,
              const float4* __restrict__ vh, const float2* __restrict__ dp, float4* __restrict__ force,
              float4* __restrict__ vel, const int* __restrict__ nbr, const int* __restrict__ cnt, int cap,
-             const unsigned* __restrict__ cmask, int mw, const float4* __restrict__ mforce, int drive) {
+             const unsigned* __restrict__ cmask, int mw, const float4* __restrict__ mforce, int drive,
+             const uint2* __restrict__ vph) {
     constexpr int G = kForceGroup;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -552,7 +570,7 @@ __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
         for (int u = 0; u < G; ++u) {
             xg[u] = pos[jq[0][u]];
             dg[u] = dp[jq[0][u]];
-            vg[u] = vpred[jq[0][u]];
+            vg[u] = HALFV ? unpack_vel(vph[jq[0][u]]) : vpred[jq[0][u]];
         }
 #pragma unroll
         for (int a = 0; a + 1 < A; ++a)
@@ -1400,7 +1418,7 @@ int rebuild_lists(GcFused* f) {
     fk_cellkey<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->a.pos, f->keys, f->vals);
     GC_CHECK_LAUNCH("fused: cube keys");
     GC_TRY(gc_counting_sort_bufs(n, f->K, f->keys, f->vals, f->sb, f->flags, st));
-    fk_permute<<<nb, f->block, 0, st>>>(n, f->dsys, f->vals, f->a, f->b, f->refpos, f->slot_of);
+    fk_permute<<<nb, f->block, 0, st>>>(n, f->dsys, f->vals, f->a, f->b, f->refpos, f->slot_of, f->ddpos);
     GC_CHECK_LAUNCH("fused: permute");
     std::swap(f->a, f->b);
     drop_graphs(f);   // captured steps are bound to the old slot arrays
@@ -1461,11 +1479,13 @@ int launch_integrate(GcFused* f, cudaStream_t st, const GcParams& p) {
     if (f->ens)
         fk_integrate<true><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vel, f->a.vh,
                                                      f->a.vpred, f->a.force, f->a.plo, f->refpos, f->a.nthro,
-                                                     hs * hs, f->rebuild, f->mpos, f->mplo, f->mnthro, f->flags);
+                                                     hs * hs, f->rebuild, f->mpos, f->mplo, f->mnthro, f->flags,
+                                                     f->ddpos);
     else
         fk_integrate<false><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vel, f->a.vh,
                                                       f->a.vpred, f->a.force, f->a.plo, f->refpos, f->a.nthro,
-                                                      hs * hs, f->rebuild, f->mpos, f->mplo, f->mnthro, f->flags);
+                                                      hs * hs, f->rebuild, f->mpos, f->mplo, f->mnthro, f->flags,
+                                                     f->ddpos);
     GC_CHECK_LAUNCH("fused: integrate");
     return GC_OK;
 }
@@ -1524,26 +1544,33 @@ int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p) {
     return GC_OK;
 }
 
-template <bool COMPACT>
+template <bool COMPACT, bool HALFV>
 void force_launch(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
     const int n = f->n, nb = gc_blocks(n, f->block);
     const float4* mf = f->ncell > 0 ? f->mforce : nullptr;
     const int* c = COMPACT ? f->ccnt : f->cnt;
     const unsigned* cm = COMPACT ? f->cmask : nullptr;
     if (f->ens)
-        fk_force<COMPACT, true><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos,
-                                                          f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel, f->nbr,
-                                                          c, f->cap, cm, f->mw, mf, drive);
+        fk_force<COMPACT, true, HALFV><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos,
+                                                                 f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
+                                                                 f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph);
     else
-        fk_force<COMPACT, false><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos,
-                                                           f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel, f->nbr,
-                                                           c, f->cap, cm, f->mw, mf, drive);
+        fk_force<COMPACT, false, HALFV><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos,
+                                                                  f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
+                                                                  f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph);
 }
 
 int launch_force(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
     if (!f->lists) return launch_tile_force(f, st, p, drive, false);
-    if (f->compact) force_launch<true>(f, st, p, drive);
-    else force_launch<false>(f, st, p, drive);
+    if (f->halfv) {
+        fk_pack_vel<<<gc_blocks(f->n, 256), 256, 0, st>>>(f->n, f->a.vpred, f->vph);
+        GC_CHECK_LAUNCH("fused: pack velocities");
+        if (f->compact) force_launch<true, true>(f, st, p, drive);
+        else force_launch<false, true>(f, st, p, drive);
+    } else {
+        if (f->compact) force_launch<true, false>(f, st, p, drive);
+        else force_launch<false, false>(f, st, p, drive);
+    }
     GC_CHECK_LAUNCH("fused: force");
     return GC_OK;
 }
@@ -1626,7 +1653,7 @@ int launch_rebuild_body(GcFused* f, cudaStream_t st) {
     fk_cellkey<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->a.pos, f->keys, f->vals);
     GC_CHECK_LAUNCH("fused: cube keys");
     GC_TRY(gc_counting_sort_bufs(n, f->K, f->keys, f->vals, f->sb, f->flags, st));
-    fk_permute<<<nb, f->block, 0, st>>>(n, f->dsys, f->vals, f->a, f->b, f->refpos, f->slot_of);
+    fk_permute<<<nb, f->block, 0, st>>>(n, f->dsys, f->vals, f->a, f->b, f->refpos, f->slot_of, f->ddpos);
     GC_CHECK_LAUNCH("fused: permute");
     fk_copy_slots<<<nb, f->block, 0, st>>>(n, f->b, f->a);
     GC_CHECK_LAUNCH("fused: copy slots");
@@ -2063,6 +2090,8 @@ int apply_options(GcFused* f, const GcFusedOptions* opt) {
     f->compact = opt->compact != 0;
     f->graph = opt->graph != 0;
     f->lists = opt->tiles == 0;
+    f->ddpos = opt->fp32_positions ? 0 : 1;
+    f->halfv = opt->half_velocity != 0;
     return GC_OK;
 }
 
@@ -2261,6 +2290,7 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
     }
     if (ok == GC_OK) ok = falloc(f, &f->refpos, n);
     if (ok == GC_OK) ok = falloc(f, &f->dp, n);
+    if (ok == GC_OK) ok = falloc(f, &f->vph, (size_t)n + 1);
     if (ok == GC_OK) ok = falloc(f, &f->slot_of, n);
     if (ok == GC_OK) ok = falloc(f, &f->keys, n > f->ncp ? n : f->ncp);
     if (ok == GC_OK) ok = falloc(f, &f->vals, n > f->ncp ? n : f->ncp);
@@ -2317,6 +2347,7 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
         f->h->need = 0;
         if (cudaMemsetAsync(f->flags, 0, sizeof(unsigned), f->st) != cudaSuccess ||
             cudaMemsetAsync(f->cnt, 0, (size_t)n * sizeof(int), f->st) != cudaSuccess ||   // lists of no slot yet
+            cudaMemsetAsync(f->vph, 0, ((size_t)n + 1) * sizeof(uint2), f->st) != cudaSuccess ||
             cudaMemsetAsync(f->drebuilds, 0, 8, f->st) != cudaSuccess ||
             cudaMemsetAsync(f->dstep, 0xff, 8, f->st) != cudaSuccess)   // -1
             ok = gc_fail(GC_ECUDA, "fused: clear counters");
@@ -2594,6 +2625,8 @@ int gc_fused_get_options(GcFused* f, GcFusedOptions* opt) {
     opt->compact = f->compact ? 1 : 0;
     opt->graph = f->graph ? 1 : 0;
     opt->tiles = f->lists ? 0 : 1;
+    opt->fp32_positions = f->ddpos ? 0 : 1;
+    opt->half_velocity = f->halfv ? 1 : 0;
     return GC_OK;
 }
 

@@ -49,6 +49,14 @@ __device__ __forceinline__ void dd_add(float& hi, float& lo, float d) {
     lo = __fsub_rn(t, __fsub_rn(hi, s));
 }
 
+// x += d for a position: double-float (dd_add) or, with ddpos = 0 (the
+// plain FP32 variant, GcFusedOptions.fp32_positions), one FP32 addition with
+// the low part left as it is (zero).
+__device__ __forceinline__ void pos_add(float& hi, float& lo, float d, int ddpos) {
+    if (ddpos) dd_add(hi, lo, d);
+    else hi = __fadd_rn(hi, d);
+}
+
 __device__ __forceinline__ double block_sum_d(double v, double* sh) {
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -185,6 +193,9 @@ struct GcFused {
     int noise_on = 1;
     bool compact = false;
     bool graph = false;            // steps run as captured graphs
+    int ddpos = 1;                 // positions double-float (0: plain FP32, GcFusedOptions.fp32_positions)
+    bool halfv = false;            // neighbour velocities packed to FP16 for the force pass
+    uint2* vph = nullptr;          // those packed velocities (x, y, z, 0 as halves)
     bool ens = false;              // kernels read the system table
     long long step = -1;           // index keying the noise of the latest step
     long long rebuilds = 0, steps = 0;

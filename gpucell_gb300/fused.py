@@ -26,9 +26,10 @@ def _ptr(a):
     return C.c_void_p(a.data_ptr())
 
 
-def _options(skin, block, list_capacity, compact, graph, tiles=False):
+def _options(skin, block, list_capacity, compact, graph, tiles=False, fp32_positions=False, half_velocity=False):
     return _lib.GcFusedOptions(skin=skin, block=block, list_capacity=list_capacity, compact=1 if compact else 0,
-                               graph=1 if graph else 0, tiles=1 if tiles else 0)
+                               graph=1 if graph else 0, tiles=1 if tiles else 0,
+                               fp32_positions=1 if fp32_positions else 0, half_velocity=1 if half_velocity else 0)
 
 
 def _cell_arrays(cfg: Config):
@@ -87,12 +88,14 @@ class _Handle:
         o = _lib.GcFusedOptions()
         _lib.call("gc_fused_get_options", self.h, C.byref(o))
         return dict(skin=round(float(o.skin), 6), block=o.block, list_capacity=o.list_capacity,
-                    compact=bool(o.compact), graph=bool(o.graph), tiles=bool(o.tiles))
+                    compact=bool(o.compact), graph=bool(o.graph), tiles=bool(o.tiles),
+                    fp32_positions=bool(o.fp32_positions), half_velocity=bool(o.half_velocity))
 
     def set_options(self, skin=0.0, block=0, list_capacity=0, compact=None, graph=None, tiles=None):
         cur = self.options()
         o = _options(skin, block, list_capacity, cur["compact"] if compact is None else compact,
-                     cur["graph"] if graph is None else graph, cur["tiles"] if tiles is None else tiles)
+                     cur["graph"] if graph is None else graph, cur["tiles"] if tiles is None else tiles,
+                     cur["fp32_positions"], cur["half_velocity"])
         _lib.call("gc_fused_set_options", self.h, C.byref(o))
 
     def autotune(self, trial_steps=30, drive_on=1, use_cache=False) -> dict:
@@ -157,12 +160,12 @@ class _Handle:
 
 class FusedSystem(_Handle):
     def __init__(self, cfg: Config, noise=True, skin=0.1, block=128, list_capacity=0, compact=True, graph=False,
-                 tiles=False):
+                 tiles=False, fp32_positions=False, half_velocity=False):
         self.cfg = cfg
         self.lib = _lib.load()
         self.h = C.c_void_p()
         consts = _lib.Structconst(**cfg.consts())
-        opt = _options(skin, block, list_capacity, compact, graph, tiles)
+        opt = _options(skin, block, list_capacity, compact, graph, tiles, fp32_positions, half_velocity)
         bbox = np.ascontiguousarray(cfg.bbox, np.float32)
         _lib.call("gc_fused_create", C.byref(consts), _ptr(bbox), cfg.pmask, 1 if noise else 0, C.byref(opt),
                   C.byref(self.h))

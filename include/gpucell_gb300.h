@@ -201,7 +201,10 @@ typedef struct {
                              passes evaluate every pair once and give each side its share.  A handle with
                              tiles turns to lists by itself when a cube holds more than 96 particles or a
                              periodic axis has fewer than three cubes */
-    int reserved[2];
+    int fp32_positions;   /* 1: positions accumulate in plain FP32 (the double-float update off), for
+                             comparing precisions */
+    int half_velocity;    /* 1: the list force pass gathers neighbour velocities packed to FP16 (8 B instead
+                             of 16), an experiment */
 } GcFusedOptions;
 /* bbox6 (host) as src/main.cuh:12; periodic_mask as gc_set_periodic. */
 int gc_fused_create(const Structconst* consts, const float* bbox6, int periodic_mask, int noise_on,

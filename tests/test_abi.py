@@ -36,8 +36,9 @@ def test_option_and_system_records_match_the_header():
     assert C.sizeof(GcSystemDesc) == 128
     assert GcSystemDesc.bbox.offset == 96 and GcSystemDesc.periodic_mask.offset == 120
     txt = open(HEADER).read()
-    assert GcFusedOptions.tiles.offset == 20
-    assert "int graph;" in txt and "int tiles;" in txt and "int reserved[2];" in txt and "Structconst consts;" in txt
+    assert GcFusedOptions.tiles.offset == 20 and GcFusedOptions.half_velocity.offset == 28
+    assert "int graph;" in txt and "int tiles;" in txt and "int fp32_positions;" in txt and "int half_velocity;" in txt
+    assert "Structconst consts;" in txt
 
 
 def test_library_exports_every_declared_function(built_library):
