@@ -538,9 +538,15 @@ __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
     int base = -32;
     // index of the next acting entry (COMPACT) or of the next entry; called
     // once per entry, in order.  The scan for a non-empty mask word ends: it
-    // runs only while k < c, and the density pass writes the c acting bits
-    // of the row and the count c together (a bound on the row's words cost
-    // 6 % of this kernel).
+    // runs only while k < c, and c = ccnt[i] is the number of bits set in the
+    // row's mask words, which fk_density writes together with it, word by
+    // word, in the same thread.  Every launch of this kernel with COMPACT
+    // follows a fk_density launch with the mask on in the same step (host-
+    // driven steps, captured steps, refresh after a rebuild, a restore or a
+    // change of options); set-up's density pass without the mask is always
+    // followed by such a step before any force pass.  A list that overflowed
+    // keeps cap entries, and both passes read the same c <= cap of them.  (A
+    // bound on the row's words cost 6 % of this kernel.)
     auto next_k = [&](int k) -> int {
         if constexpr (COMPACT) {
             while (m == 0) {
@@ -1004,10 +1010,14 @@ __device__ __forceinline__ void morse_run(const GcParams& p, const GcGrid& g, fl
     for (; s < b; ++s) morse_pair(p, g, xi, ai, mspos[s], msarea + s, f);
 }
 
-// Morse aggregation between vertices of different cells, one thread per
+// Morse aggregation between vertices of different cells, eight lanes per
 // vertex in grid order, over the (2R+1)^3 aggregation cubes around it (R = 2
-// for cubes at least MaxCut/2 wide, 1 for cubes at least MaxCut wide).  The
-// sort is stable and membrane vertices are in id order, so
+// for cubes at least MaxCut/2 wide, 1 for cubes at least MaxCut wide): lane
+// k of a vertex's group scans the rows (dy, dz) k, k + 8, ... of the stencil,
+// and the group adds its eight partial forces by a fixed xor tree.  Vertices
+// near dense membrane contacts have several times the mean number of
+// candidates; split eight ways, their scans no longer set the length of the
+// pass.  The sort is stable and membrane vertices are in id order, so
 // within a cube the candidates ascend by id.  RUNS (every cell is one
 // contiguous id range that carries its CellTab index, checked at set-up):
 // the vertex's own cell is one run of a cube's candidates, bounded by two
@@ -1019,6 +1029,7 @@ __device__ __forceinline__ void morse_run(const GcParams& p, const GcGrid& g, fl
 #define GC_AGG_BS 128
 #endif
 constexpr int kAggBS = GC_AGG_BS;
+constexpr int kAggLanes = 8;   // lanes per vertex (a power of two dividing 32)
 
 template <bool RUNS>
 __global__ void __launch_bounds__(kAggBS) fk_magg(int ncp, GcParams p, const SysInfo* __restrict__ sys,
@@ -1028,29 +1039,30 @@ __global__ void __launch_bounds__(kAggBS) fk_magg(int ncp, GcParams p, const Sys
                                                   const int* __restrict__ celltab,
                                                   const int2* __restrict__ cell_verts, float4* __restrict__ magg,
                                                   float4* __restrict__ mforce) {
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= ncp) return;
-    int v = order[q];
-    const SysInfo& S = sys[msys ? msys[v] : 0];
-    const GcGrid& g = S.mg;
-    float3 xi = xyz(mspos[q]);
-    int ci = celltab[v];
-    float ai = msarea[q];
-    unsigned own_lo = 0, own_hi = 0;   // ids of the vertex's own cell
-    if (RUNS) {
-        int2 cv = cell_verts[ci];
-        own_lo = S.cs + (unsigned)(cv.x - (int)S.m0);
-        own_hi = S.cs + (unsigned)(cv.y - (int)S.m0);
-    }
-    int cx = cube_coord(xi.x, 0, g), cy = cube_coord(xi.y, 1, g), cz = cube_coord(xi.z, 2, g);
-    const int R = S.mlr;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = (int)(t / kAggLanes), k = (int)(t % kAggLanes);
+    const bool live = q < ncp;   // whole groups: kAggLanes divides the block
     float3 f = f3(0.f, 0.f, 0.f);
-    for (int dz = -R; dz <= R; ++dz) {
-        int z = cube_step(cz, dz, 2, g);
-        if (z < 0) continue;
-        for (int dy = -R; dy <= R; ++dy) {
-            int y = cube_step(cy, dy, 1, g);
-            if (y < 0) continue;
+    int v = 0;
+    if (live) {
+        v = order[q];
+        const SysInfo& S = sys[msys ? msys[v] : 0];
+        const GcGrid& g = S.mg;
+        const float3 xi = xyz(mspos[q]);
+        const int ci = celltab[v];
+        const float ai = msarea[q];
+        unsigned own_lo = 0, own_hi = 0;   // ids of the vertex's own cell
+        if (RUNS) {
+            int2 cv = cell_verts[ci];
+            own_lo = S.cs + (unsigned)(cv.x - (int)S.m0);
+            own_hi = S.cs + (unsigned)(cv.y - (int)S.m0);
+        }
+        const int cx = cube_coord(xi.x, 0, g), cy = cube_coord(xi.y, 1, g), cz = cube_coord(xi.z, 2, g);
+        const int R = S.mlr, side = 2 * R + 1;
+        for (int row = k; row < side * side; row += kAggLanes) {
+            const int z = cube_step(cz, row / side - R, 2, g);
+            const int y = cube_step(cy, row % side - R, 1, g);
+            if (z < 0 || y < 0) continue;
             for (int dx = -R; dx <= R; ++dx) {
                 int x = cube_step(cx, dx, 0, g);
                 if (x < 0) continue;
@@ -1084,6 +1096,14 @@ __global__ void __launch_bounds__(kAggBS) fk_magg(int ncp, GcParams p, const Sys
             }
         }
     }
+    // the group's partial forces, added by a fixed tree
+#pragma unroll
+    for (int o = kAggLanes / 2; o; o >>= 1) {
+        f.x += __shfl_xor_sync(0xffffffffu, f.x, o, kAggLanes);
+        f.y += __shfl_xor_sync(0xffffffffu, f.y, o, kAggLanes);
+        f.z += __shfl_xor_sync(0xffffffffu, f.z, o, kAggLanes);
+    }
+    if (!live || k != 0) return;
     magg[v] = make_float4(f.x, f.y, f.z, 0.f);
     float4* o = &mforce[v];
     o->x += f.x;   // one thread per vertex, after the deformation kernels
@@ -1532,7 +1552,7 @@ int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p) {
         const int nb = gc_blocks(f->ncp, f->block);
         fk_msort<<<nb, f->block, 0, st>>>(f->ncp, f->mvals, f->mpos, f->parea, f->mspos, f->msarea);
         GC_CHECK_LAUNCH("fused: aggregation order");
-        const int nba = gc_blocks(f->ncp, kAggBS);
+        const int nba = gc_blocks((int)((long long)f->ncp * kAggLanes), kAggBS);
         if (f->agg_runs)
             fk_magg<true><<<nba, kAggBS, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mvals, f->sb_agg.cnt, f->mspos,
                                                   f->msarea, f->celltab, f->cell_verts, f->magg, f->mforce);

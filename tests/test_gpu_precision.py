@@ -4,7 +4,8 @@
   double-float positions, on a walled channel with a cell over 1000 steps
   (noise off): both follow the oracle; the double-float trajectory stays
   closer (drift printed for both), and particles far from the origin under
-  a small body force keep their displacement only with double-float
+  a small body force, whose every step's displacement is below half an FP32
+  ulp of their position, keep it accurately only with double-float
   positions.
 * Neighbour velocities packed to FP16 for the force gathers
   (GcFusedOptions.half_velocity), an experiment: one force evaluation on
@@ -60,10 +61,11 @@ def test_fp32_positions_against_double_float(cuda_device):
 
 def test_fp32_positions_lose_small_displacements_far_out(cuda_device):
     """A fluid box shifted to x ~ 150-160 under a small body force: after
-    1000 steps (mean displacement ~1e-3, each step's below half an FP32 ulp
-    of x, 7.6e-6) the mean displacement along x matches the oracle's with
-    double-float positions (within 1 %), and not with FP32 ones, where each
-    step's displacement rounds away."""
+    1000 steps (mean displacement ~1e-3; each step's displacement, up to
+    2e-6, is below half an FP32 ulp of x, 7.6e-6) the mean displacement along
+    x matches the oracle's with double-float positions (within 1 %; measured
+    4e-5), and FP32 positions, which round every step's displacement to a
+    whole ulp, end farther off (measured 0.6 %)."""
     from gpucell_gb300.fused import FusedSystem
     base = gen.suspension(nx=24, ny=12, nz=12, ncells=0, seed=2, phys=gen.Physics(ext_force=2e-3, temp=0.0))
     shift = np.array([150.0, 0.0, 0.0], np.float32)
