@@ -202,18 +202,18 @@ TILE_PARTIAL_BYTES = {"force": 2 * 14 * 12, "density": 2 * 14 * 4}
 # the kernel's code, refreshed whenever it changes; the line says which
 # capture they come from):
 #   python bench.py --small --no-ensemble --cpu-steps 0 --no-plain --no-engine --no-output --no-parity
-#       --no-configs --steps 3 --warmup 3 --profile-steps 1 --e2e-steps 1   (plain run, exit 0), then
-#   ncu --set full --clock-control none -k regex:"fk_(force|density)" -s 6 -c 2 <the same command>
+#       --no-configs --no-variants --steps 3 --warmup 3 --profile-steps 1 --e2e-steps 1   (plain run, exit 0),
+#   then ncu --set full --clock-control none -k regex:"fk_(force|density)" -s 6 -c 2 <the same command>
 # on the 524,288-particle suspension (warp instructions and FP32 operations
 # per particle, mean list 143.7), and
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none
-#       -k regex:"fk_force" -s 8 -c 2 python bench.py --no-ensemble --cpu-steps 0 --no-plain --no-output
-#       --no-parity --no-configs --steps 4 --warmup 3 --profile-steps 1 --e2e-steps 1
+#       -k regex:"fk_force" -s 8 -c 2 python bench.py --no-ensemble --cpu-steps 0 --no-plain --no-engine
+#       --no-output --no-parity --no-configs --no-variants --steps 4 --warmup 3 --profile-steps 1 --e2e-steps 1
 # at full size (DRAM bytes of one launch, one pass).
 FORCE_COUNTERS = {
     "kernel_version": "fk_force: one thread per particle over its compact list of acting entries",
-    "dram_bytes_per_launch_4M": 2.845227264e9 + 0.127872512e9,
-    "warp_inst_per_particle": 348382172 / 524288,
+    "dram_bytes_per_launch_4M": 2.854405632e9 + 0.128385792e9,
+    "warp_inst_per_particle": 346474930 / 524288,
     "fp32_flop_per_particle": 5.224e9 / 524288,
 }
 # SM schedulers of a GB300 (152 SMs x 4, one warp instruction per cycle
