@@ -118,18 +118,113 @@ def measured_peaks():
     return PEAKS_FALLBACK, "fallback"
 
 
+# Clock-event reason bits of NVML's public API (nvmlClocksEventReason*), the
+# ones a bench line reports.
+NVML_REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+                0x80: "hw_power_brake_slowdown"}
+
+
+def _nvml():
+    """NVML through ctypes (read-only queries), or None where the driver's
+    library is absent."""
+    import ctypes
+    try:
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+    except OSError:
+        return None
+    if lib.nvmlInit_v2() != 0:
+        return None
+    return lib
+
+
+def _nvml_handle(lib, device):
+    """The NVML handle of CUDA device `device` (by PCI address when torch
+    gives it, else by index)."""
+    import ctypes
+    h = ctypes.c_void_p()
+    try:
+        import torch
+        p = torch.cuda.get_device_properties(device)
+        bus = f"{p.pci_domain_id:08x}:{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0".encode()
+        if lib.nvmlDeviceGetHandleByPciBusId_v2(ctypes.c_char_p(bus), ctypes.byref(h)) == 0:
+            return h
+    except (AttributeError, RuntimeError, AssertionError):
+        pass
+    if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(device), ctypes.byref(h)) == 0:
+        return h
+    return None
+
+
+def clock_record(samples, source, interval_ms):
+    """The bench line's `clocks` record from (sm_mhz, sm_max_mhz, reasons)
+    samples: median SM clock, the largest maximum clock, every throttle
+    reason active in any sample."""
+    if not samples:
+        return None
+    reasons = set()
+    for _, _, r in samples:
+        reasons |= set(r)
+    return {"sm_mhz": statistics.median(x[0] for x in samples), "sm_max_mhz": max(x[1] for x in samples),
+            "samples": len(samples), "reasons": sorted(reasons), "source": source, "interval_ms": interval_ms}
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons, sampled every 50 ms."""
+    """SM clocks and throttle reasons of the benchmarked GPU during a timed
+    region: NVML queried every `interval_ms` from a thread (the foreign calls
+    release the GIL), or, where NVML cannot be loaded, nvidia-smi every 50 ms.
+    Reading these settings changes nothing on the GPU."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self):
+    def __init__(self, interval_ms=10):
         self.proc = None
         self.path = None
+        self.thread = None
+        self.interval_ms = interval_ms
 
-    def start(self):
+    def start(self, device=None):
+        if device is None:
+            try:
+                import torch
+                device = torch.cuda.current_device()
+            except (ImportError, RuntimeError, AssertionError):
+                device = 0
+        lib = _nvml()
+        h = _nvml_handle(lib, device) if lib is not None else None
+        if h is not None:
+            self._start_nvml(lib, h)
+        else:
+            self._start_smi()
+
+    def _start_nvml(self, lib, h):
+        import ctypes  # noqa: F401 (the by-reference arguments below)
+        import threading
+        self.samples, self.stop_evt = [], threading.Event()
+        have_events = hasattr(lib, "nvmlDeviceGetCurrentClocksEventReasons")
+        reasons_fn = (lib.nvmlDeviceGetCurrentClocksEventReasons if have_events
+                      else lib.nvmlDeviceGetCurrentClocksThrottleReasons)
+        first = threading.Event()
+
+        def run():
+            sm, mx, r = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+            while not self.stop_evt.is_set():
+                if (lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(sm)) == 0          # NVML_CLOCK_SM
+                        and lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0
+                        and reasons_fn(h, ctypes.byref(r)) == 0):
+                    self.samples.append((float(sm.value), float(mx.value),
+                                         [nm for bit, nm in NVML_REASONS.items() if r.value & bit]))
+                first.set()
+                self.stop_evt.wait(self.interval_ms / 1e3)
+            first.set()
+
+        self.lib = lib
+        self.thread = threading.Thread(target=run, daemon=True)
+        self.thread.start()
+        first.wait(1.5)   # the timed region starts once the first sample is in
+
+    def _start_smi(self):
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
@@ -147,6 +242,12 @@ class ClockSampler:
             time.sleep(0.02)
 
     def stop(self, gpu_index=0):
+        if self.thread is not None:
+            self.stop_evt.set()
+            self.thread.join(timeout=5)
+            self.thread = None
+            self.lib.nvmlShutdown()
+            return clock_record(self.samples, "nvml", self.interval_ms)
         if not self.proc:
             return None
         self.proc.terminate()
@@ -155,25 +256,19 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.fh.close()
-        sm, smax, reasons = [], [], set()
+        samples = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9 or f[0] != str(gpu_index):
                 continue
             try:
-                sm.append(float(f[1]))
-                smax.append(float(f[2]))
+                sm, smax = float(f[1]), float(f[2])
             except ValueError:
                 continue
-            for nm, v in zip(names, f[5:9]):
-                if v.lower().startswith("active"):
-                    reasons.add(nm)
+            samples.append((sm, smax, [nm for nm, v in zip(names, f[5:9]) if v.lower().startswith("active")]))
         os.unlink(self.path)
-        if not sm:
-            return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
-                "reasons": sorted(reasons)}
+        return clock_record(samples, "nvidia-smi", 50)
 
 
 def plain_bytes_per_step(cfg):
@@ -420,7 +515,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     sampler = ClockSampler()
     if rank == 0:
-        sampler.start()
+        sampler.start(local)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     torch.cuda.synchronize()

@@ -68,9 +68,53 @@ def test_clock_samples_are_read_with_their_throttle_reasons(tmp_path):
     s.proc = _FakeSampler()
     rec = s.stop(gpu_index=0)
     assert rec == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "samples": 3,
-                   "reasons": ["hw_thermal_slowdown", "sw_power_cap"]}
+                   "reasons": ["hw_thermal_slowdown", "sw_power_cap"], "source": "nvidia-smi", "interval_ms": 50}
     assert not os.path.exists(s.path)
     assert bench.ClockSampler().stop() is None   # never started: no record
+
+
+class _FakeNvml:
+    """Stands in for NVML: SM clocks 1980 then 2070 MHz, sw_power_cap then
+    hw_slowdown + sw_power_cap active."""
+
+    def __init__(self):
+        self.n = 0
+        self.shut = False
+
+    def nvmlDeviceGetClockInfo(self, h, kind, p):
+        assert kind == 1
+        p._obj.value = 1980 if self.n == 0 else 2070
+        return 0
+
+    def nvmlDeviceGetMaxClockInfo(self, h, kind, p):
+        p._obj.value = 2070
+        return 0
+
+    def nvmlDeviceGetCurrentClocksEventReasons(self, h, p):
+        p._obj.value = 0x4 if self.n == 0 else 0xC
+        self.n += 1
+        return 0
+
+    def nvmlShutdown(self):
+        self.shut = True
+        return 0
+
+
+def test_nvml_clock_samples_are_taken_in_a_thread():
+    """The NVML sampler: one sample at least before the timed region
+    starts, the reason bits named, NVML shut down at the end."""
+    import time
+
+    import bench
+    lib = _FakeNvml()
+    s = bench.ClockSampler(interval_ms=5)
+    s._start_nvml(lib, object())
+    assert len(s.samples) >= 1
+    time.sleep(0.05)
+    rec = s.stop()
+    assert lib.shut and rec["source"] == "nvml" and rec["interval_ms"] == 5
+    assert rec["samples"] >= 2 and rec["sm_max_mhz"] == 2070.0
+    assert rec["reasons"] == ["hw_slowdown", "sw_power_cap"]
 
 
 def test_metric_name_follows_the_workload_size():
