@@ -125,28 +125,36 @@ __global__ void fk_integrate(int n, GcParams p, SysInfo s0, const SysInfo* __res
             pos_add(x.y, lo.y, p.dt * v.y + h * f.y, ddpos);
             pos_add(x.z, lo.z, p.dt * v.z + h * f.z, ddpos);
             if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) raise_flag(flags, GC_FLAG_NONFINITE);
-            int4 t = nthro[i];
-            bool crossed = false;
+            // periodic crossings; the crossing counts are read only where
+            // they change or are mirrored (membrane vertices)
+            int cr[3] = {0, 0, 0};
             float* xs[3] = {&x.x, &x.y, &x.z};
             float* ls[3] = {&lo.x, &lo.y, &lo.z};
-            int* ts[3] = {&t.x, &t.y, &t.z};
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 if (!(S.g.pmask & (1 << a))) continue;
                 float c = *xs[a];
-                if (c >= S.g.hi[a]) { pos_add(*xs[a], *ls[a], -S.g.L[a], ddpos); *ts[a] += 1; crossed = true; }
-                else if (c < S.g.lo[a]) { pos_add(*xs[a], *ls[a], S.g.L[a], ddpos); *ts[a] -= 1; crossed = true; }
+                if (c >= S.g.hi[a]) { pos_add(*xs[a], *ls[a], -S.g.L[a], ddpos); cr[a] = 1; }
+                else if (c < S.g.lo[a]) { pos_add(*xs[a], *ls[a], S.g.L[a], ddpos); cr[a] = -1; }
             }
-            if (crossed) nthro[i] = t;
+            const bool crossed = (cr[0] | cr[1] | cr[2]) != 0, memb = id >= S.cs;
+            int4 t = make_int4(0, 0, 0, 0);
+            if (crossed || memb) {
+                t = nthro[i];
+                t.x += cr[0];
+                t.y += cr[1];
+                t.z += cr[2];
+                if (crossed) nthro[i] = t;
+            }
             pos[i] = x;
             plo[i] = lo;
+            // VelHalf's fourth word is always zero
             float hs = 0.5f * p.dt * p.inv_mass, l = p.lambda * p.dt * p.inv_mass;
-            float4 w = vh[i];
-            vh[i] = make_float4(v.x + hs * f.x, v.y + hs * f.y, v.z + hs * f.z, w.w);
+            vh[i] = make_float4(v.x + hs * f.x, v.y + hs * f.y, v.z + hs * f.z, 0.f);
             vpred[i] = make_float4(v.x + l * f.x, v.y + l * f.y, v.z + l * f.z, 0.f);
             float3 d = min_image(xyz(x), xyz(refpos[i]), S.g);
             far = norm2_rn(d) > half_skin2;
-            if (id >= S.cs) {
+            if (memb) {
                 unsigned m = S.m0 + (id - S.cs);
                 mpos[m] = x;
                 mplo[m] = lo;
@@ -434,7 +442,9 @@ __global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, 
                 }
             }
         };
-        if (near_face(xi, S.g, wrap_margin)) run(std::true_type{});
+        // one form per warp (the image where any of its particles is near a
+        // periodic face), so that a warp does not run both
+        if (__any_sync(__activemask(), near_face(xi, S.g, wrap_margin))) run(std::true_type{});
         else run(std::false_type{});
         if (ccnt) ccnt[i] = kc;
         float rho = p.mass * sum;
@@ -510,7 +520,7 @@ __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
              const float4* __restrict__ vh, const float2* __restrict__ dp, float4* __restrict__ force,
              float4* __restrict__ vel, const int* __restrict__ nbr, const int* __restrict__ cnt, int cap,
              const unsigned* __restrict__ cmask, int mw, const float4* __restrict__ mforce, int drive,
-             const uint2* __restrict__ vph) {
+             const uint2* __restrict__ vph, float wrap_margin) {
     constexpr int G = kForceGroup;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -561,69 +571,83 @@ __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
         }
     };
     constexpr int A = kForceAhead;
-    int jq[A][G];
+    // The pair terms are gathered into three vectors: one coefficient along
+    // d = x_i - x_j (pressure, the e e^T parts of the viscous and random
+    // forces, with e = d / r folded into the coefficients as 1/r^2), one
+    // along v_ij (viscous) and one along xi_ij (random).  F (d_i^-1 d_j^-1)
+    // is formed as F times the product of the two inverse number densities,
+    // the same product from either side of the pair.
+    const float cAB = p.sqrtAB - p.sqrtA;
+    auto run = [&](auto wrapc) {
+        constexpr bool W = decltype(wrapc)::value;
+        int jq[A][G];
 #pragma unroll
-    for (int a = 0; a < A; ++a)
+        for (int a = 0; a < A; ++a)
 #pragma unroll
-        for (int u = 0; u < G; ++u) {
-            int k = a * G + u;
-            jq[a][u] = k < c ? __ldg(lp + (size_t)next_k(k) * 32) : i;
-        }
-    for (int k0 = 0; k0 < c; k0 += G) {
-        float4 xg[G], vg[G];
-        float2 dg[G];
+            for (int u = 0; u < G; ++u) {
+                int k = a * G + u;
+                jq[a][u] = k < c ? __ldg(lp + (size_t)next_k(k) * 32) : i;
+            }
+        for (int k0 = 0; k0 < c; k0 += G) {
+            float4 xg[G], vg[G];
+            float2 dg[G];
 #pragma unroll
-        for (int u = 0; u < G; ++u) {
-            xg[u] = pos[jq[0][u]];
-            dg[u] = dp[jq[0][u]];
-            vg[u] = HALFV ? unpack_vel(vph[jq[0][u]]) : vpred[jq[0][u]];
-        }
+            for (int u = 0; u < G; ++u) {
+                xg[u] = pos[jq[0][u]];
+                dg[u] = dp[jq[0][u]];
+                vg[u] = HALFV ? unpack_vel(vph[jq[0][u]]) : vpred[jq[0][u]];
+            }
 #pragma unroll
-        for (int a = 0; a + 1 < A; ++a)
+            for (int a = 0; a + 1 < A; ++a)
 #pragma unroll
-            for (int u = 0; u < G; ++u) jq[a][u] = jq[a + 1][u];
+                for (int u = 0; u < G; ++u) jq[a][u] = jq[a + 1][u];
 #pragma unroll
-        for (int u = 0; u < G; ++u) {
-            int k = k0 + A * G + u;
-            jq[A - 1][u] = k < c ? __ldg(lp + (size_t)next_k(k) * 32) : i;
-        }
+            for (int u = 0; u < G; ++u) {
+                int k = k0 + A * G + u;
+                jq[A - 1][u] = k < c ? __ldg(lp + (size_t)next_k(k) * 32) : i;
+            }
 #pragma unroll
-        for (int u = 0; u < G; ++u) {
-            if (k0 + u >= c) break;
-            float4 xj4 = xg[u];
-            float3 d = pair_image(xi, xyz(xj4), B);
-            float r2 = norm2_rn(d);
-            if (!COMPACT && (r2 >= p.rc2 || r2 <= 0.f)) continue;   // coincident pairs exert no force
-            unsigned idj = fid(xj4);
-            float inv_r = rsqrtf(r2);
-            if (idj < b2) {   // Bound1: repulsion only
-                if (r2 < p.rep_r0sq) {
-                    float ir2 = inv_r * inv_r;
-                    float q2 = p.rep_r0sq * ir2, q4 = q2 * q2, q12 = q4 * q4 * q4;
-                    f += (p.rep_D * (q12 - q4) * ir2) * d;
+            for (int u = 0; u < G; ++u) {
+                if (k0 + u >= c) break;
+                float4 xj4 = xg[u];
+                float3 d = pair_diff<W>(xi, xyz(xj4), B);
+                float r2 = norm2_rn(d);
+                if (!COMPACT && (r2 >= p.rc2 || r2 <= 0.f)) continue;   // coincident pairs exert no force
+                unsigned idj = fid(xj4);
+                float inv_r = rsqrtf(r2);
+                if (idj < b2) {   // Bound1: repulsion only
+                    if (r2 < p.rep_r0sq) {
+                        float ir2 = inv_r * inv_r;
+                        float q2 = p.rep_r0sq * ir2, q4 = q2 * q2, q12 = q4 * q4 * q4;
+                        f += (p.rep_D * (q12 - q4) * ir2) * d;
+                    }
+                    continue;
                 }
-                continue;
-            }
-            float2 dpj = dg[u];
-            float4 vj = vg[u];
-            float r = r2 * inv_r;
-            float F = wendland_f(r, p);
-            f += ((dpi.y + dpj.y) * F) * d;
-            float3 e = inv_r * d;
-            float3 vij = f3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z);
-            float ev = dot3(e, vij);
-            float fdd = F * dpi.x * dpj.x;
-            f -= fdd * (p.visA * vij + (p.visB * ev) * e);
-            if (noise) {
-                float qq = p.noise_pref * fdd;
-                float q = qq > 0.f ? qq * rsqrtf(qq) : 0.f;
-                q = id < idj ? q : -q;   // the pair sign of xi_ij
-                float3 xi_ = pair_noise_unsigned_k(id - id0, idj - id0, key);
-                float exi = dot3(e, xi_);
-                f += q * (p.sqrtA * xi_ + ((p.sqrtAB - p.sqrtA) * exi) * e);
+                float2 dpj = dg[u];
+                float4 vj = vg[u];
+                float F = wendland_f(r2 * inv_r, p);
+                float ir2 = inv_r * inv_r;
+                float3 vij = f3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z);
+                float fdd = F * (dpi.x * dpj.x);
+                float cd = (dpi.y + dpj.y) * F - (fdd * p.visB) * dot3(d, vij) * ir2;
+                f += (-fdd * p.visA) * vij;
+                if (noise) {
+                    float qq = p.noise_pref * fdd;
+                    float q = qq > 0.f ? qq * rsqrtf(qq) : 0.f;
+                    q = id < idj ? q : -q;   // the pair sign of xi_ij
+                    float3 xi_ = pair_noise_unsigned_k(id - id0, idj - id0, key);
+                    cd += (q * cAB) * dot3(d, xi_) * ir2;
+                    f += (q * p.sqrtA) * xi_;
+                }
+                f += cd * d;
             }
         }
-    }
+    };
+    // A warp whose particles all lie farther than wrap_margin from every
+    // periodic face forms plain differences (equal to the minimum image for
+    // every listed pair there); any other warp forms the image.
+    if (__any_sync(__activemask(), near_face(xi, S.g, wrap_margin))) run(std::true_type{});
+    else run(std::false_type{});
     if (drive) f.x += S.gx;
     if (id >= S.cs && mforce) {
         float4 mf = mforce[S.m0 + (id - S.cs)];
@@ -1573,11 +1597,13 @@ void force_launch(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
     if (f->ens)
         fk_force<COMPACT, true, HALFV><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos,
                                                                  f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
-                                                                 f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph);
+                                                                 f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph,
+                                                                 wrap_margin(f));
     else
         fk_force<COMPACT, false, HALFV><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos,
                                                                   f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
-                                                                  f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph);
+                                                                  f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph,
+                                                                  wrap_margin(f));
 }
 
 int launch_force(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
