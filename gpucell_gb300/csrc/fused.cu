@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, 
                         const float3 dd = pair_diff<W>(xi, xyz(xj[u]), B);
                         const float r2 = fmaf(dd.x, dd.x, fmaf(dd.y, dd.y, dd.z * dd.z));
                         const bool in = r2 < p.rc2, apart = r2 > 0.f, sdpd = fid(xj[u]) >= b2;
-                        const float r = apart ? r2 * rsqrtf(r2) : 0.f;
+                        const float r = apart ? r2 * rsqrt_ftz(r2) : 0.f;
                         const float w = wendland_w(r, p);
                         sum += in && sdpd ? w : 0.f;
                         // acting: an SDPD partner within rc, or a Bound1 wall within the repulsion range
@@ -614,7 +614,7 @@ __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
                 float r2 = norm2_rn(d);
                 if (!COMPACT && (r2 >= p.rc2 || r2 <= 0.f)) continue;   // coincident pairs exert no force
                 unsigned idj = fid(xj4);
-                float inv_r = rsqrtf(r2);
+                float inv_r = rsqrt_ftz(r2);
                 if (idj < b2) {   // Bound1: repulsion only
                     if (r2 < p.rep_r0sq) {
                         float ir2 = inv_r * inv_r;
@@ -633,7 +633,7 @@ __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
                 f += (-fdd * p.visA) * vij;
                 if (noise) {
                     float qq = p.noise_pref * fdd;
-                    float q = qq > 0.f ? qq * rsqrtf(qq) : 0.f;
+                    float q = qq > 0.f ? qq * rsqrt_ftz(qq) : 0.f;
                     q = id < idj ? q : -q;   // the pair sign of xi_ij
                     float3 xi_ = pair_noise_unsigned_k(id - id0, idj - id0, key);
                     cd += (q * cAB) * dot3(d, xi_) * ir2;

@@ -117,6 +117,16 @@ __device__ __forceinline__ float3 min_image(float3 a, float3 b, const GcGrid& g)
               min_image_1(__fsub_rn(a.z, b.z), 2, g));
 }
 
+// 1/sqrt(x) by the hardware approximation with subnormal inputs flushed to
+// zero (PTX rsqrt.approx.ftz.f32): the pair loops call it only on normal
+// numbers (r^2 of two distinct listed particles, positive noise
+// amplitudes), where it matches rsqrtf without rsqrtf's subnormal path.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 __device__ __forceinline__ float norm2_rn(float3 d) {
     return __fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z));
 }
