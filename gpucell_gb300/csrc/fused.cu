@@ -22,8 +22,11 @@
 //     i at ((i/32)*cap + k)*32 + i%32, so a warp reads 128 contiguous bytes
 //     per k), and rebuilt (with a re-sort) only when some particle has moved
 //     more than skin/2 since the last build.  Every step still tests
-//     r^2 < rc^2 with the same FP32 expression as the boundary kernels, so
-//     the pairs that interact are exactly the same.
+//     r^2 < rc^2 in FP32 on the listed pairs, with r^2 formed by fused
+//     multiply-adds (the boundary kernels and the oracle round each square:
+//     a pair within one rounding of the cut-off, where the kernel and its
+//     derivative are below 1e-21 of their peaks, may count in one and not
+//     in the other).
 //   * Passes are fused: integrate + periodic wrap + predictor (K2, K3, K9);
 //     density + equation of state + wall velocity (K8, K11, K10); SDPD +
 //     wall repulsion + body force + membrane forces + corrector (K12, K13,
@@ -426,7 +429,7 @@ __global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, 
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
                         const float3 dd = pair_diff<W>(xi, xyz(xj[u]), B);
-                        const float r2 = fmaf(dd.x, dd.x, fmaf(dd.y, dd.y, dd.z * dd.z));
+                        const float r2 = norm2_fma(dd);
                         const bool in = r2 < p.rc2, apart = r2 > 0.f, sdpd = fid(xj[u]) >= b2;
                         const float r = apart ? r2 * rsqrt_ftz(r2) : 0.f;
                         const float w = wendland_w(r, p);
@@ -513,7 +516,7 @@ __global__ void fk_pack_vel(int n, const float4* __restrict__ v, uint2* __restri
     out[i] = make_uint2(*reinterpret_cast<const unsigned*>(&a), *reinterpret_cast<const unsigned*>(&b));
 }
 
-template <bool COMPACT, bool ENS, bool HALFV>
+template <bool COMPACT, bool ENS, bool HALFV, bool NOISE>
 __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
     fk_force(int n, GcParams p, SysInfo s0, const SysInfo* __restrict__ sys, const int* __restrict__ sysid,
              const unsigned* __restrict__ nkey, const float4* __restrict__ pos, const float4* __restrict__ vpred,
@@ -539,7 +542,6 @@ __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
     const uint32_t key = ENS ? nkey[s] : p.noise_key;
     float4 vi = vpred[i];
     float2 dpi = dp[i];
-    bool noise = p.noise_pref > 0.f;
     float3 f = f3(0.f, 0.f, 0.f);
     int c = cnt[i];
     const int* lp = nbr + sell(i, 0, cap);
@@ -611,7 +613,7 @@ __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
                 if (k0 + u >= c) break;
                 float4 xj4 = xg[u];
                 float3 d = pair_diff<W>(xi, xyz(xj4), B);
-                float r2 = norm2_rn(d);
+                float r2 = norm2_fma(d);   // as in fk_density
                 if (!COMPACT && (r2 >= p.rc2 || r2 <= 0.f)) continue;   // coincident pairs exert no force
                 unsigned idj = fid(xj4);
                 float inv_r = rsqrt_ftz(r2);
@@ -631,7 +633,7 @@ __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
                 float fdd = F * (dpi.x * dpj.x);
                 float cd = (dpi.y + dpj.y) * F - (fdd * p.visB) * dot3(d, vij) * ir2;
                 f += (-fdd * p.visA) * vij;
-                if (noise) {
+                if constexpr (NOISE) {
                     float qq = p.noise_pref * fdd;
                     float q = qq > 0.f ? qq * rsqrt_ftz(qq) : 0.f;
                     q = id < idj ? q : -q;   // the pair sign of xi_ij
@@ -1588,22 +1590,26 @@ int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p) {
     return GC_OK;
 }
 
-template <bool COMPACT, bool HALFV>
-void force_launch(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
+template <bool COMPACT, bool HALFV, bool NOISE>
+void force_launch_n(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
     const int n = f->n, nb = gc_blocks(n, f->block);
     const float4* mf = f->ncell > 0 ? f->mforce : nullptr;
     const int* c = COMPACT ? f->ccnt : f->cnt;
     const unsigned* cm = COMPACT ? f->cmask : nullptr;
     if (f->ens)
-        fk_force<COMPACT, true, HALFV><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos,
-                                                                 f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
-                                                                 f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph,
-                                                                 wrap_margin(f));
+        fk_force<COMPACT, true, HALFV, NOISE><<<nb, f->block, 0, st>>>(
+            n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
+            f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph, wrap_margin(f));
     else
-        fk_force<COMPACT, false, HALFV><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos,
-                                                                  f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
-                                                                  f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph,
-                                                                  wrap_margin(f));
+        fk_force<COMPACT, false, HALFV, NOISE><<<nb, f->block, 0, st>>>(
+            n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
+            f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph, wrap_margin(f));
+}
+
+template <bool COMPACT, bool HALFV>
+void force_launch(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
+    if (p.noise_pref > 0.f) force_launch_n<COMPACT, HALFV, true>(f, st, p, drive);
+    else force_launch_n<COMPACT, HALFV, false>(f, st, p, drive);
 }
 
 int launch_force(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {

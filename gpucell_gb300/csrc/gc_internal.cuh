@@ -127,6 +127,10 @@ __device__ __forceinline__ float rsqrt_ftz(float x) {
     return y;
 }
 
+// |d|^2 with fused multiply-adds: the form the fused step's pair passes use
+// (one rounding fewer than norm2_rn; both passes of a step form it alike).
+__device__ __forceinline__ float norm2_fma(float3 d) { return fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z)); }
+
 __device__ __forceinline__ float norm2_rn(float3 d) {
     return __fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z));
 }
