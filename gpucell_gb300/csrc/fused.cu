@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(kMaxBS, GC_BUILD_MIN_BLOCKS) fk_build_list(int
 #define GC_DENS_MIN_BLOCKS 5
 #endif
 
-template <bool ENS>
+template <bool ENS, bool B1>
 __global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, GcParams p, SysInfo s0, const SysInfo* __restrict__ sys,
                                                   const int* __restrict__ sysid, const float4* __restrict__ pos,
                                                   float4* __restrict__ vpred, const float4* __restrict__ vh,
@@ -397,7 +397,10 @@ __global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, 
     int c = cnt[i];
     const int* lp = nbr + sell(i, 0, cap);
     if (t == PT_FLUID || t == PT_MEMB) {
-        float sum = p.w0;
+        // the sum of W / wnorm, the particle's own share (W(0) / wnorm = 1)
+        // first; wnorm multiplies it once at the end
+        float acc = 1.f;
+        const float inv_rc4 = 4.f * p.inv_rc;
         int kc = 0;
         // The list is padded to a multiple of four entries with the sentinel
         // slot.  Entries go in groups of four: the indices of the next group
@@ -430,12 +433,14 @@ __global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, 
                     for (int u = 0; u < 4; ++u) {
                         const float3 dd = pair_diff<W>(xi, xyz(xj[u]), B);
                         const float r2 = norm2_fma(dd);
-                        const bool in = r2 < p.rc2, apart = r2 > 0.f, sdpd = fid(xj[u]) >= b2;
+                        // without Bound1 walls in any system (B1 false) every partner is SDPD
+                        const bool in = r2 < p.rc2, apart = r2 > 0.f, sdpd = !B1 || fid(xj[u]) >= b2;
                         const float r = apart ? r2 * rsqrt_ftz(r2) : 0.f;
-                        const float w = wendland_w(r, p);
-                        sum += in && sdpd ? w : 0.f;
+                        // (1 - s)^4 (1 + 4 s), s = r / rc
+                        const float tt = fmaf(-r, p.inv_rc, 1.f), t2 = tt * tt;
+                        acc += in && sdpd ? t2 * t2 * fmaf(r, inv_rc4, 1.f) : 0.f;
                         // acting: an SDPD partner within rc, or a Bound1 wall within the repulsion range
-                        const bool act = in && apart && (sdpd || r2 < p.rep_r0sq);
+                        const bool act = in && apart && (sdpd || (B1 && r2 < p.rep_r0sq));
                         m |= (unsigned)act << (k0 - w0 + u);
                     }
                 }
@@ -450,6 +455,7 @@ __global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, 
         if (__any_sync(__activemask(), near_face(xi, S.g, wrap_margin))) run(std::true_type{});
         else run(std::false_type{});
         if (ccnt) ccnt[i] = kc;
+        const float sum = p.wnorm * acc;
         float rho = p.mass * sum;
         float c2 = (t == PT_MEMB) ? p.c2sq : p.c1sq;
         float inv_d = __frcp_rn(sum);
@@ -516,7 +522,7 @@ __global__ void fk_pack_vel(int n, const float4* __restrict__ v, uint2* __restri
     out[i] = make_uint2(*reinterpret_cast<const unsigned*>(&a), *reinterpret_cast<const unsigned*>(&b));
 }
 
-template <bool COMPACT, bool ENS, bool HALFV, bool NOISE>
+template <bool COMPACT, bool ENS, bool HALFV, bool NOISE, bool B1>
 __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
     fk_force(int n, GcParams p, SysInfo s0, const SysInfo* __restrict__ sys, const int* __restrict__ sysid,
              const unsigned* __restrict__ nkey, const float4* __restrict__ pos, const float4* __restrict__ vpred,
@@ -617,7 +623,7 @@ __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
                 if (!COMPACT && (r2 >= p.rc2 || r2 <= 0.f)) continue;   // coincident pairs exert no force
                 unsigned idj = fid(xj4);
                 float inv_r = rsqrt_ftz(r2);
-                if (idj < b2) {   // Bound1: repulsion only
+                if (B1 && idj < b2) {   // Bound1: repulsion only (B1: some system has such walls)
                     if (r2 < p.rep_r0sq) {
                         float ir2 = inv_r * inv_r;
                         float q2 = p.rep_r0sq * ir2, q4 = q2 * q2, q12 = q4 * q4 * q4;
@@ -1541,12 +1547,25 @@ int launch_density(GcFused* f, cudaStream_t st, const GcParams& p, bool mark) {
     const int n = f->n, nb = gc_blocks(n, f->block);
     unsigned* cm = mark && f->compact ? f->cmask : nullptr;
     int* cc = mark && f->compact ? f->ccnt : nullptr;
-    if (f->ens)
-        fk_density<true><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vpred, f->a.vh,
-                                                   f->dp, f->nbr, f->cnt, f->cap, cm, f->mw, cc, wrap_margin(f));
-    else
-        fk_density<false><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vpred, f->a.vh,
-                                                    f->dp, f->nbr, f->cnt, f->cap, cm, f->mw, cc, wrap_margin(f));
+    if (f->ens) {
+        if (f->has_b1)
+            fk_density<true, true><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vpred,
+                                                            f->a.vh, f->dp, f->nbr, f->cnt, f->cap, cm, f->mw, cc,
+                                                            wrap_margin(f));
+        else
+            fk_density<true, false><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vpred,
+                                                             f->a.vh, f->dp, f->nbr, f->cnt, f->cap, cm, f->mw, cc,
+                                                             wrap_margin(f));
+    } else {
+        if (f->has_b1)
+            fk_density<false, true><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vpred,
+                                                             f->a.vh, f->dp, f->nbr, f->cnt, f->cap, cm, f->mw, cc,
+                                                             wrap_margin(f));
+        else
+            fk_density<false, false><<<nb, f->block, 0, st>>>(n, p, s0(f), f->dsys, f->a.sys, f->a.pos, f->a.vpred,
+                                                              f->a.vh, f->dp, f->nbr, f->cnt, f->cap, cm, f->mw, cc,
+                                                              wrap_margin(f));
+    }
     GC_CHECK_LAUNCH("fused: density");
     return GC_OK;
 }
@@ -1590,26 +1609,32 @@ int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p) {
     return GC_OK;
 }
 
-template <bool COMPACT, bool HALFV, bool NOISE>
+template <bool COMPACT, bool HALFV, bool NOISE, bool B1>
 void force_launch_n(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
     const int n = f->n, nb = gc_blocks(n, f->block);
     const float4* mf = f->ncell > 0 ? f->mforce : nullptr;
     const int* c = COMPACT ? f->ccnt : f->cnt;
     const unsigned* cm = COMPACT ? f->cmask : nullptr;
     if (f->ens)
-        fk_force<COMPACT, true, HALFV, NOISE><<<nb, f->block, 0, st>>>(
+        fk_force<COMPACT, true, HALFV, NOISE, B1><<<nb, f->block, 0, st>>>(
             n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
             f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph, wrap_margin(f));
     else
-        fk_force<COMPACT, false, HALFV, NOISE><<<nb, f->block, 0, st>>>(
+        fk_force<COMPACT, false, HALFV, NOISE, B1><<<nb, f->block, 0, st>>>(
             n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
             f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph, wrap_margin(f));
 }
 
 template <bool COMPACT, bool HALFV>
 void force_launch(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
-    if (p.noise_pref > 0.f) force_launch_n<COMPACT, HALFV, true>(f, st, p, drive);
-    else force_launch_n<COMPACT, HALFV, false>(f, st, p, drive);
+    const bool noise = p.noise_pref > 0.f;
+    if (f->has_b1) {
+        if (noise) force_launch_n<COMPACT, HALFV, true, true>(f, st, p, drive);
+        else force_launch_n<COMPACT, HALFV, false, true>(f, st, p, drive);
+    } else {
+        if (noise) force_launch_n<COMPACT, HALFV, true, false>(f, st, p, drive);
+        else force_launch_n<COMPACT, HALFV, false, false>(f, st, p, drive);
+    }
 }
 
 int launch_force(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
@@ -2327,6 +2352,8 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
         id0 += c.nTotalPar;
         m0 += c.nCellPar;
     }
+    f->has_b1 = false;
+    for (const SysInfo& S : f->hsys) f->has_b1 = f->has_b1 || S.b2 > S.id0;
     const int n = f->n;
     int ok = GC_OK;
     SlotArrays* sa[2] = {&f->a, &f->b};

@@ -197,6 +197,7 @@ struct GcFused {
     bool halfv = false;            // neighbour velocities packed to FP16 for the force pass
     uint2* vph = nullptr;          // those packed velocities (x, y, z, 0 as halves)
     bool ens = false;              // kernels read the system table
+    bool has_b1 = true;            // some system has Bound1 wall particles
     long long step = -1;           // index keying the noise of the latest step
     long long rebuilds = 0, steps = 0;
     cudaStream_t st = 0;
