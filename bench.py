@@ -301,16 +301,18 @@ TILE_PARTIAL_BYTES = {"force": 2 * 14 * 12, "density": 2 * 14 * 4}
 #       --no-configs --no-variants --steps 3 --warmup 3 --profile-steps 1 --e2e-steps 1   (plain run, exit 0),
 #   then ncu --set full --clock-control none -k regex:"fk_(force|density)" -s 6 -c 2 <the same command>
 # on the 524,288-particle suspension (warp instructions and FP32 operations
-# per particle, mean list 143.7), and
+# per particle; skin 0.125 rc, mean list 166.5), and
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none
-#       -k regex:"fk_force" -s 8 -c 2 python bench.py --no-ensemble --cpu-steps 0 --no-plain --no-engine
-#       --no-output --no-parity --no-configs --no-variants --steps 4 --warmup 3 --profile-steps 1 --e2e-steps 1
+#       -k regex:"fk_(force|density|build_list|mgather|medge|mgeo|mtri|integrate)" -s 8 -c 8 python bench.py
+#       --no-ensemble --cpu-steps 0 --no-plain --no-engine --no-output --no-parity --no-configs --no-variants
+#       --steps 4 --warmup 3 --profile-steps 1 --e2e-steps 1
 # at full size (DRAM bytes of one launch, one pass).
 FORCE_COUNTERS = {
-    "kernel_version": "fk_force: one thread per particle over its compact list of acting entries",
-    "dram_bytes_per_launch_4M": 2.854405632e9 + 0.128385792e9,
-    "warp_inst_per_particle": 346474930 / 524288,
-    "fp32_flop_per_particle": 5.224e9 / 524288,
+    "kernel_version": "fk_force<1,0,0,1,0>: one thread per particle over its compact list of acting entries, "
+                      "pair terms as three coefficient vectors, noise and wall-free forms as template switches",
+    "dram_bytes_per_launch_4M": 3.256612864e9 + 0.129022976e9,
+    "warp_inst_per_particle": 278141655 / 524288,
+    "fp32_flop_per_particle": 4.1227e9 / 524288,
 }
 # SM schedulers of a GB300 (152 SMs x 4, one warp instruction per cycle
 # each) and its FP32 lanes (152 SMs x 128, an FMA counting 2).
@@ -349,7 +351,7 @@ def rooflines(cfg, ms_per_step, force_ms, dens_ms, mean_nb, hbm, peak_kind, cloc
         "formula": f"B_alg = 352 N + 16 N_tri + 32 N_edge + 28 N_vert = 352*{n} + 16*{cfg.ntri} + 32*{cfg.nedge} "
                    f"+ 28*{cfg.ncp} = {b_alg / 1e9:.4f} GB per step; frac = B_alg / (ms_per_step) / peak",
         "note": "algorithmic bytes of the plain FP32 step per unit of work (neighbour state from cache, no lists); "
-                "the fused step is bound by instruction issue in its pair kernels (issue_roofline)",
+                "the fused step is bound by instruction issue and gather latency in its pair kernels (issue_roofline)",
     }
     f_alg = FORCE_ALG_BYTES * n
     d_alg = 20 * n
