@@ -501,6 +501,7 @@ __global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, 
 #endif
 constexpr int kForceGroup = GC_FORCE_GROUP;
 constexpr int kForceAhead = GC_FORCE_AHEAD;   // groups of list indices loaded ahead
+
 #ifndef GC_FORCE_MIN_BLOCKS
 #define GC_FORCE_MIN_BLOCKS (kForceGroup == 1 ? 6 : (kForceGroup == 2 ? 4 : 3))
 #endif
@@ -586,68 +587,72 @@ __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
     // is formed as F times the product of the two inverse number densities,
     // the same product from either side of the pair.
     const float cAB = p.sqrtAB - p.sqrtA;
-    auto run = [&](auto wrapc) {
+    // one pair: neighbour position (with its id), (1/d, P/d^2) and velocity
+    auto pair = [&](auto wrapc, float4 xj4, float2 dpj, float4 vj) {
         constexpr bool W = decltype(wrapc)::value;
-        int jq[A][G];
-#pragma unroll
-        for (int a = 0; a < A; ++a)
-#pragma unroll
-            for (int u = 0; u < G; ++u) {
-                int k = a * G + u;
-                jq[a][u] = k < c ? __ldg(lp + (size_t)next_k(k) * 32) : i;
-            }
-        for (int k0 = 0; k0 < c; k0 += G) {
-            float4 xg[G], vg[G];
-            float2 dg[G];
-#pragma unroll
-            for (int u = 0; u < G; ++u) {
-                xg[u] = pos[jq[0][u]];
-                dg[u] = dp[jq[0][u]];
-                vg[u] = HALFV ? unpack_vel(vph[jq[0][u]]) : vpred[jq[0][u]];
-            }
-#pragma unroll
-            for (int a = 0; a + 1 < A; ++a)
-#pragma unroll
-                for (int u = 0; u < G; ++u) jq[a][u] = jq[a + 1][u];
-#pragma unroll
-            for (int u = 0; u < G; ++u) {
-                int k = k0 + A * G + u;
-                jq[A - 1][u] = k < c ? __ldg(lp + (size_t)next_k(k) * 32) : i;
-            }
-#pragma unroll
-            for (int u = 0; u < G; ++u) {
-                if (k0 + u >= c) break;
-                float4 xj4 = xg[u];
-                float3 d = pair_diff<W>(xi, xyz(xj4), B);
-                float r2 = norm2_fma(d);   // as in fk_density
-                if (!COMPACT && (r2 >= p.rc2 || r2 <= 0.f)) continue;   // coincident pairs exert no force
-                unsigned idj = fid(xj4);
-                float inv_r = rsqrt_ftz(r2);
-                if (B1 && idj < b2) {   // Bound1: repulsion only (B1: some system has such walls)
-                    if (r2 < p.rep_r0sq) {
-                        float ir2 = inv_r * inv_r;
-                        float q2 = p.rep_r0sq * ir2, q4 = q2 * q2, q12 = q4 * q4 * q4;
-                        f += (p.rep_D * (q12 - q4) * ir2) * d;
-                    }
-                    continue;
-                }
-                float2 dpj = dg[u];
-                float4 vj = vg[u];
-                float F = wendland_f(r2 * inv_r, p);
+        float3 d = pair_diff<W>(xi, xyz(xj4), B);
+        float r2 = norm2_fma(d);   // as in fk_density
+        if (!COMPACT && (r2 >= p.rc2 || r2 <= 0.f)) return;   // coincident pairs exert no force
+        unsigned idj = fid(xj4);
+        float inv_r = rsqrt_ftz(r2);
+        if (B1 && idj < b2) {   // Bound1: repulsion only (B1: some system has such walls)
+            if (r2 < p.rep_r0sq) {
                 float ir2 = inv_r * inv_r;
-                float3 vij = f3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z);
-                float fdd = F * (dpi.x * dpj.x);
-                float cd = (dpi.y + dpj.y) * F - (fdd * p.visB) * dot3(d, vij) * ir2;
-                f += (-fdd * p.visA) * vij;
-                if constexpr (NOISE) {
-                    float qq = p.noise_pref * fdd;
-                    float q = qq > 0.f ? qq * rsqrt_ftz(qq) : 0.f;
-                    q = id < idj ? q : -q;   // the pair sign of xi_ij
-                    float3 xi_ = pair_noise_unsigned_k(id - id0, idj - id0, key);
-                    cd += (q * cAB) * dot3(d, xi_) * ir2;
-                    f += (q * p.sqrtA) * xi_;
+                float q2 = p.rep_r0sq * ir2, q4 = q2 * q2, q12 = q4 * q4 * q4;
+                f += (p.rep_D * (q12 - q4) * ir2) * d;
+            }
+            return;
+        }
+        float F = wendland_f(r2 * inv_r, p);
+        float ir2 = inv_r * inv_r;
+        float3 vij = f3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z);
+        float fdd = F * (dpi.x * dpj.x);
+        float cd = (dpi.y + dpj.y) * F - (fdd * p.visB) * dot3(d, vij) * ir2;
+        f += (-fdd * p.visA) * vij;
+        if constexpr (NOISE) {
+            float qq = p.noise_pref * fdd;
+            float q = qq > 0.f ? qq * rsqrt_ftz(qq) : 0.f;
+            q = id < idj ? q : -q;   // the pair sign of xi_ij
+            float3 xi_ = pair_noise_unsigned_k(id - id0, idj - id0, key);
+            cd += (q * cAB) * dot3(d, xi_) * ir2;
+            f += (q * p.sqrtA) * xi_;
+        }
+        f += cd * d;
+    };
+    auto gather_v = [&](int j) -> float4 { return HALFV ? unpack_vel(vph[j]) : vpred[j]; };
+    auto run = [&](auto wrapc) {
+        {
+            int jq[A][G];
+#pragma unroll
+            for (int a = 0; a < A; ++a)
+#pragma unroll
+                for (int u = 0; u < G; ++u) {
+                    int k = a * G + u;
+                    jq[a][u] = k < c ? __ldg(lp + (size_t)next_k(k) * 32) : i;
                 }
-                f += cd * d;
+            for (int k0 = 0; k0 < c; k0 += G) {
+                float4 xg[G], vg[G];
+                float2 dg[G];
+#pragma unroll
+                for (int u = 0; u < G; ++u) {
+                    xg[u] = pos[jq[0][u]];
+                    dg[u] = dp[jq[0][u]];
+                    vg[u] = gather_v(jq[0][u]);
+                }
+#pragma unroll
+                for (int a = 0; a + 1 < A; ++a)
+#pragma unroll
+                    for (int u = 0; u < G; ++u) jq[a][u] = jq[a + 1][u];
+#pragma unroll
+                for (int u = 0; u < G; ++u) {
+                    int k = k0 + A * G + u;
+                    jq[A - 1][u] = k < c ? __ldg(lp + (size_t)next_k(k) * 32) : i;
+                }
+#pragma unroll
+                for (int u = 0; u < G; ++u) {
+                    if (k0 + u >= c) break;
+                    pair(wrapc, xg[u], dg[u], vg[u]);
+                }
             }
         }
     };
@@ -1016,30 +1021,37 @@ __global__ void fk_msort(int ncp, const int* __restrict__ order, const float4* _
 }
 
 // Morse force on a vertex at xi (area ai) from a vertex at y (area *aj).
+// One Morse pair.  WRAP false: the vertex lies farther than the stencil's
+// reach from every periodic face, where the plain difference is the minimum
+// image.  De beta (e^2 - e) (a_i + a_j) is 2 De beta (e^2 - e) (a_i + a_j) / 2
+// exactly (the factors of two are exact).
+template <bool WRAP>
 __device__ __forceinline__ void morse_pair(const GcParams& p, const GcGrid& g, float3 xi, float ai, float4 y,
                                            const float* __restrict__ aj, float3& f) {
-    float3 d = min_image(xi, xyz(y), g);
+    const float3 d = WRAP ? min_image(xi, xyz(y), g) : f3(__fsub_rn(xi.x, y.x), __fsub_rn(xi.y, y.y), __fsub_rn(xi.z, y.z));
     float r2 = norm2_rn(d);
     if (r2 >= p.maxcut2 || r2 <= 0.f) return;
-    float r = sqrtf(r2);
+    const float inv_r = rsqrt_ftz(r2);
+    const float r = r2 * inv_r;
     float ex = __expf(p.beta * (p.r0m - r));
-    float fm = 2.f * p.De * p.beta * (ex * ex - ex) * 0.5f * (ai + *aj);
-    f += (fm / r) * d;
+    float fm = p.De * p.beta * (ex * ex - ex) * (ai + *aj);
+    f += (fm * inv_r) * d;
 }
 
 // Candidates [a, b) of the cube-ordered arrays, four loads in flight.
+template <bool WRAP>
 __device__ __forceinline__ void morse_run(const GcParams& p, const GcGrid& g, float3 xi, float ai, unsigned a,
                                           unsigned b, const float4* __restrict__ mspos,
                                           const float* __restrict__ msarea, float3& f) {
     unsigned s = a;
     for (; s + 4 <= b; s += 4) {
         float4 y0 = mspos[s], y1 = mspos[s + 1], y2 = mspos[s + 2], y3 = mspos[s + 3];
-        morse_pair(p, g, xi, ai, y0, msarea + s, f);
-        morse_pair(p, g, xi, ai, y1, msarea + s + 1, f);
-        morse_pair(p, g, xi, ai, y2, msarea + s + 2, f);
-        morse_pair(p, g, xi, ai, y3, msarea + s + 3, f);
+        morse_pair<WRAP>(p, g, xi, ai, y0, msarea + s, f);
+        morse_pair<WRAP>(p, g, xi, ai, y1, msarea + s + 1, f);
+        morse_pair<WRAP>(p, g, xi, ai, y2, msarea + s + 2, f);
+        morse_pair<WRAP>(p, g, xi, ai, y3, msarea + s + 3, f);
     }
-    for (; s < b; ++s) morse_pair(p, g, xi, ai, mspos[s], msarea + s, f);
+    for (; s < b; ++s) morse_pair<WRAP>(p, g, xi, ai, mspos[s], msarea + s, f);
 }
 
 // Morse aggregation between vertices of different cells, eight lanes per
@@ -1091,42 +1103,58 @@ __global__ void __launch_bounds__(kAggBS) fk_magg(int ncp, GcParams p, const Sys
         }
         const int cx = cube_coord(xi.x, 0, g), cy = cube_coord(xi.y, 1, g), cz = cube_coord(xi.z, 2, g);
         const int R = S.mlr, side = 2 * R + 1;
-        for (int row = k; row < side * side; row += kAggLanes) {
-            const int z = cube_step(cz, row / side - R, 2, g);
-            const int y = cube_step(cy, row % side - R, 1, g);
-            if (z < 0 || y < 0) continue;
-            for (int dx = -R; dx <= R; ++dx) {
-                int x = cube_step(cx, dx, 0, g);
-                if (x < 0) continue;
-                int c = S.mcube0 + cube_key(x, y, z, g);
-                const unsigned s0 = start[c], s1 = start[c + 1];
-                if (s0 == s1) continue;
-                if (RUNS) {
-                    if (own_hi < fid(mspos[s0]) || own_lo > fid(mspos[s1 - 1])) {
-                        morse_run(p, g, xi, ai, s0, s1, mspos, msarea, f);
-                        continue;
+        // farther than R + 1 cubes from every periodic face: no cube of the
+        // stencil wraps and every candidate is nearer than half the box
+        bool nearf = false;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if (!(g.pmask & (1 << a))) continue;
+            const float m = (float)(R + 1) / g.invw[a];
+            const float x = a == 0 ? xi.x : (a == 1 ? xi.y : xi.z);
+            nearf |= (x - g.lo[a] <= m) || (g.hi[a] - x <= m);
+        }
+        auto scan = [&](auto wrapc) {
+            constexpr bool W = decltype(wrapc)::value;
+            for (int row = k; row < side * side; row += kAggLanes) {
+                const int z = cube_step(cz, row / side - R, 2, g);
+                const int y = cube_step(cy, row % side - R, 1, g);
+                if (z < 0 || y < 0) continue;
+                for (int dx = -R; dx <= R; ++dx) {
+                    int x = cube_step(cx, dx, 0, g);
+                    if (x < 0) continue;
+                    int c = S.mcube0 + cube_key(x, y, z, g);
+                    const unsigned s0 = start[c], s1 = start[c + 1];
+                    if (s0 == s1) continue;
+                    if (RUNS) {
+                        if (own_hi < fid(mspos[s0]) || own_lo > fid(mspos[s1 - 1])) {
+                            morse_run<W>(p, g, xi, ai, s0, s1, mspos, msarea, f);
+                            continue;
+                        }
+                        unsigned lo = s0, hi = s1;
+                        while (lo < hi) {   // first candidate of the own cell
+                            unsigned mid = (lo + hi) >> 1;
+                            if (fid(mspos[mid]) < own_lo) lo = mid + 1;
+                            else hi = mid;
+                        }
+                        const unsigned a = lo;
+                        hi = s1;
+                        while (lo < hi) {   // first candidate past it
+                            unsigned mid = (lo + hi) >> 1;
+                            if (fid(mspos[mid]) <= own_hi) lo = mid + 1;
+                            else hi = mid;
+                        }
+                        morse_run<W>(p, g, xi, ai, s0, a, mspos, msarea, f);
+                        morse_run<W>(p, g, xi, ai, lo, s1, mspos, msarea, f);
+                    } else {
+                        for (unsigned s = s0; s < s1; ++s)
+                            if (celltab[order[s]] != ci) morse_pair<W>(p, g, xi, ai, mspos[s], msarea + s, f);
                     }
-                    unsigned lo = s0, hi = s1;
-                    while (lo < hi) {   // first candidate of the own cell
-                        unsigned mid = (lo + hi) >> 1;
-                        if (fid(mspos[mid]) < own_lo) lo = mid + 1;
-                        else hi = mid;
-                    }
-                    const unsigned a = lo;
-                    hi = s1;
-                    while (lo < hi) {   // first candidate past it
-                        unsigned mid = (lo + hi) >> 1;
-                        if (fid(mspos[mid]) <= own_hi) lo = mid + 1;
-                        else hi = mid;
-                    }
-                    morse_run(p, g, xi, ai, s0, a, mspos, msarea, f);
-                    morse_run(p, g, xi, ai, lo, s1, mspos, msarea, f);
-                } else {
-                    for (unsigned s = s0; s < s1; ++s)
-                        if (celltab[order[s]] != ci) morse_pair(p, g, xi, ai, mspos[s], msarea + s, f);
                 }
             }
-        }
+        };
+        // one form per warp
+        if (__any_sync(__activemask(), nearf)) scan(std::true_type{});
+        else scan(std::false_type{});
     }
     // the group's partial forces, added by a fixed tree
 #pragma unroll
