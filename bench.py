@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--no-plain", dest="plain", action="store_false", help="skip the FP32 boundary-path timing")
     ap.add_argument("--no-engine", dest="engine", action="store_false",
                     help="skip the boundary entry points with the fused engine behind them")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=10,
                     help="timed FP64 oracle steps of the CPU baseline (after one warm-up step)")
     ap.add_argument("--ref-steps-cap", type=int, default=30,

@@ -2205,38 +2205,59 @@ int apply_options(GcFused* f, const GcFusedOptions* opt) {
 namespace gcf {
 
 // Loads the ids [id_base, id_base + count) from host or device arrays.
+// Host transfers of at least kXferSplit particles go in kXferChunks pieces:
+// the copies of piece c on the library's stream overlap the conversion
+// kernel of piece c - 1 (load) or c + 1 (store) on the side stream, so the
+// copy engines are not left idle while the kernels run.
+constexpr int kXferChunks = 4;
+constexpr int kXferSplit = 1 << 20;
+
+static void load_piece(GcFused* f, cudaStream_t ks, unsigned id_base, int k0, int k1, const float* dx,
+                       const float* dv, const float* dh, const float* df, const int* dn) {
+    const int keep = f->setup_done ? 1 : 0;
+    auto at = [&](const auto* a) { return a ? a + 3 * (size_t)k0 : a; };
+    fk_load<<<gc_blocks(k1 - k0, f->block), f->block, 0, ks>>>(
+        k1 - k0, id_base + (unsigned)k0, f->dsys, f->nsys, keep, at(dx), at(dv), at(dh), at(df), at(dn), f->slot_of,
+        f->a.pos, f->a.plo, f->a.vel, f->a.vh, f->a.force, f->a.nthro, keep && f->ncell > 0 ? f->mpos : nullptr,
+        f->mplo, f->mnthro);
+}
+
 int load_range(GcFused* f, unsigned id_base, int count, const float* pos, const float* vel,
                       const float* velhalf, const float* force, const int* nthro, int from_device) {
     if (count <= 0) return GC_OK;
     cudaStream_t st = f->st;
-    const float *dx = pos, *dv = vel, *dh = velhalf, *df = force;
-    const int* dn = nthro;
-    if (!from_device) {
-        size_t b3 = (size_t)count * 12;
-        GC_TRY(stage_bytes(f, 5 * b3));
-        char* s = (char*)f->stage;
-        cudaError_t ce = cudaSuccess;
-        auto up = [&](const void* src, size_t off) -> const void* {
-            if (!src) return nullptr;
-            cudaError_t e = cudaMemcpyAsync(s + off, src, b3, cudaMemcpyHostToDevice, st);
-            if (e != cudaSuccess) ce = e;
-            return s + off;
-        };
-        dx = (const float*)up(pos, 0);
-        dv = (const float*)up(vel, b3);
-        dh = (const float*)up(velhalf, 2 * b3);
-        df = (const float*)up(force, 3 * b3);
-        dn = (const int*)up(nthro, 4 * b3);
-        GC_CUDA(ce, "fused_load: upload");
+    if (from_device) {
+        load_piece(f, st, id_base, 0, count, pos, vel, velhalf, force, nthro);
+        GC_CHECK_LAUNCH("fused: load");
+        return GC_OK;
     }
-    int keep = f->setup_done ? 1 : 0;
-    fk_load<<<gc_blocks(count, f->block), f->block, 0, st>>>(count, id_base, f->dsys, f->nsys, keep, dx, dv, dh, df,
-                                                             dn, f->slot_of, f->a.pos, f->a.plo, f->a.vel, f->a.vh,
-                                                             f->a.force, f->a.nthro,
-                                                             keep && f->ncell > 0 ? f->mpos : nullptr, f->mplo,
-                                                             f->mnthro);
-    GC_CHECK_LAUNCH("fused: load");
-    if (!from_device) GC_CUDA(cudaStreamSynchronize(st), "fused_load");   // the staging buffer is reused
+    const size_t b3 = (size_t)count * 12;
+    GC_TRY(stage_bytes(f, 5 * b3));
+    char* s = (char*)f->stage;
+    const void* src[5] = {pos, vel, velhalf, force, nthro};
+    const int nch = count >= kXferSplit ? kXferChunks : 1;
+    for (int c = 0; c < nch; ++c) {
+        const int k0 = (int)((long long)count * c / nch), k1 = (int)((long long)count * (c + 1) / nch);
+        for (int a = 0; a < 5; ++a)
+            if (src[a])
+                GC_CUDA(cudaMemcpyAsync(s + a * b3 + (size_t)k0 * 12, (const char*)src[a] + (size_t)k0 * 12,
+                                        (size_t)(k1 - k0) * 12, cudaMemcpyHostToDevice, st),
+                        "fused_load: upload");
+        cudaStream_t ks = st;
+        if (nch > 1) {   // piece c converts on the side stream once its copies are in
+            GC_CUDA(cudaEventRecord(f->xev[c], st), "fused_load");
+            GC_CUDA(cudaStreamWaitEvent(f->mst, f->xev[c], 0), "fused_load");
+            ks = f->mst;
+        }
+        auto st_of = [&](int a) { return src[a] ? (const float*)(s + a * b3) : nullptr; };
+        load_piece(f, ks, id_base, k0, k1, st_of(0), st_of(1), st_of(2), st_of(3), (const int*)st_of(4));
+        GC_CHECK_LAUNCH("fused: load");
+    }
+    if (nch > 1) {
+        GC_CUDA(cudaEventRecord(f->ev_join, f->mst), "fused_load");
+        GC_CUDA(cudaStreamWaitEvent(st, f->ev_join, 0), "fused_load");
+    }
+    GC_CUDA(cudaStreamSynchronize(st), "fused_load");   // the staging buffer is reused
     return GC_OK;
 }
 
@@ -2244,34 +2265,61 @@ int store_range(GcFused* f, unsigned id_base, int count, float* pos, float* vel,
                        float* force, float* velhalf, int* nthro, int to_device) {
     if (count <= 0) return GC_OK;
     cudaStream_t st = f->st;
-    float *x = pos, *v = vel, *r = rho, *pr = press, *fo = force, *vh = velhalf;
-    int* nt = nthro;
-    size_t b3 = (size_t)count * 12, b1 = (size_t)count * 4;
-    if (!to_device) {
-        GC_TRY(stage_bytes(f, 5 * b3 + 2 * b1));
-        char* s = (char*)f->stage;
-        x = pos ? (float*)(s) : nullptr;
-        v = vel ? (float*)(s + b3) : nullptr;
-        fo = force ? (float*)(s + 2 * b3) : nullptr;
-        vh = velhalf ? (float*)(s + 3 * b3) : nullptr;
-        nt = nthro ? (int*)(s + 4 * b3) : nullptr;
-        r = rho ? (float*)(s + 5 * b3) : nullptr;
-        pr = press ? (float*)(s + 5 * b3 + b1) : nullptr;
+    auto piece = [&](cudaStream_t ks, int k0, int k1, float* x, float* v, float* r, float* pr, float* fo, float* vh,
+                     int* nt) {
+        auto at3 = [&](auto* a) { return a ? a + 3 * (size_t)k0 : a; };
+        auto at1 = [&](float* a) { return a ? a + k0 : a; };
+        fk_store<<<gc_blocks(k1 - k0, f->block), f->block, 0, ks>>>(
+            k1 - k0, id_base + (unsigned)k0, f->p, f->slot_of, f->a.pos, f->a.vel, f->a.vh, f->a.force, f->dp,
+            f->a.nthro, at3(x), at3(v), at1(r), at1(pr), at3(fo), at3(vh), at3(nt));
+    };
+    if (to_device) {
+        piece(st, 0, count, pos, vel, rho, press, force, velhalf, nthro);
+        GC_CHECK_LAUNCH("fused: store");
+        return GC_OK;
     }
-    fk_store<<<gc_blocks(count, f->block), f->block, 0, st>>>(count, id_base, f->p, f->slot_of, f->a.pos, f->a.vel,
-                                                              f->a.vh, f->a.force, f->dp, f->a.nthro, x, v, r, pr, fo,
-                                                              vh, nt);
-    GC_CHECK_LAUNCH("fused: store");
-    if (!to_device) {
-        if (pos) GC_CUDA(cudaMemcpyAsync(pos, x, b3, cudaMemcpyDeviceToHost, st), "fused_store");
-        if (vel) GC_CUDA(cudaMemcpyAsync(vel, v, b3, cudaMemcpyDeviceToHost, st), "fused_store");
-        if (force) GC_CUDA(cudaMemcpyAsync(force, fo, b3, cudaMemcpyDeviceToHost, st), "fused_store");
-        if (velhalf) GC_CUDA(cudaMemcpyAsync(velhalf, vh, b3, cudaMemcpyDeviceToHost, st), "fused_store");
-        if (nthro) GC_CUDA(cudaMemcpyAsync(nthro, nt, b3, cudaMemcpyDeviceToHost, st), "fused_store");
-        if (rho) GC_CUDA(cudaMemcpyAsync(rho, r, b1, cudaMemcpyDeviceToHost, st), "fused_store");
-        if (press) GC_CUDA(cudaMemcpyAsync(press, pr, b1, cudaMemcpyDeviceToHost, st), "fused_store");
-        GC_CUDA(cudaStreamSynchronize(st), "fused_store");
+    const size_t b3 = (size_t)count * 12, b1 = (size_t)count * 4;
+    GC_TRY(stage_bytes(f, 5 * b3 + 2 * b1));
+    char* s = (char*)f->stage;
+    float* x = pos ? (float*)(s) : nullptr;
+    float* v = vel ? (float*)(s + b3) : nullptr;
+    float* fo = force ? (float*)(s + 2 * b3) : nullptr;
+    float* vh = velhalf ? (float*)(s + 3 * b3) : nullptr;
+    int* nt = nthro ? (int*)(s + 4 * b3) : nullptr;
+    float* r = rho ? (float*)(s + 5 * b3) : nullptr;
+    float* pr = press ? (float*)(s + 5 * b3 + b1) : nullptr;
+    const int nch = count >= kXferSplit ? kXferChunks : 1;
+    if (nch > 1) {   // the side stream starts after the work before the store
+        GC_CUDA(cudaEventRecord(f->ev_fork, st), "fused_store");
+        GC_CUDA(cudaStreamWaitEvent(f->mst, f->ev_fork, 0), "fused_store");
     }
+    for (int c = 0; c < nch; ++c) {
+        const int k0 = (int)((long long)count * c / nch), k1 = (int)((long long)count * (c + 1) / nch);
+        const size_t o3 = (size_t)k0 * 12, n3 = (size_t)(k1 - k0) * 12, o1 = (size_t)k0 * 4, n1 = (size_t)(k1 - k0) * 4;
+        if (nch > 1) {   // piece c gathers on the side stream, its copies wait for it
+            piece(f->mst, k0, k1, x, v, r, pr, fo, vh, nt);
+            GC_CHECK_LAUNCH("fused: store");
+            GC_CUDA(cudaEventRecord(f->xev[c], f->mst), "fused_store");
+            GC_CUDA(cudaStreamWaitEvent(st, f->xev[c], 0), "fused_store");
+        } else {
+            piece(st, k0, k1, x, v, r, pr, fo, vh, nt);
+            GC_CHECK_LAUNCH("fused: store");
+        }
+        auto down = [&](void* dst, const void* src, size_t off, size_t bytes) -> int {
+            if (!dst) return GC_OK;
+            GC_CUDA(cudaMemcpyAsync((char*)dst + off, (const char*)src + off, bytes, cudaMemcpyDeviceToHost, st),
+                    "fused_store");
+            return GC_OK;
+        };
+        GC_TRY(down(pos, x, o3, n3));
+        GC_TRY(down(vel, v, o3, n3));
+        GC_TRY(down(force, fo, o3, n3));
+        GC_TRY(down(velhalf, vh, o3, n3));
+        GC_TRY(down(nthro, nt, o3, n3));
+        GC_TRY(down(rho, r, o1, n1));
+        GC_TRY(down(press, pr, o1, n1));
+    }
+    GC_CUDA(cudaStreamSynchronize(st), "fused_store");
     return GC_OK;
 }
 
@@ -2422,6 +2470,9 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
                         cudaEventCreateWithFlags(&f->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
                         cudaEventCreateWithFlags(&f->ev_join, cudaEventDisableTiming) != cudaSuccess))
         ok = gc_fail(GC_ECUDA, "fused: membrane stream");
+    for (int c = 0; c < 4 && ok == GC_OK; ++c)
+        if (cudaEventCreateWithFlags(&f->xev[c], cudaEventDisableTiming) != cudaSuccess)
+            ok = gc_fail(GC_ECUDA, "fused: transfer events");
     if (ok == GC_OK) ok = build_grids(f);
     if (ok == GC_OK) {
         // list capacity: expected neighbours within rc + skin at the largest
@@ -2779,6 +2830,8 @@ int gc_fused_destroy(GcFused* f) {
     if (f->mst) cudaStreamDestroy(f->mst);
     if (f->ev_fork) cudaEventDestroy(f->ev_fork);
     if (f->ev_join) cudaEventDestroy(f->ev_join);
+    for (int c = 0; c < 4; ++c)
+        if (f->xev[c]) cudaEventDestroy(f->xev[c]);
     if (f->sortmem_agg) cudaFree(f->sortmem_agg);
     for (cudaEvent_t e : f->ev) cudaEventDestroy(e);
     for (void* q : f->allocs) cudaFree(q);

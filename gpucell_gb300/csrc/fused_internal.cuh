@@ -260,6 +260,7 @@ struct GcFused {
     // force pass, beside the rebuild check, the list rebuild and the density.
     cudaStream_t mst = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t xev[4] = {nullptr, nullptr, nullptr, nullptr};   // chunks of a host load / store
     // membranes (global indices over the ensemble)
     int ncell = 0, ntri = 0, nedge = 0, ncp = 0;
     int3* tri = nullptr;
