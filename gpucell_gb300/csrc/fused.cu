@@ -546,7 +546,9 @@ __global__ void __launch_bounds__(kMaxBS, force_min_blocks(ENS))
     const Box B = box_of(S);
     const unsigned b2 = S.b2;
     const unsigned id0 = S.id0;
-    const uint32_t key = ENS ? nkey[s] : p.noise_key;
+    // one system: the key of the step from the parameters, or, in a captured
+    // step, from the device (fk_step_begin derives it at each replay)
+    const uint32_t key = ENS ? nkey[s] : (nkey ? nkey[0] : p.noise_key);
     float4 vi = vpred[i];
     float2 dpi = dp[i];
     float3 f = f3(0.f, 0.f, 0.f);
@@ -1643,13 +1645,14 @@ void force_launch_n(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
     const float4* mf = f->ncell > 0 ? f->mforce : nullptr;
     const int* c = COMPACT ? f->ccnt : f->cnt;
     const unsigned* cm = COMPACT ? f->cmask : nullptr;
+    const unsigned* nk = f->ens || f->capturing ? f->nkey : nullptr;
     if (f->ens)
         fk_force<COMPACT, true, HALFV, NOISE, B1><<<nb, f->block, 0, st>>>(
-            n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
+            n, p, s0(f), f->dsys, f->a.sys, nk, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
             f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph, wrap_margin(f));
     else
         fk_force<COMPACT, false, HALFV, NOISE, B1><<<nb, f->block, 0, st>>>(
-            n, p, s0(f), f->dsys, f->a.sys, f->nkey, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
+            n, p, s0(f), f->dsys, f->a.sys, nk, f->a.pos, f->a.vpred, f->a.vh, f->dp, f->a.force, f->a.vel,
             f->nbr, c, f->cap, cm, f->mw, mf, drive, f->vph, wrap_margin(f));
 }
 
@@ -1781,6 +1784,7 @@ int capture_step(GcFused* f, int drive) {
     GcParams p = f->p;
     unsigned long long l0 = gc_launch_count();
     GC_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "fused: begin capture");
+    f->capturing = true;
     int rc = GC_OK;
     cudaGraph_t g = nullptr;
     cudaGraphConditionalHandle hcond = 0;
@@ -1826,6 +1830,7 @@ int capture_step(GcFused* f, int drive) {
         if ((rc = launch_force(f, st, p, drive)) != GC_OK) break;
         if ((rc = launch_wallvel(f, st, p)) != GC_OK) break;
     } while (0);
+    f->capturing = false;
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &graph);
     unsigned long long l1 = gc_launch_count();
@@ -2410,7 +2415,7 @@ int gc_ensemble_create(int nsys, const GcSystemDesc* d, int noise_on, const GcFu
     f->p.nT = (unsigned)ntot;
     f->p.nCP = (unsigned)ncp;
     f->skin = f->skin_rel * f->p.rc;
-    f->ens = nsys > 1 || f->graph;
+    f->ens = nsys > 1;
     f->hsys.resize(nsys);
     unsigned id0 = 0, m0 = 0;
     for (int s = 0; s < nsys; ++s) {
@@ -2796,7 +2801,7 @@ int gc_fused_set_options(GcFused* f, const GcFusedOptions* opt) {
     int old_block = f->block;
     GC_TRY(apply_options(f, opt));
     f->skin = f->skin_rel * f->p.rc;
-    f->ens = f->nsys > 1 || f->graph;
+    f->ens = f->nsys > 1;
     bool regrid = f->skin_rel != old_skin || f->lists != old_lists;
     if (regrid) GC_TRY(build_grids(f));
     int cap = f->cap;

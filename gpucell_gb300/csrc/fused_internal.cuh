@@ -196,7 +196,8 @@ struct GcFused {
     int ddpos = 1;                 // positions double-float (0: plain FP32, GcFusedOptions.fp32_positions)
     bool halfv = false;            // neighbour velocities packed to FP16 for the force pass
     uint2* vph = nullptr;          // those packed velocities (x, y, z, 0 as halves)
-    bool ens = false;              // kernels read the system table
+    bool ens = false;              // kernels read the system table (several systems)
+    bool capturing = false;        // a step is being captured: the noise key comes from the device
     bool has_b1 = true;            // some system has Bound1 wall particles
     long long step = -1;           // index keying the noise of the latest step
     long long rebuilds = 0, steps = 0;

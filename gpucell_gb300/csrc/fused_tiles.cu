@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(kTileBS, GC_TILE_FORCE_MIN_BLOCKS)
     const SysInfo& S = ENS ? sys[s] : s0;
     const Box B = box_of(S);
     const unsigned b2 = S.b2, fl = S.fl, id0 = S.id0;
-    const uint32_t key = ENS ? nkey[s] : p.noise_key;
+    const uint32_t key = ENS ? nkey[s] : (nkey ? nkey[0] : p.noise_key);   // as in fk_force
     const bool noise = p.noise_pref > 0.f;
     const unsigned sa = start[C], na = start[C + 1] - sa;
     if (na > (unsigned)kTileMax) return;   // the build raised GC_FLAG_TILE_FULL
@@ -675,7 +675,8 @@ template <bool ENS>
 int tile_force_launch(GcFused* f, cudaStream_t st, const GcParams& p, int drive) {
     const int K = f->K, n = f->n;
     fk_tile_force<ENS><<<(K + kTileWarps - 1) / kTileWarps, kTileBS, 0, st>>>(
-        K, p, f->hsys[0], f->dsys, f->cube_sys, f->nkey, f->sb.cnt, f->tnb, f->toff, f->tent, f->tent_chunks, f->a.pos,
+        K, p, f->hsys[0], f->dsys, f->cube_sys, f->ens || f->capturing ? f->nkey : nullptr, f->sb.cnt, f->tnb, f->toff,
+        f->tent, f->tent_chunks, f->a.pos,
         f->a.vpred, f->dp, f->pf, n, f->flags);
     GC_CHECK_LAUNCH("fused: tile force");
     const float4* mf = f->ncell > 0 ? f->mforce : nullptr;

@@ -69,3 +69,25 @@ def test_full_size_properties(cuda_device, cfg2):
     assert ea < 1e-6 and ev < 1e-6
     assert np.abs(a["Area64"] / a["Area0"] - 1).max() < 0.02
     assert np.abs(a["Vol64"] / a["Vol0"] - 1).max() < 0.02
+
+
+def test_host_load_and_store_in_pieces_round_trip(cuda_device, cfg2):
+    """Host loads and stores of a million particles or more go in four
+    pieces (copies of one piece beside the conversion kernel of the next):
+    a state loaded in place comes back bit for bit, each array in the
+    caller's order, including the pieces' edges."""
+    from gpucell_gb300.fused import FusedSystem
+    rng = np.random.default_rng(5)
+    n = cfg2.n
+    assert n >= 1 << 20   # the pieced path
+    fs = FusedSystem(cfg2, noise=False)
+    state = {"pos": cfg2.coor.astype(np.float32),
+             "vel": rng.standard_normal((n, 3)).astype(np.float32),
+             "velhalf": rng.standard_normal((n, 3)).astype(np.float32),
+             "force": rng.standard_normal((n, 3)).astype(np.float32),
+             "nthro": rng.integers(-3, 4, size=(n, 3)).astype(np.int32)}
+    fs.load(state["pos"], state["vel"], state["velhalf"], state["force"], state["nthro"])
+    got = fs.fetch()
+    fs.close()
+    for k, want in state.items():
+        assert np.array_equal(got[k], want), k
