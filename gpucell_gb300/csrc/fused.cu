@@ -1128,10 +1128,13 @@ __global__ void __launch_bounds__(kAggBS) fk_magg(int ncp, GcParams p, const Sys
                     const unsigned s0 = start[c], s1 = start[c + 1];
                     if (s0 == s1) continue;
                     if (RUNS) {
-                        if (own_hi < fid(mspos[s0]) || own_lo > fid(mspos[s1 - 1])) {
+                        const unsigned id_first = fid(mspos[s0]), id_last = fid(mspos[s1 - 1]);
+                        if (own_hi < id_first || own_lo > id_last) {
                             morse_run<W>(p, g, xi, ai, s0, s1, mspos, msarea, f);
                             continue;
                         }
+                        // ids ascend within a cube: a cube of the own cell alone has no candidate
+                        if (own_lo <= id_first && id_last <= own_hi) continue;
                         unsigned lo = s0, hi = s1;
                         while (lo < hi) {   // first candidate of the own cell
                             unsigned mid = (lo + hi) >> 1;
