@@ -1115,13 +1115,29 @@ __global__ void __launch_bounds__(kAggBS) fk_magg(int ncp, GcParams p, const Sys
             const float x = a == 0 ? xi.x : (a == 1 ? xi.y : xi.z);
             nearf |= (x - g.lo[a] <= m) || (g.hi[a] - x <= m);
         }
+        // distance from the vertex to the cube dc steps away along an axis
+        // (its offset f inside its own cube, cube width w): rows and cubes
+        // farther than MaxCut (with a margin far above the rounding) hold no
+        // partner and are not read
+        const float wx = 1.f / g.invw[0], wy = 1.f / g.invw[1], wz = 1.f / g.invw[2];
+        const float fx = xi.x - (g.origin[0] + (float)cx * wx), fy = xi.y - (g.origin[1] + (float)cy * wy),
+                    fz = xi.z - (g.origin[2] + (float)cz * wz);
+        auto gap = [](int dc, float f, float w) {
+            return fmaxf(0.f, dc > 0 ? (float)dc * w - f : (dc < 0 ? f - (float)(dc + 1) * w : 0.f));
+        };
+        const float cutm = p.maxcut + 1e-3f, cutm2 = cutm * cutm;
         auto scan = [&](auto wrapc) {
             constexpr bool W = decltype(wrapc)::value;
             for (int row = k; row < side * side; row += kAggLanes) {
-                const int z = cube_step(cz, row / side - R, 2, g);
-                const int y = cube_step(cy, row % side - R, 1, g);
+                const int dz = row / side - R, dy = row % side - R;
+                const float gz = gap(dz, fz, wz), gy = gap(dy, fy, wy), dyz = gy * gy + gz * gz;
+                if (dyz > cutm2) continue;
+                const int z = cube_step(cz, dz, 2, g);
+                const int y = cube_step(cy, dy, 1, g);
                 if (z < 0 || y < 0) continue;
                 for (int dx = -R; dx <= R; ++dx) {
+                    const float gx = gap(dx, fx, wx);
+                    if (dyz + gx * gx > cutm2) continue;
                     int x = cube_step(cx, dx, 0, g);
                     if (x < 0) continue;
                     int c = S.mcube0 + cube_key(x, y, z, g);
