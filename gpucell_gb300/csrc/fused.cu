@@ -1056,126 +1056,165 @@ __device__ __forceinline__ void morse_run(const GcParams& p, const GcGrid& g, fl
     for (; s < b; ++s) morse_pair<WRAP>(p, g, xi, ai, mspos[s], msarea + s, f);
 }
 
-// Morse aggregation between vertices of different cells, eight lanes per
-// vertex in grid order, over the (2R+1)^3 aggregation cubes around it (R = 2
-// for cubes at least MaxCut/2 wide, 1 for cubes at least MaxCut wide): lane
-// k of a vertex's group scans the rows (dy, dz) k, k + 8, ... of the stencil,
-// and the group adds its eight partial forces by a fixed xor tree.  Vertices
-// near dense membrane contacts have several times the mean number of
-// candidates; split eight ways, their scans no longer set the length of the
-// pass.  The sort is stable and membrane vertices are in id order, so
-// within a cube the candidates ascend by id.  RUNS (every cell is one
-// contiguous id range that carries its CellTab index, checked at set-up):
-// the vertex's own cell is one run of a cube's candidates, bounded by two
-// binary searches where the cube's first and last ids say it is there, and
-// the candidates on either side are scanned without a test; otherwise every
-// candidate's CellTab is compared.  Both visit the same candidates in the
-// same order.
+// Morse aggregation by Verlet lists of its own.  When the neighbour lists
+// are rebuilt, each membrane vertex lists the vertices of other cells within
+// MaxCut + skin (no particle moves more than skin/2 before the next rebuild,
+// so every pair within MaxCut until then is listed); each step evaluates
+// only the listed pairs.
+//
+// The list build (fk_mlist) runs eight lanes per vertex in aggregation-grid
+// order over the (2R+1)^3 aggregation cubes around it (R = 2 for cubes at
+// least MaxCut/2 wide, 1 for cubes at least MaxCut wide): lane k scans the
+// rows (dy, dz) k, k + 8, ... of the stencil, skipping rows and cubes
+// farther than the cut-off; a first pass counts each lane's candidates, a
+// scan places them, and a second pass writes them, so a vertex's list is
+// lane 0's candidates, then lane 1's, ... in scan order.  The sort is stable
+// and membrane vertices are in id order, so within a cube the candidates
+// ascend by id.  RUNS (every cell is one contiguous id range that carries
+// its CellTab index, checked at set-up): a cube of the own cell alone is
+// skipped from its first and last ids, and otherwise the own cell is one run
+// bounded by two binary searches; without RUNS every candidate's CellTab is
+// compared.  Both find the same candidates in the same order.
+//
+// The pass (fk_maggl) runs eight lanes per vertex in membrane order, lane k
+// taking the entries k, k + 8, ... of the vertex's list; the group adds its
+// eight partial forces by a fixed xor tree.
 #ifndef GC_AGG_BS
 #define GC_AGG_BS 128
 #endif
 constexpr int kAggBS = GC_AGG_BS;
 constexpr int kAggLanes = 8;   // lanes per vertex (a power of two dividing 32)
+// Overflow of the Morse lists inside a captured step (a word of the handle's
+// internal overflow flags, never reported as a device status)
+constexpr unsigned kMorseFull = 1u << 24;
 
-template <bool RUNS>
-__global__ void __launch_bounds__(kAggBS) fk_magg(int ncp, GcParams p, const SysInfo* __restrict__ sys,
-                                                  const int* __restrict__ msys, const int* __restrict__ order,
-                                                  const unsigned* __restrict__ start,
-                                                  const float4* __restrict__ mspos, const float* __restrict__ msarea,
-                                                  const int* __restrict__ celltab,
-                                                  const int2* __restrict__ cell_verts, float4* __restrict__ magg,
-                                                  float4* __restrict__ mforce) {
+template <bool RUNS, bool FILL>
+__global__ void __launch_bounds__(kAggBS) fk_mlist(int ncp, GcParams p, float cutl, const SysInfo* __restrict__ sys,
+                                                   const int* __restrict__ msys, const int* __restrict__ order,
+                                                   const unsigned* __restrict__ start,
+                                                   const float4* __restrict__ mspos, const int* __restrict__ celltab,
+                                                   const int2* __restrict__ cell_verts, unsigned* __restrict__ moff,
+                                                   int* __restrict__ mlist, unsigned mcap,
+                                                   unsigned* __restrict__ oflag) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = (int)(t / kAggLanes), k = (int)(t % kAggLanes);
-    const bool live = q < ncp;   // whole groups: kAggLanes divides the block
-    float3 f = f3(0.f, 0.f, 0.f);
-    int v = 0;
-    if (live) {
-        v = order[q];
-        const SysInfo& S = sys[msys ? msys[v] : 0];
-        const GcGrid& g = S.mg;
-        const float3 xi = xyz(mspos[q]);
-        const int ci = celltab[v];
-        const float ai = msarea[q];
-        unsigned own_lo = 0, own_hi = 0;   // ids of the vertex's own cell
-        if (RUNS) {
-            int2 cv = cell_verts[ci];
-            own_lo = S.cs + (unsigned)(cv.x - (int)S.m0);
-            own_hi = S.cs + (unsigned)(cv.y - (int)S.m0);
+    if (q >= ncp) return;
+    const int v = order[q];
+    const SysInfo& S = sys[msys ? msys[v] : 0];
+    const GcGrid& g = S.mg;
+    const float3 xi = xyz(mspos[q]);
+    const int ci = celltab[v];
+    unsigned own_lo = 0, own_hi = 0;   // ids of the vertex's own cell
+    if (RUNS) {
+        int2 cv = cell_verts[ci];
+        own_lo = S.cs + (unsigned)(cv.x - (int)S.m0);
+        own_hi = S.cs + (unsigned)(cv.y - (int)S.m0);
+    }
+    const size_t slot = (size_t)v * kAggLanes + k;
+    unsigned w = 0, wend = 0;   // this lane's entries (FILL)
+    bool write = true;
+    if (FILL) {
+        w = moff[slot];
+        wend = moff[slot + 1];
+        if (moff[(size_t)ncp * kAggLanes] > mcap) {   // the lists do not fit: the host grows them
+            write = false;
+            if (k == 0 && q == 0) atomicOr(oflag, kMorseFull);
         }
-        const int cx = cube_coord(xi.x, 0, g), cy = cube_coord(xi.y, 1, g), cz = cube_coord(xi.z, 2, g);
-        const int R = S.mlr, side = 2 * R + 1;
-        // farther than R + 1 cubes from every periodic face: no cube of the
-        // stencil wraps and every candidate is nearer than half the box
-        bool nearf = false;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            if (!(g.pmask & (1 << a))) continue;
-            const float m = (float)(R + 1) / g.invw[a];
-            const float x = a == 0 ? xi.x : (a == 1 ? xi.y : xi.z);
-            nearf |= (x - g.lo[a] <= m) || (g.hi[a] - x <= m);
-        }
-        // distance from the vertex to the cube dc steps away along an axis
-        // (its offset f inside its own cube, cube width w): rows and cubes
-        // farther than MaxCut (with a margin far above the rounding) hold no
-        // partner and are not read
-        const float wx = 1.f / g.invw[0], wy = 1.f / g.invw[1], wz = 1.f / g.invw[2];
-        const float fx = xi.x - (g.origin[0] + (float)cx * wx), fy = xi.y - (g.origin[1] + (float)cy * wy),
-                    fz = xi.z - (g.origin[2] + (float)cz * wz);
-        auto gap = [](int dc, float f, float w) {
-            return fmaxf(0.f, dc > 0 ? (float)dc * w - f : (dc < 0 ? f - (float)(dc + 1) * w : 0.f));
-        };
-        const float cutm = p.maxcut + 1e-3f, cutm2 = cutm * cutm;
-        auto scan = [&](auto wrapc) {
-            constexpr bool W = decltype(wrapc)::value;
-            for (int row = k; row < side * side; row += kAggLanes) {
-                const int dz = row / side - R, dy = row % side - R;
-                const float gz = gap(dz, fz, wz), gy = gap(dy, fy, wy), dyz = gy * gy + gz * gz;
-                if (dyz > cutm2) continue;
-                const int z = cube_step(cz, dz, 2, g);
-                const int y = cube_step(cy, dy, 1, g);
-                if (z < 0 || y < 0) continue;
-                for (int dx = -R; dx <= R; ++dx) {
-                    const float gx = gap(dx, fx, wx);
-                    if (dyz + gx * gx > cutm2) continue;
-                    int x = cube_step(cx, dx, 0, g);
-                    if (x < 0) continue;
-                    int c = S.mcube0 + cube_key(x, y, z, g);
-                    const unsigned s0 = start[c], s1 = start[c + 1];
-                    if (s0 == s1) continue;
-                    if (RUNS) {
-                        const unsigned id_first = fid(mspos[s0]), id_last = fid(mspos[s1 - 1]);
-                        if (own_hi < id_first || own_lo > id_last) {
-                            morse_run<W>(p, g, xi, ai, s0, s1, mspos, msarea, f);
-                            continue;
-                        }
-                        // ids ascend within a cube: a cube of the own cell alone has no candidate
-                        if (own_lo <= id_first && id_last <= own_hi) continue;
-                        unsigned lo = s0, hi = s1;
-                        while (lo < hi) {   // first candidate of the own cell
-                            unsigned mid = (lo + hi) >> 1;
-                            if (fid(mspos[mid]) < own_lo) lo = mid + 1;
-                            else hi = mid;
-                        }
-                        const unsigned a = lo;
-                        hi = s1;
-                        while (lo < hi) {   // first candidate past it
-                            unsigned mid = (lo + hi) >> 1;
-                            if (fid(mspos[mid]) <= own_hi) lo = mid + 1;
-                            else hi = mid;
-                        }
-                        morse_run<W>(p, g, xi, ai, s0, a, mspos, msarea, f);
-                        morse_run<W>(p, g, xi, ai, lo, s1, mspos, msarea, f);
-                    } else {
-                        for (unsigned s = s0; s < s1; ++s)
-                            if (celltab[order[s]] != ci) morse_pair<W>(p, g, xi, ai, mspos[s], msarea + s, f);
-                    }
-                }
+    }
+    const float cut2 = cutl * cutl;
+    unsigned cnt = 0;
+    auto take = [&](unsigned s, float3 d) {
+        const float r2 = norm2_rn(d);
+        if (r2 < cut2) {
+            if (FILL) {
+                if (write && w < wend) mlist[w] = order[s];
+                ++w;
+            } else {
+                ++cnt;
             }
-        };
-        // one form per warp
-        if (__any_sync(__activemask(), nearf)) scan(std::true_type{});
-        else scan(std::false_type{});
+        }
+    };
+    const int cx = cube_coord(xi.x, 0, g), cy = cube_coord(xi.y, 1, g), cz = cube_coord(xi.z, 2, g);
+    const int R = S.mlr, side = 2 * R + 1;
+    // distance from the vertex to the cube dc steps away along an axis (its
+    // offset f inside its own cube, cube width w): rows and cubes farther
+    // than the cut-off (with a margin far above the rounding) hold no
+    // candidate and are not read
+    const float wx = 1.f / g.invw[0], wy = 1.f / g.invw[1], wz = 1.f / g.invw[2];
+    const float fx = xi.x - (g.origin[0] + (float)cx * wx), fy = xi.y - (g.origin[1] + (float)cy * wy),
+                fz = xi.z - (g.origin[2] + (float)cz * wz);
+    auto gap = [](int dc, float f, float w) {
+        return fmaxf(0.f, dc > 0 ? (float)dc * w - f : (dc < 0 ? f - (float)(dc + 1) * w : 0.f));
+    };
+    const float cutm = cutl + 1e-3f, cutm2 = cutm * cutm;
+    for (int row = k; row < side * side; row += kAggLanes) {
+        const int dz = row / side - R, dy = row % side - R;
+        const float gz = gap(dz, fz, wz), gy = gap(dy, fy, wy), dyz = gy * gy + gz * gz;
+        if (dyz > cutm2) continue;
+        const int z = cube_step(cz, dz, 2, g);
+        const int y = cube_step(cy, dy, 1, g);
+        if (z < 0 || y < 0) continue;
+        for (int dx = -R; dx <= R; ++dx) {
+            const float gx = gap(dx, fx, wx);
+            if (dyz + gx * gx > cutm2) continue;
+            int x = cube_step(cx, dx, 0, g);
+            if (x < 0) continue;
+            int c = S.mcube0 + cube_key(x, y, z, g);
+            const unsigned s0 = start[c], s1 = start[c + 1];
+            if (s0 == s1) continue;
+            auto run = [&](unsigned a, unsigned b) {
+                for (unsigned s = a; s < b; ++s) take(s, min_image(xi, xyz(mspos[s]), g));
+            };
+            if (RUNS) {
+                const unsigned id_first = fid(mspos[s0]), id_last = fid(mspos[s1 - 1]);
+                if (own_hi < id_first || own_lo > id_last) {
+                    run(s0, s1);
+                    continue;
+                }
+                // ids ascend within a cube: a cube of the own cell alone has no candidate
+                if (own_lo <= id_first && id_last <= own_hi) continue;
+                unsigned lo = s0, hi = s1;
+                while (lo < hi) {   // first candidate of the own cell
+                    unsigned mid = (lo + hi) >> 1;
+                    if (fid(mspos[mid]) < own_lo) lo = mid + 1;
+                    else hi = mid;
+                }
+                const unsigned a = lo;
+                hi = s1;
+                while (lo < hi) {   // first candidate past it
+                    unsigned mid = (lo + hi) >> 1;
+                    if (fid(mspos[mid]) <= own_hi) lo = mid + 1;
+                    else hi = mid;
+                }
+                run(s0, a);
+                run(lo, s1);
+            } else {
+                for (unsigned s = s0; s < s1; ++s)
+                    if (celltab[order[s]] != ci) take(s, min_image(xi, xyz(mspos[s]), g));
+            }
+        }
+    }
+    if (!FILL) moff[slot] = cnt;
+}
+
+__global__ void __launch_bounds__(kAggBS) fk_maggl(int ncp, GcParams p, const SysInfo* __restrict__ sys,
+                                                   const int* __restrict__ msys, const float4* __restrict__ mpos,
+                                                   const float* __restrict__ parea, const unsigned* __restrict__ moff,
+                                                   const int* __restrict__ mlist, float4* __restrict__ magg,
+                                                   float4* __restrict__ mforce) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = (int)(t / kAggLanes), k = (int)(t % kAggLanes);
+    const bool live = v < ncp;   // whole groups: kAggLanes divides the block
+    float3 f = f3(0.f, 0.f, 0.f);
+    if (live) {
+        const GcGrid& g = sys[msys ? msys[v] : 0].mg;
+        const float3 xi = xyz(mpos[v]);
+        const float ai = parea[v];
+        const unsigned b = moff[(size_t)v * kAggLanes], e = moff[(size_t)(v + 1) * kAggLanes];
+        for (unsigned u = b + k; u < e; u += kAggLanes) {
+            const int j = mlist[u];
+            morse_pair<true>(p, g, xi, ai, mpos[j], parea + j, f);
+        }
     }
     // the group's partial forces, added by a fixed tree
 #pragma unroll
@@ -1190,6 +1229,18 @@ __global__ void __launch_bounds__(kAggBS) fk_magg(int ncp, GcParams p, const Sys
     o->x += f.x;   // one thread per vertex, after the deformation kernels
     o->y += f.y;
     o->z += f.z;
+}
+
+// Membrane positions at the latest rebuild (the reference positions of the
+// displacement check), in membrane order: a restored handle rebuilds its
+// Morse lists from them, as the run it continues built them.
+__global__ void fk_gather_mref(int ncp, const SysInfo* __restrict__ sys, const int* __restrict__ msys,
+                               const int* __restrict__ slot_of, const float4* __restrict__ refpos,
+                               float4* __restrict__ mref) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= ncp) return;
+    const SysInfo& S = sys[msys ? msys[m] : 0];
+    mref[m] = refpos[slot_of[S.cs + (unsigned)(m - (int)S.m0)]];
 }
 
 // ---------------------------------------------------------------------------
@@ -1411,6 +1462,74 @@ int ensure_agg_sort_bufs(GcFused* f) {
     return GC_OK;
 }
 
+// The Morse lists of the current membrane positions `mp` (membrane order):
+// sort the vertices into the aggregation cubes, count each lane's
+// candidates within MaxCut + skin, scan, write.  From the host (`host`) the
+// entries grow to fit, with room for the rebuilds of captured steps; inside
+// a captured step a list that does not fit raises kMorseFull in the
+// overflow flags and the host runs the steps again with room.
+int build_morse_lists(GcFused* f, cudaStream_t st, const float4* mp, bool host) {
+    if (!f->have_agg || f->ncp <= 0 || f->ncell <= 0) return GC_OK;
+    const int ncp = f->ncp;
+    const size_t nl = (size_t)ncp * kAggLanes + 1;
+    if (host && !f->moff) {
+        GC_CUDA(cudaMalloc(&f->moff, nl * sizeof(unsigned)), "fused: Morse lists");
+        GC_CUDA(cudaMalloc(&f->mscan, gc_scan_blocks((int)nl) * sizeof(unsigned)), "fused: Morse lists");
+        drop_graphs(f);
+    }
+    if (!f->moff) return gc_fail(GC_ESTATE, "fused: Morse lists not allocated");
+    fk_mkey<<<gc_blocks(ncp, f->block), f->block, 0, st>>>(ncp, f->dsys, f->msys, mp, f->mkeys, f->mvals);
+    GC_CHECK_LAUNCH("fused: aggregation keys");
+    GC_TRY(gc_counting_sort_bufs(ncp, f->Kagg, f->mkeys, f->mvals, f->sb_agg, f->flags, st));
+    fk_msort<<<gc_blocks(ncp, f->block), f->block, 0, st>>>(ncp, f->mvals, mp, f->parea, f->mspos, f->msarea);
+    GC_CHECK_LAUNCH("fused: aggregation order");
+    const float cutl = f->p.maxcut + f->skin;
+    const int nba = gc_blocks((int)((long long)ncp * kAggLanes), kAggBS);
+    GC_CUDA(cudaMemsetAsync(f->moff + (nl - 1), 0, sizeof(unsigned), st), "fused: Morse lists");
+    auto pass = [&](auto fill) -> int {
+        constexpr bool F = decltype(fill)::value;
+        if (f->agg_runs)
+            fk_mlist<true, F><<<nba, kAggBS, 0, st>>>(ncp, f->p, cutl, f->dsys, f->msys, f->mvals, f->sb_agg.cnt,
+                                                      f->mspos, f->celltab, f->cell_verts, f->moff, f->mlist,
+                                                      (unsigned)f->mcap, f->oflag);
+        else
+            fk_mlist<false, F><<<nba, kAggBS, 0, st>>>(ncp, f->p, cutl, f->dsys, f->msys, f->mvals, f->sb_agg.cnt,
+                                                       f->mspos, f->celltab, f->cell_verts, f->moff, f->mlist,
+                                                       (unsigned)f->mcap, f->oflag);
+        GC_CHECK_LAUNCH("fused: Morse lists");
+        return GC_OK;
+    };
+    GC_TRY(pass(std::false_type{}));
+    GC_TRY(gc_scan_exclusive(f->moff, (int)nl, f->mscan, st));
+    if (host) {
+        unsigned total = 0;
+        GC_CUDA(cudaMemcpyAsync(&total, f->moff + (nl - 1), sizeof(unsigned), cudaMemcpyDeviceToHost, st),
+                "fused: Morse lists");
+        GC_CUDA(cudaStreamSynchronize(st), "fused: Morse lists");
+        if ((size_t)(1.25 * total) > f->mcap || !f->mlist) {
+            // room for the lists to grow between host-side rebuilds
+            const size_t want = (size_t)(1.5 * total) + 4096;
+            if (f->mlist) cudaFree(f->mlist);
+            f->mlist = nullptr;
+            f->mcap = 0;
+            GC_CUDA(cudaMalloc(&f->mlist, want * sizeof(int)), "fused: Morse lists");
+            f->mcap = want;
+            drop_graphs(f);
+        }
+    }
+    return pass(std::true_type{});
+}
+
+// The Morse lists as the latest rebuild built them: from the reference
+// positions of the displacement check (a restore).
+int build_morse_lists_from_ref(GcFused* f, cudaStream_t st) {
+    if (!f->have_agg || f->ncp <= 0 || f->ncell <= 0) return GC_OK;
+    if (!f->mref) GC_CUDA(cudaMalloc(&f->mref, (size_t)f->ncp * sizeof(float4)), "fused: Morse lists");
+    fk_gather_mref<<<gc_blocks(f->ncp, 256), 256, 0, st>>>(f->ncp, f->dsys, f->msys, f->slot_of, f->refpos, f->mref);
+    GC_CHECK_LAUNCH("fused: reference membrane positions");
+    return build_morse_lists(f, st, f->mref, true);
+}
+
 // Per-system list grids (cubes at least rc + skin wide) and aggregation
 // grids, their global cube offsets, and the device copy of the table.
 int build_grids(GcFused* f) {
@@ -1533,6 +1652,7 @@ int rebuild_lists(GcFused* f) {
             GC_TRY(switch_to_lists(f));
             return rebuild_lists(f);
         }
+        GC_TRY(build_morse_lists(f, st, f->mpos, true));
         f->rebuilds++;
         return GC_OK;
     }
@@ -1553,6 +1673,7 @@ int rebuild_lists(GcFused* f) {
         // longest list wanted (with room) and rebuild
         GC_TRY(alloc_list(f, grown_capacity(f, 2 * f->cap)));
     }
+    GC_TRY(build_morse_lists(f, st, f->mpos, true));
     f->rebuilds++;
     return GC_OK;
 }
@@ -1639,20 +1760,10 @@ int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p) {
                                                                  f->tarea, f->mforce, f->parea);
     GC_CHECK_LAUNCH("fused: membrane forces per vertex");
     if (f->have_agg) {
-        fk_mkey<<<gc_blocks(f->ncp, f->block), f->block, 0, st>>>(f->ncp, f->dsys, f->msys, f->mpos, f->mkeys,
-                                                                  f->mvals);
-        GC_CHECK_LAUNCH("fused: aggregation keys");
-        GC_TRY(gc_counting_sort_bufs(f->ncp, f->Kagg, f->mkeys, f->mvals, f->sb_agg, f->flags, st));
-        const int nb = gc_blocks(f->ncp, f->block);
-        fk_msort<<<nb, f->block, 0, st>>>(f->ncp, f->mvals, f->mpos, f->parea, f->mspos, f->msarea);
-        GC_CHECK_LAUNCH("fused: aggregation order");
+        // the listed pairs (the lists are built with the neighbour lists)
         const int nba = gc_blocks((int)((long long)f->ncp * kAggLanes), kAggBS);
-        if (f->agg_runs)
-            fk_magg<true><<<nba, kAggBS, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mvals, f->sb_agg.cnt, f->mspos,
-                                                  f->msarea, f->celltab, f->cell_verts, f->magg, f->mforce);
-        else
-            fk_magg<false><<<nba, kAggBS, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mvals, f->sb_agg.cnt, f->mspos,
-                                                   f->msarea, f->celltab, f->cell_verts, f->magg, f->mforce);
+        fk_maggl<<<nba, kAggBS, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mpos, f->parea, f->moff, f->mlist, f->magg,
+                                         f->mforce);
         GC_CHECK_LAUNCH("fused: aggregation");
     }
     return GC_OK;
@@ -1753,10 +1864,12 @@ int one_step(GcFused* f, int drive) {
     if (f->ens) GC_TRY(launch_step_begin(f, st));
     else GC_CUDA(cudaMemsetAsync(f->rebuild, 0, sizeof(int), st), "fused: flag");
     GC_TRY(launch_integrate(f, st, p));
-    GC_TRY(fork_membranes(f, st, f->mst, p));
     GC_CUDA(cudaMemcpyAsync(&f->h->rebuild, f->rebuild, sizeof(int), cudaMemcpyDeviceToHost, st), "fused: flag");
     GC_CUDA(cudaStreamSynchronize(st), "fused: flag");
     if (f->h->rebuild) GC_TRY(rebuild_lists(f));
+    // the membrane passes beside the density pass (after a rebuild, which
+    // writes the Morse lists they read)
+    GC_TRY(fork_membranes(f, st, f->mst, p));
     prof_mark(f, st);
     GC_TRY(launch_density(f, st, p, true));
     prof_mark(f, st);
@@ -1786,13 +1899,14 @@ int launch_rebuild_body(GcFused* f, cudaStream_t st) {
     GC_CHECK_LAUNCH("fused: copy slots");
     if (!f->lists) {
         GC_TRY(wall_lists(f, st, f->a.pos, false));
-        return tiles_build(f, st, f->a.pos, false);
+        GC_TRY(tiles_build(f, st, f->a.pos, false));
+        return build_morse_lists(f, st, f->mpos, false);
     }
     float cut = f->p.rc + f->skin;
     fk_build_list<<<nb, f->block, 0, st>>>(n, f->dsys, f->a.sys, f->a.pos, f->sb.cnt, f->nbr, f->cnt, f->cap,
                                           cut * cut, f->oflag, f->need, 0);
     GC_CHECK_LAUNCH("fused: build lists");
-    return GC_OK;
+    return build_morse_lists(f, st, f->mpos, false);
 }
 
 int capture_step(GcFused* f, int drive) {
@@ -1818,7 +1932,6 @@ int capture_step(GcFused* f, int drive) {
         if (e != cudaSuccess) { rc = gc_cuda_fail(e, "fused: conditional handle"); break; }
         if ((rc = launch_step_begin(f, st)) != GC_OK) break;
         if ((rc = launch_integrate(f, st, p)) != GC_OK) break;
-        if ((rc = fork_membranes(f, st, f->gst3, p)) != GC_OK) break;
         fk_set_cond<<<1, 1, 0, st>>>(hcond, f->rebuild, f->drebuilds);
         gc_count_launch();
         if ((e = cudaGetLastError()) != cudaSuccess) { rc = gc_cuda_fail(e, "fused: set condition"); break; }
@@ -1844,6 +1957,9 @@ int capture_step(GcFused* f, int drive) {
         if (rc != GC_OK) break;
         if (e != cudaSuccess) { rc = gc_cuda_fail(e, "fused: end rebuild capture"); break; }
         body_kernels = (long long)(gc_launch_count() - lb);
+        // the membrane passes after the conditional rebuild (which writes the
+        // Morse lists they read), beside the density pass
+        if ((rc = fork_membranes(f, st, f->gst3, p)) != GC_OK) break;
         if ((rc = launch_density(f, st, p, true)) != GC_OK) break;
         if ((rc = join_membranes(f, st)) != GC_OK) break;
         if ((rc = launch_force(f, st, p, drive)) != GC_OK) break;
@@ -2002,7 +2118,7 @@ int graph_segment(GcFused* f, int nsteps, int drive) {
         long long nreb = (long long)(f->h->drebuilds - f->drebuilds_seen);
         f->drebuilds_seen = f->h->drebuilds;
         gc_add_launches(f->kernels_step * nsteps + f->kernels_rebuild * nreb);
-        if (!(f->h->oflag & (GC_FLAG_CELL_OVERFLOW | GC_FLAG_TILE_FULL))) {
+        if (!(f->h->oflag & (GC_FLAG_CELL_OVERFLOW | GC_FLAG_TILE_FULL | kMorseFull))) {
             f->step = step0 + nsteps;
             f->steps += nsteps;
             f->rebuilds += nreb;
@@ -2013,7 +2129,21 @@ int graph_segment(GcFused* f, int nsteps, int drive) {
         // per-particle lists) and run them again
         GC_TRY(restore_state(f, &f->snap));
         f->step = step0;
-        if (f->h->oflag & GC_FLAG_TILE_FULL) {
+        if (f->h->oflag & kMorseFull) {
+            // the Morse lists: room for what the failed rebuild wanted
+            unsigned need = 0;
+            GC_CUDA(cudaMemcpy(&need, f->moff + (size_t)f->ncp * kAggLanes, sizeof(unsigned), cudaMemcpyDeviceToHost),
+                    "fused: Morse lists");
+            const size_t want = (size_t)(1.5 * (need > f->mcap ? need : f->mcap)) + 4096;
+            if (f->mlist) cudaFree(f->mlist);
+            f->mlist = nullptr;
+            f->mcap = 0;
+            GC_CUDA(cudaMalloc(&f->mlist, want * sizeof(int)), "fused: Morse lists");
+            f->mcap = want;
+        }
+        if (!(f->h->oflag & (GC_FLAG_CELL_OVERFLOW | GC_FLAG_TILE_FULL))) {
+            // only the Morse lists overflowed
+        } else if (f->h->oflag & GC_FLAG_TILE_FULL) {
             GC_TRY(switch_to_lists(f));
         } else if (!f->lists) {
             unsigned need = 0;
@@ -2668,6 +2798,7 @@ int gc_fused_setup(GcFused* f) {
             p, f->dsys, f->msys, f->nedge, f->edge, f->mpos, f->mplo, f->mnthro, f->shear, f->bend, f->l0, f->lmax, f->perlen,
             f->hpow, f->hbend, f->refang, f->flags);
         GC_CHECK_LAUNCH("fused: set-up mechanics");
+        GC_TRY(build_morse_lists(f, st, f->mpos, true));
         GC_TRY(launch_membranes(f, st, p));   // membrane outputs of the loaded state
     }
     f->step = -1;
@@ -2857,6 +2988,8 @@ int gc_fused_destroy(GcFused* f) {
     for (int c = 0; c < 4; ++c)
         if (f->xev[c]) cudaEventDestroy(f->xev[c]);
     if (f->sortmem_agg) cudaFree(f->sortmem_agg);
+    for (void* q : {(void*)f->moff, (void*)f->mscan, (void*)f->mlist, (void*)f->mref})
+        if (q) cudaFree(q);
     for (cudaEvent_t e : f->ev) cudaEventDestroy(e);
     for (void* q : f->allocs) cudaFree(q);
     if (f->nbr) cudaFree(f->nbr);

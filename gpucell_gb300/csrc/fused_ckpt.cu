@@ -119,7 +119,7 @@ int rebuild_from_ref(GcFused* f) {
         if (f->h->oflag & GC_FLAG_TILE_FULL)
             return gc_fail(GC_EDEVICE, "restore: a cube holds more particles than the pair tiles take; restore into "
                                        "a handle with per-particle lists (GcFusedOptions.tiles = 0)");
-        return GC_OK;
+        return build_morse_lists_from_ref(f, st);
     }
     float cut = f->p.rc + f->skin;
     for (int attempt = 0; attempt < 4; ++attempt) {
@@ -131,7 +131,7 @@ int rebuild_from_ref(GcFused* f) {
         GC_CUDA(cudaMemcpyAsync(&f->h->oflag, f->oflag, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "restore");
         GC_CUDA(cudaMemcpyAsync(&f->h->need, f->need, sizeof(int), cudaMemcpyDeviceToHost, st), "restore");
         GC_CUDA(cudaStreamSynchronize(st), "restore");
-        if (!(f->h->oflag & GC_FLAG_CELL_OVERFLOW)) return GC_OK;
+        if (!(f->h->oflag & GC_FLAG_CELL_OVERFLOW)) return build_morse_lists_from_ref(f, st);
         GC_TRY(alloc_list(f, grown_capacity(f, 2 * f->cap)));
     }
     return gc_fail(GC_EDEVICE, "restore: neighbour lists overflow %d entries", f->cap);

@@ -255,6 +255,14 @@ struct GcFused {
     GcSortBufs sb{};
     void* sortmem_agg = nullptr;   // the aggregation sort's own temporaries: it runs beside the list rebuild
     int sort_agg_n = 0, sort_agg_K = 0;
+    // Morse Verlet lists: per vertex and lane the offset of its entries
+    // (ncp x 8 + 1, scanned), the scan's block sums, the entries (membrane
+    // indices) and their capacity, and the membrane positions of a restore
+    unsigned* moff = nullptr;
+    unsigned* mscan = nullptr;
+    int* mlist = nullptr;
+    size_t mcap = 0;
+    float4* mref = nullptr;
     GcSortBufs sb_agg{};
     // The membrane kernels depend only on the integrated membrane positions:
     // they run on their own stream from the end of the integration to the
@@ -340,6 +348,8 @@ int build_grids(GcFused* f);
 int sync_dstep(GcFused* f);
 int rebuild_lists(GcFused* f);
 int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p);
+int build_morse_lists(GcFused* f, cudaStream_t st, const float4* mp, bool host);
+int build_morse_lists_from_ref(GcFused* f, cudaStream_t st);
 int one_step(GcFused* f, int drive);
 int prepare_graph(GcFused* f, int drive);
 int save_state(GcFused* f, StateCopy* c);
