@@ -151,6 +151,7 @@ _SIGS = {
     "gc_fused_step": [_P, _I, _I],
     "gc_fused_store": [_P] * 8 + [_I],
     "gc_fused_store_cells": [_P] * 8 + [_I],
+    "gc_fused_step_store": [_P, _I] + [_P] * 14,
     "gc_fused_cell_sums": [_P, _P, _P],
     "gc_fused_stats": [_P] * 6,
     "gc_fused_flags": [_P, _P],

@@ -1855,6 +1855,8 @@ int join_membranes(GcFused* f, cudaStream_t st) {
     return GC_OK;
 }
 
+int early_store(GcFused* f, cudaStream_t st, int phase);
+
 // One step on the host-driven path: the host reads the rebuild flag.
 int one_step(GcFused* f, int drive) {
     cudaStream_t st = f->st;
@@ -1870,14 +1872,18 @@ int one_step(GcFused* f, int drive) {
     // the membrane passes beside the density pass (after a rebuild, which
     // writes the Morse lists they read)
     GC_TRY(fork_membranes(f, st, f->mst, p));
+    if (f->es) GC_TRY(early_store(f, st, 0));
     prof_mark(f, st);
     GC_TRY(launch_density(f, st, p, true));
+    if (f->es) GC_TRY(early_store(f, st, 1));
     prof_mark(f, st);
     GC_TRY(join_membranes(f, st));
+    if (f->es) GC_TRY(early_store(f, st, 2));
     prof_mark(f, st);
     GC_TRY(launch_force(f, st, p, drive));
     prof_mark(f, st);
     GC_TRY(launch_wallvel(f, st, p));
+    if (f->es) GC_TRY(early_store(f, st, 3));
     f->steps++;
     return GC_OK;
 }
@@ -2479,16 +2485,20 @@ int store_range(GcFused* f, unsigned id_base, int count, float* pos, float* vel,
 
 // Membrane outputs of cells [c0, c0 + nc), vertices [m0, m0 + nv),
 // triangles [t0, t0 + nt).
-int store_cells_range(GcFused* f, int c0, int nc, int m0, int nv, int t0, int nt, float* area, float* vol,
-                             float* defforce, float* aggforce, float* trinordir, float* tricenter, float* pararea,
-                             int to_device) {
+size_t cells_stage_bytes(size_t snc, size_t snv, size_t snt) {
+    return 4 * (2 * snc + 3 * snv + 3 * snv + 3 * snt + 3 * snt + snv) + 64;
+}
+
+// The membrane outputs through the staging area `stage` on stream `st`;
+// `sync`: wait for the copies.
+int store_cells_on(GcFused* f, cudaStream_t st, char* stage, bool sync, int c0, int nc, int m0, int nv, int t0,
+                   int nt, float* area, float* vol, float* defforce, float* aggforce, float* trinordir,
+                   float* tricenter, float* pararea, int to_device) {
     if (f->ncell <= 0 || nc <= 0) return GC_OK;
-    cudaStream_t st = f->st;
     float *a = area, *vo = vol, *df = defforce, *ag = aggforce, *tn = trinordir, *tc = tricenter, *pa = pararea;
     size_t snc = nc, snv = nv, snt = nt;
     if (!to_device) {
-        GC_TRY(stage_bytes(f, 4 * (2 * snc + 3 * snv + 3 * snv + 3 * snt + 3 * snt + snv) + 64));
-        char* s = (char*)f->stage;
+        char* s = stage;
         size_t off = 0;
         auto take = [&](size_t cnt) { float* q = (float*)(s + off); off += 4 * cnt; return q; };
         a = take(snc); vo = take(snc); df = take(3 * snv); ag = take(3 * snv); tn = take(3 * snt); tc = take(3 * snt);
@@ -2508,9 +2518,79 @@ int store_cells_range(GcFused* f, int c0, int nc, int m0, int nv, int t0, int nt
         if (trinordir) GC_CUDA(cudaMemcpyAsync(trinordir, tn, 12 * snt, cudaMemcpyDeviceToHost, st), "store cells");
         if (tricenter) GC_CUDA(cudaMemcpyAsync(tricenter, tc, 12 * snt, cudaMemcpyDeviceToHost, st), "store cells");
         if (pararea) GC_CUDA(cudaMemcpyAsync(pararea, pa, 4 * snv, cudaMemcpyDeviceToHost, st), "store cells");
-        GC_CUDA(cudaStreamSynchronize(st), "store cells");
+        if (sync) GC_CUDA(cudaStreamSynchronize(st), "store cells");
     }
     return GC_OK;
+}
+
+int store_cells_range(GcFused* f, int c0, int nc, int m0, int nv, int t0, int nt, float* area, float* vol,
+                             float* defforce, float* aggforce, float* trinordir, float* tricenter, float* pararea,
+                             int to_device) {
+    if (f->ncell <= 0 || nc <= 0) return GC_OK;
+    if (!to_device) GC_TRY(stage_bytes(f, cells_stage_bytes(nc, nv, nt)));
+    return store_cells_on(f, f->st, (char*)f->stage, true, c0, nc, m0, nv, t0, nt, area, vol, defforce, aggforce,
+                          trinordir, tricenter, pararea, to_device);
+}
+
+// The particle outputs of every slot gathered into the staging area `s`
+// (one region per array, as store_range lays them out) and copied to host
+// memory on stream `ks`, without waiting (NULL outputs are skipped).
+size_t particle_stage_bytes(size_t n) { return 5 * n * 12 + 2 * n * 4; }
+
+int store_particles_on(GcFused* f, cudaStream_t ks, char* s, float* pos, float* vel, float* rho, float* press,
+                       float* force, float* velhalf, int* nthro) {
+    if (!(pos || vel || rho || press || force || velhalf || nthro)) return GC_OK;
+    const size_t n = f->n, b3 = n * 12, b1 = n * 4;
+    float* x = pos ? (float*)(s) : nullptr;
+    float* v = vel ? (float*)(s + b3) : nullptr;
+    float* fo = force ? (float*)(s + 2 * b3) : nullptr;
+    float* vh = velhalf ? (float*)(s + 3 * b3) : nullptr;
+    int* nt = nthro ? (int*)(s + 4 * b3) : nullptr;
+    float* r = rho ? (float*)(s + 5 * b3) : nullptr;
+    float* pr = press ? (float*)(s + 5 * b3 + b1) : nullptr;
+    fk_store<<<gc_blocks(f->n, f->block), f->block, 0, ks>>>(f->n, 0u, f->p, f->slot_of, f->a.pos, f->a.vel, f->a.vh,
+                                                             f->a.force, f->dp, f->a.nthro, x, v, r, pr, fo, vh, nt);
+    GC_CHECK_LAUNCH("fused: store");
+    auto down = [&](void* dst, const void* src, size_t bytes) -> int {
+        if (!dst) return GC_OK;
+        GC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ks), "fused_step_store");
+        return GC_OK;
+    };
+    GC_TRY(down(pos, x, b3));
+    GC_TRY(down(vel, v, b3));
+    GC_TRY(down(force, fo, b3));
+    GC_TRY(down(velhalf, vh, b3));
+    GC_TRY(down(nthro, nt, b3));
+    GC_TRY(down(rho, r, b1));
+    GC_TRY(down(press, pr, b1));
+    return GC_OK;
+}
+
+// gc_fused_step_store's copies at the points of the step where their data
+// are final: 0 after the integration and any rebuild (positions, VelHalf,
+// crossing counts), 1 after the density pass (density, pressure), 2 after
+// the membrane passes (membrane outputs) -- these on the copy stream,
+// beside the rest of the step -- and 3 at the end (velocities, forces),
+// after which the step's stream waits for the copy stream.
+int early_store(GcFused* f, cudaStream_t st, int phase) {
+    const EarlyStore& e = *f->es;
+    char* s = (char*)f->stage;
+    if (phase < 3) {
+        GC_CUDA(cudaEventRecord(f->xe[phase], st), "fused_step_store");
+        GC_CUDA(cudaStreamWaitEvent(f->xst, f->xe[phase], 0), "fused_step_store");
+    }
+    switch (phase) {
+    case 0: return store_particles_on(f, f->xst, s, e.pos, nullptr, nullptr, nullptr, nullptr, e.velhalf, e.nthro);
+    case 1: return store_particles_on(f, f->xst, s, nullptr, nullptr, e.rho, e.press, nullptr, nullptr, nullptr);
+    case 2:
+        return store_cells_on(f, f->xst, s + particle_stage_bytes(f->n), false, 0, f->ncell, 0, f->ncp, 0, f->ntri,
+                              e.area, e.vol, e.defforce, e.aggforce, e.trinordir, e.tricenter, e.pararea, 0);
+    default:
+        GC_TRY(store_particles_on(f, st, s, nullptr, e.vel, nullptr, nullptr, e.force, nullptr, nullptr));
+        GC_CUDA(cudaEventRecord(f->xe[3], f->xst), "fused_step_store");
+        GC_CUDA(cudaStreamWaitEvent(st, f->xe[3], 0), "fused_step_store");
+        return GC_OK;
+    }
 }
 
 int cell_sums_range(GcFused* f, int c0, int nc, double* area, double* vol) {
@@ -2842,6 +2922,31 @@ int gc_fused_store_cells(GcFused* f, float* area, float* vol, float* defforce, f
                              tricenter, pararea, to_device);
 }
 
+int gc_fused_step_store(GcFused* f, int drive_on, float* pos, float* vel, float* rho, float* press, float* force,
+                        float* velhalf, int* nthro, float* area, float* vol, float* defforce, float* aggforce,
+                        float* trinordir, float* tricenter, float* pararea) {
+    if (!f || !f->setup_done) return gc_fail(GC_ESTATE, "fused_step_store: call gc_fused_setup first");
+    if (f->graph && !f->profile) {   // captured steps: the step, then the stores
+        GC_TRY(gc_fused_step(f, 1, drive_on));
+        GC_TRY(store_range(f, 0, f->n, pos, vel, rho, press, force, velhalf, nthro, 0));
+        return store_cells_range(f, 0, f->ncell, 0, f->ncp, 0, f->ntri, area, vol, defforce, aggforce, trinordir,
+                                 tricenter, pararea, 0);
+    }
+    GC_TRY(stage_bytes(f, particle_stage_bytes(f->n) + cells_stage_bytes(f->ncell, f->ncp, f->ntri)));
+    if (!f->xst) GC_CUDA(cudaStreamCreateWithFlags(&f->xst, cudaStreamNonBlocking), "fused_step_store: stream");
+    for (int k = 0; k < 4; ++k)
+        if (!f->xe[k]) GC_CUDA(cudaEventCreateWithFlags(&f->xe[k], cudaEventDisableTiming), "fused_step_store: event");
+    EarlyStore e{pos, vel, rho, press, force, velhalf, nthro, area, vol, defforce, aggforce, trinordir, tricenter,
+                 pararea};
+    f->es = &e;
+    const int rc = one_step(f, drive_on ? 1 : 0);
+    f->es = nullptr;
+    cudaStreamSynchronize(f->xst);
+    GC_TRY(rc);
+    GC_CUDA(cudaStreamSynchronize(f->st), "fused_step_store");
+    return GC_OK;
+}
+
 int gc_ensemble_store_cells(GcFused* f, int sys, float* area, float* vol, float* defforce, float* aggforce,
                             float* trinordir, float* tricenter, float* pararea, int to_device) {
     GC_TRY(check_sys(f, sys, "store_cells"));
@@ -2990,6 +3095,10 @@ int gc_fused_destroy(GcFused* f) {
     if (f->sortmem_agg) cudaFree(f->sortmem_agg);
     for (void* q : {(void*)f->moff, (void*)f->mscan, (void*)f->mlist, (void*)f->mref})
         if (q) cudaFree(q);
+    if (f->xst) cudaStreamSynchronize(f->xst);
+    for (int k = 0; k < 4; ++k)
+        if (f->xe[k]) cudaEventDestroy(f->xe[k]);
+    if (f->xst) cudaStreamDestroy(f->xst);
     for (cudaEvent_t e : f->ev) cudaEventDestroy(e);
     for (void* q : f->allocs) cudaFree(q);
     if (f->nbr) cudaFree(f->nbr);

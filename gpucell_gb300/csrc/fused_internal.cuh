@@ -177,6 +177,15 @@ struct StateCopy {
 
 }  // namespace gcf
 
+namespace gcf {
+// Host outputs of gc_fused_step_store, copied while the step still runs.
+struct EarlyStore {
+    float *pos, *vel, *rho, *press, *force, *velhalf;
+    int* nthro;
+    float *area, *vol, *defforce, *aggforce, *trinordir, *tricenter, *pararea;
+};
+}  // namespace gcf
+
 struct GcFused {
     GcParams p;
     int nsys = 1;
@@ -270,6 +279,9 @@ struct GcFused {
     cudaStream_t mst = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t xev[4] = {nullptr, nullptr, nullptr, nullptr};   // chunks of a host load / store
+    const gcf::EarlyStore* es = nullptr;   // set during gc_fused_step_store
+    cudaStream_t xst = nullptr;            // its copy stream
+    cudaEvent_t xe[4] = {nullptr, nullptr, nullptr, nullptr};
     // membranes (global indices over the ensemble)
     int ncell = 0, ntri = 0, nedge = 0, ncp = 0;
     int3* tri = nullptr;

@@ -185,6 +185,19 @@ class FusedSystem(_Handle):
     def setup(self):
         _lib.call("gc_fused_setup", self.h)
 
+    def step_fetch(self, drive_on=1) -> dict:
+        """One step and its outputs (gc_fused_step_store: what is final early
+        in the step is copied while the step still runs); the keys of
+        `fetch` but the FP64 cell sums."""
+        out = _particle_out(self.cfg.n)
+        c = self.cfg
+        cells = _cell_out(c) if c.ncell else {k: None for k in _CELL_KEYS}
+        _lib.call("gc_fused_step_store", self.h, int(drive_on), *[_ptr(out[k]) for k in _PARTICLE_KEYS],
+                  *[_ptr(cells[k]) for k in _CELL_KEYS])
+        if c.ncell:
+            out.update(cells)
+        return out
+
     def fetch(self) -> dict:
         out = _particle_out(self.cfg.n)
         _lib.call("gc_fused_store", self.h, *[_ptr(out[k]) for k in _PARTICLE_KEYS], 0)

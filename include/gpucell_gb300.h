@@ -232,6 +232,18 @@ int gc_fused_store(GcFused* f, float* pos, float* vel, float* rho, float* press,
 /* Membrane outputs of the latest step, in the reference's orders. */
 int gc_fused_store_cells(GcFused* f, float* area, float* vol, float* defforce, float* aggforce, float* trinordir,
                          float* tricenter, float* pararea, int to_device);
+/* One timestep with its outputs in host memory: the same results as
+ * gc_fused_step(f, 1, drive_on) followed by gc_fused_store(..., 0) and
+ * gc_fused_store_cells(..., 0) (NULL pointers are skipped).  What is final
+ * early in the step is copied while the step still runs: positions, VelHalf
+ * and crossing counts after the integration, density and pressure after the
+ * density pass, the membrane outputs after the membrane passes; velocities
+ * and forces at the end.  Host pointers (pinned memory lets the copies run
+ * beside the kernels); returns when every copy is done.  In captured steps
+ * (GcFusedOptions.graph) the step runs first and the stores after it. */
+int gc_fused_step_store(GcFused* f, int drive_on, float* pos, float* vel, float* rho, float* press, float* force,
+                        float* velhalf, int* nthro, float* area, float* vol, float* defforce, float* aggforce,
+                        float* trinordir, float* tricenter, float* pararea);
 /* Per-cell area and volume as summed (FP64), host pointers. */
 int gc_fused_cell_sums(GcFused* f, double* area, double* vol);
 /* List rebuilds, steps taken, list capacity, mean and max list length. */

@@ -286,3 +286,29 @@ def test_device_buffers_load_and_store_like_host_ones(cuda_device):
         assert np.array_equal(got[k], want[k]), k
     fs.close()
     ref.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_step_store_matches_step_then_store(cuda_device, graph):
+    """gc_fused_step_store (the outputs that are final early in the step
+    copied beside the rest of it) returns exactly what a step followed by
+    gc_fused_store and gc_fused_store_cells returns, across list rebuilds:
+    a walled channel with a cell, and a Couette rouleau with Morse
+    aggregation."""
+    from gpucell_gb300.fused import FusedSystem
+    phys = gen.Physics(sur_energy=5.0, max_cut=1.2, zero_len=0.3, sca_fac=4.0)
+    cfgs = [gen.small_channel(),
+            gen.couette(nx=36, ny=18, nz=24, ncells=2, subdiv=2, cell_diameter=3.0, shear_rate=0.5, seed=31,
+                        phys=phys)]
+    for cfg in cfgs:
+        a = FusedSystem(cfg, noise=True, skin=0.03, graph=graph)
+        b = FusedSystem(cfg, noise=True, skin=0.03, graph=graph)
+        for _ in range(12):
+            got = a.step_fetch(1)
+            b.step(1, 1)
+            want = b.fetch()
+            for k, v in got.items():
+                assert np.array_equal(v, want[k]), k
+        assert a.stats()["rebuilds"] >= 2 and a.flags() == 0
+        a.close()
+        b.close()
