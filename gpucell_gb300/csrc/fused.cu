@@ -1200,11 +1200,14 @@ __global__ void __launch_bounds__(kAggBS) fk_mlist(int ncp, GcParams p, float cu
 __global__ void __launch_bounds__(kAggBS) fk_maggl(int ncp, GcParams p, const SysInfo* __restrict__ sys,
                                                    const int* __restrict__ msys, const float4* __restrict__ mpos,
                                                    const float* __restrict__ parea, const unsigned* __restrict__ moff,
-                                                   const int* __restrict__ mlist, float4* __restrict__ magg,
-                                                   float4* __restrict__ mforce) {
+                                                   const int* __restrict__ mlist, unsigned mcap,
+                                                   float4* __restrict__ magg, float4* __restrict__ mforce) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int v = (int)(t / kAggLanes), k = (int)(t % kAggLanes);
-    const bool live = v < ncp;   // whole groups: kAggLanes divides the block
+    // whole groups: kAggLanes divides the block.  Lists that did not fit
+    // (raised as kMorseFull; the host runs the steps again with room) are
+    // not read.
+    const bool live = v < ncp && moff[(size_t)ncp * kAggLanes] <= mcap;
     float3 f = f3(0.f, 0.f, 0.f);
     if (live) {
         const GcGrid& g = sys[msys ? msys[v] : 0].mg;
@@ -1506,9 +1509,9 @@ int build_morse_lists(GcFused* f, cudaStream_t st, const float4* mp, bool host) 
         GC_CUDA(cudaMemcpyAsync(&total, f->moff + (nl - 1), sizeof(unsigned), cudaMemcpyDeviceToHost, st),
                 "fused: Morse lists");
         GC_CUDA(cudaStreamSynchronize(st), "fused: Morse lists");
-        if ((size_t)(1.25 * total) > f->mcap || !f->mlist) {
-            // room for the lists to grow between host-side rebuilds
-            const size_t want = (size_t)(1.5 * total) + 4096;
+        if ((size_t)(f->mroom * total) + f->mextra > f->mcap || !f->mlist) {
+            // room for the lists to grow in the rebuilds of captured steps
+            const size_t want = (size_t)((f->mroom + f->mslack) * total) + f->mextra;
             if (f->mlist) cudaFree(f->mlist);
             f->mlist = nullptr;
             f->mcap = 0;
@@ -1762,8 +1765,8 @@ int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p) {
     if (f->have_agg) {
         // the listed pairs (the lists are built with the neighbour lists)
         const int nba = gc_blocks((int)((long long)f->ncp * kAggLanes), kAggBS);
-        fk_maggl<<<nba, kAggBS, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mpos, f->parea, f->moff, f->mlist, f->magg,
-                                         f->mforce);
+        fk_maggl<<<nba, kAggBS, 0, st>>>(f->ncp, p, f->dsys, f->msys, f->mpos, f->parea, f->moff, f->mlist,
+                                         (unsigned)f->mcap, f->magg, f->mforce);
         GC_CHECK_LAUNCH("fused: aggregation");
     }
     return GC_OK;
@@ -2196,6 +2199,16 @@ int alloc_cells(GcFused* f, int ncell, int ntri, int nedge, int ncp) {
     GC_TRY(falloc(f, &f->inc, 4 * (size_t)nedge + 3 * (size_t)ntri));
     GC_CUDA(cudaMemsetAsync(f->magg, 0, (size_t)ncp * sizeof(float4), f->st), "fused: magg");
     f->have_agg = f->p.De != 0.f && f->p.maxcut > 0.f;
+    // GPUCELL_MORSE_ROOM (tests): the Morse lists' room beyond the latest
+    // build as a factor, with no extra entries (1 fills them exactly)
+    if (const char* e = getenv("GPUCELL_MORSE_ROOM")) {
+        const double r = atof(e);
+        if (r >= 1.0) {
+            f->mroom = r;
+            f->mslack = 0.0;
+            f->mextra = 0;
+        }
+    }
     return GC_OK;
 }
 

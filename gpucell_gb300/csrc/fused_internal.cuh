@@ -271,6 +271,9 @@ struct GcFused {
     unsigned* mscan = nullptr;
     int* mlist = nullptr;
     size_t mcap = 0;
+    double mroom = 1.25;           // Morse entries kept free beyond the latest build (factor)
+    double mslack = 0.25;          // more when the entries are reallocated
+    size_t mextra = 4096;          // and in addition
     float4* mref = nullptr;
     GcSortBufs sb_agg{};
     // The membrane kernels depend only on the integrated membrane positions:

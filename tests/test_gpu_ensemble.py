@@ -116,15 +116,23 @@ def test_captured_steps_follow_host_steps(cuda_device, ensemble):
     assert capt.flags() == 0
 
 
-def test_captured_steps_with_aggregation_follow_host_steps(cuda_device):
-    """The Morse aggregation pass (its own sort, the cube-ordered copies and
-    the per-cube search) inside captured steps: a two-cell rouleau in Couette
-    flow follows the host-driven steps, aggregation forces included."""
+@pytest.mark.parametrize("room", ["default", "exact"])
+def test_captured_steps_with_aggregation_follow_host_steps(cuda_device, monkeypatch, room):
+    """The Morse aggregation inside captured steps (its lists rebuilt in the
+    captured rebuilds, the listed pairs each step): a two-cell rouleau in
+    Couette flow follows the host-driven steps, aggregation forces included.
+    With the Morse lists allocated to fit exactly ("exact",
+    GPUCELL_MORSE_ROOM=1), a captured rebuild whose lists grow overflows
+    them; the host runs those steps again with room, and the results are
+    the same."""
     from gpucell_gb300.fused import FusedSystem
+    if room == "exact":
+        monkeypatch.setenv("GPUCELL_MORSE_ROOM", "1")
     cfg = gen.couette(nx=36, ny=18, nz=24, ncells=2, subdiv=2, cell_diameter=3.0, shear_rate=0.5, seed=31)
     host, capt = FusedSystem(cfg, graph=False), FusedSystem(cfg, graph=True)
-    host.set_options(skin=0.12)
-    capt.set_options(skin=0.12)
+    skin = 0.12 if room == "default" else 0.02
+    host.set_options(skin=skin)
+    capt.set_options(skin=skin)
     for _ in range(3):
         host.step(10, 1)
         capt.step(10, 1)
