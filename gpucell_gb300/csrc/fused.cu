@@ -1875,18 +1875,18 @@ int one_step(GcFused* f, int drive) {
     // the membrane passes beside the density pass (after a rebuild, which
     // writes the Morse lists they read)
     GC_TRY(fork_membranes(f, st, f->mst, p));
-    if (f->es) GC_TRY(early_store(f, st, 0));
+    if (f->early) GC_TRY(f->early(f, st, 0));
     prof_mark(f, st);
     GC_TRY(launch_density(f, st, p, true));
-    if (f->es) GC_TRY(early_store(f, st, 1));
+    if (f->early) GC_TRY(f->early(f, st, 1));
     prof_mark(f, st);
     GC_TRY(join_membranes(f, st));
-    if (f->es) GC_TRY(early_store(f, st, 2));
+    if (f->early) GC_TRY(f->early(f, st, 2));
     prof_mark(f, st);
     GC_TRY(launch_force(f, st, p, drive));
     prof_mark(f, st);
     GC_TRY(launch_wallvel(f, st, p));
-    if (f->es) GC_TRY(early_store(f, st, 3));
+    if (f->early) GC_TRY(f->early(f, st, 3));
     f->steps++;
     return GC_OK;
 }
@@ -2585,6 +2585,13 @@ int store_particles_on(GcFused* f, cudaStream_t ks, char* s, float* pos, float* 
 // the membrane passes (membrane outputs) -- these on the copy stream,
 // beside the rest of the step -- and 3 at the end (velocities, forces),
 // after which the step's stream waits for the copy stream.
+int ensure_early_stream(GcFused* f) {
+    if (!f->xst) GC_CUDA(cudaStreamCreateWithFlags(&f->xst, cudaStreamNonBlocking), "fused: write stream");
+    for (int k = 0; k < 4; ++k)
+        if (!f->xe[k]) GC_CUDA(cudaEventCreateWithFlags(&f->xe[k], cudaEventDisableTiming), "fused: write events");
+    return GC_OK;
+}
+
 int early_store(GcFused* f, cudaStream_t st, int phase) {
     const EarlyStore& e = *f->es;
     char* s = (char*)f->stage;
@@ -2946,13 +2953,13 @@ int gc_fused_step_store(GcFused* f, int drive_on, float* pos, float* vel, float*
                                  tricenter, pararea, 0);
     }
     GC_TRY(stage_bytes(f, particle_stage_bytes(f->n) + cells_stage_bytes(f->ncell, f->ncp, f->ntri)));
-    if (!f->xst) GC_CUDA(cudaStreamCreateWithFlags(&f->xst, cudaStreamNonBlocking), "fused_step_store: stream");
-    for (int k = 0; k < 4; ++k)
-        if (!f->xe[k]) GC_CUDA(cudaEventCreateWithFlags(&f->xe[k], cudaEventDisableTiming), "fused_step_store: event");
+    GC_TRY(ensure_early_stream(f));
     EarlyStore e{pos, vel, rho, press, force, velhalf, nthro, area, vol, defforce, aggforce, trinordir, tricenter,
                  pararea};
     f->es = &e;
+    f->early = early_store;
     const int rc = one_step(f, drive_on ? 1 : 0);
+    f->early = nullptr;
     f->es = nullptr;
     cudaStreamSynchronize(f->xst);
     GC_TRY(rc);

@@ -282,8 +282,13 @@ struct GcFused {
     cudaStream_t mst = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t xev[4] = {nullptr, nullptr, nullptr, nullptr};   // chunks of a host load / store
-    const gcf::EarlyStore* es = nullptr;   // set during gc_fused_step_store
-    cudaStream_t xst = nullptr;            // its copy stream
+    // outputs written while a step runs (gc_fused_step_store, the engine's
+    // write-back): called at four points of a host-driven step (0 after the
+    // integration and any rebuild, 1 after the density pass, 2 after the
+    // membrane passes, 3 at the end) with the step's stream
+    int (*early)(GcFused*, cudaStream_t, int) = nullptr;
+    const gcf::EarlyStore* es = nullptr;   // gc_fused_step_store's host buffers
+    cudaStream_t xst = nullptr;            // the stream of those writes
     cudaEvent_t xe[4] = {nullptr, nullptr, nullptr, nullptr};
     // membranes (global indices over the ensemble)
     int ncell = 0, ntri = 0, nedge = 0, ncp = 0;
@@ -364,6 +369,7 @@ int sync_dstep(GcFused* f);
 int rebuild_lists(GcFused* f);
 int launch_membranes(GcFused* f, cudaStream_t st, const GcParams& p);
 int build_morse_lists(GcFused* f, cudaStream_t st, const float4* mp, bool host);
+int ensure_early_stream(GcFused* f);
 int build_morse_lists_from_ref(GcFused* f, cudaStream_t st);
 int one_step(GcFused* f, int drive);
 int prepare_graph(GcFused* f, int drive);
