@@ -262,7 +262,7 @@ struct GcFused {
     size_t sortmem_bytes = 0;
     int sort_n = 0, sort_K = 0;
     GcSortBufs sb{};
-    void* sortmem_agg = nullptr;   // the aggregation sort's own temporaries: it runs beside the list rebuild
+    void* sortmem_agg = nullptr;   // the aggregation sort's own temporaries (the Morse list build)
     int sort_agg_n = 0, sort_agg_K = 0;
     // Morse Verlet lists: per vertex and lane the offset of its entries
     // (ncp x 8 + 1, scanned), the scan's block sums, the entries (membrane
