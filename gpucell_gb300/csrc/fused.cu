@@ -406,14 +406,17 @@ __global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, 
         // slot.  Entries go in groups of four: the indices of the next group
         // are loaded while the current group is evaluated, so that a thread
         // keeps four index loads and four position loads in flight; the
-        // acting-entry bits of each 32-entry word are stored once.
+        // acting-entry bits of each 32-entry word are stored once.  The
+        // lanes of a warp read each line of the list together, once: the
+        // index loads stream (evict first), so that the list does not push
+        // the particle data the gathers need out of the caches.
         const int c4 = (c + 3) & ~3;
         auto run = [&](auto wrap) {
             constexpr bool W = decltype(wrap)::value;
             int jq[4];
             if (c4 > 0) {
 #pragma unroll
-                for (int u = 0; u < 4; ++u) jq[u] = __ldg(lp + (size_t)u * 32);
+                for (int u = 0; u < 4; ++u) jq[u] = __ldcs(lp + (size_t)u * 32);
             }
             for (int w0 = 0; w0 < c4; w0 += 32) {
                 unsigned m = 0;
@@ -424,7 +427,7 @@ __global__ void __launch_bounds__(kMaxBS, GC_DENS_MIN_BLOCKS) fk_density(int n, 
                     for (int u = 0; u < 4; ++u) xj[u] = pos[jq[u]];
                     if (k0 + 4 < c4) {
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) jq[u] = __ldg(lp + (size_t)(k0 + 4 + u) * 32);
+                        for (int u = 0; u < 4; ++u) jq[u] = __ldcs(lp + (size_t)(k0 + 4 + u) * 32);
                     }
                     // without branches: W is formed for every entry and added
                     // (as +0 when the entry does not count, which leaves the sum
