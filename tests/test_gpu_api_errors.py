@@ -76,6 +76,8 @@ def test_bad_topology_and_call_order(cuda_device):
         set_cells(arrs)
         with pytest.raises(_lib.GcError, match="setup first"):
             _lib.call("gc_fused_step", h, 1, 1)
+        with pytest.raises(_lib.GcError, match="setup first"):
+            _lib.call("gc_fused_step_store", h, 1, *[C.c_void_p(0)] * 14)
         with pytest.raises(_lib.GcError, match="load the state"):
             _lib.call("gc_fused_setup", h)
         with pytest.raises(_lib.GcError, match="NULL"):
@@ -97,6 +99,7 @@ def test_bad_topology_and_call_order(cuda_device):
         with pytest.raises(_lib.GcError, match="contact"):
             _lib.call("gc_ensemble_rouleaux", h, 0, C.c_float(-1.0), C.c_void_p(0), C.c_void_p(0), C.byref(n))
         _lib.call("gc_fused_step", h, 3, 1)   # the handle still works after the refusals
+        _lib.call("gc_fused_step_store", h, 1, *[C.c_void_p(0)] * 14)   # a step, every output skipped
         flags = C.c_uint()
         _lib.call("gc_fused_flags", h, C.byref(flags))
         assert flags.value == 0
