@@ -17,11 +17,15 @@
 //     and no pair ever spans two systems.  Each slot carries its system
 //     index.  One simulation is an ensemble of one whose kernels take the
 //     system from their parameters instead of the table.
-//   * Neighbours come from Verlet lists with a skin: built from a 27-cube
-//     scan at cut-off rc + skin, stored 32 slots interleaved (entry k of slot
-//     i at ((i/32)*cap + k)*32 + i%32, so a warp reads 128 contiguous bytes
-//     per k), and rebuilt (with a re-sort) only when some particle has moved
-//     more than skin/2 since the last build.  Every step still tests
+//   * Neighbours come from Verlet lists with a skin: built from a scan of
+//     the cubes around each particle at cut-off rc + skin (5 x 5 x 5 cubes
+//     half that wide, rows and cells beyond the cut-off skipped; 27 cubes of
+//     full width where a periodic axis has fewer than five), stored 32 slots
+//     interleaved (entry k of slot i at ((i/32)*cap + k)*32 + i%32, so a
+//     warp reads 128 contiguous bytes per k), and rebuilt (with a re-sort)
+//     only when some particle has moved more than skin/2 since the last
+//     build.  The Morse aggregation's pairs (vertices of different cells)
+//     have lists of their own, built with these.  Every step still tests
 //     r^2 < rc^2 in FP32 on the listed pairs, with r^2 formed by fused
 //     multiply-adds (the boundary kernels and the oracle round each square:
 //     a pair within one rounding of the cut-off, where the kernel and its
