@@ -1101,11 +1101,11 @@ __global__ void __launch_bounds__(kAggBS) fk_mlist(int ncp, GcParams p, float cu
                                                    const unsigned* __restrict__ start,
                                                    const float4* __restrict__ mspos, const int* __restrict__ celltab,
                                                    const int2* __restrict__ cell_verts, unsigned* __restrict__ moff,
-                                                   int* __restrict__ mlist, unsigned mcap,
-                                                   unsigned* __restrict__ oflag) {
+                                                   unsigned* __restrict__ mcnt, int* __restrict__ mlist,
+                                                   unsigned mcap, unsigned* __restrict__ oflag) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = (int)(t / kAggLanes), k = (int)(t % kAggLanes);
-    if (q >= ncp) return;
+    if (q >= ncp) return;   // whole groups: kAggLanes divides the block
     const int v = order[q];
     const SysInfo& S = sys[msys ? msys[v] : 0];
     const GcGrid& g = S.mg;
@@ -1118,12 +1118,13 @@ __global__ void __launch_bounds__(kAggBS) fk_mlist(int ncp, GcParams p, float cu
         own_hi = S.cs + (unsigned)(cv.y - (int)S.m0);
     }
     const size_t slot = (size_t)v * kAggLanes + k;
-    unsigned w = 0, wend = 0;   // this lane's entries (FILL)
+    unsigned w = 0, wend = 0;   // this lane's entries (FILL): after the vertex's offset, the lower lanes' counts
     bool write = true;
     if (FILL) {
-        w = moff[slot];
-        wend = moff[slot + 1];
-        if (moff[(size_t)ncp * kAggLanes] > mcap) {   // the lists do not fit: the host grows them
+        w = moff[v];
+        for (int l = 0; l < k; ++l) w += mcnt[(size_t)v * kAggLanes + l];
+        wend = w + mcnt[slot];
+        if (moff[ncp] > mcap) {   // the lists do not fit: the host grows them
             write = false;
             if (k == 0 && q == 0) atomicOr(oflag, kMorseFull);
         }
@@ -1201,7 +1202,14 @@ __global__ void __launch_bounds__(kAggBS) fk_mlist(int ncp, GcParams p, float cu
             }
         }
     }
-    if (!FILL) moff[slot] = cnt;
+    if (!FILL) {
+        // this lane's count, and the vertex's total (the group's eight lanes)
+        mcnt[slot] = cnt;
+        const unsigned gm = 0xFFu << (threadIdx.x & 24);
+#pragma unroll
+        for (int o = kAggLanes / 2; o; o >>= 1) cnt += __shfl_xor_sync(gm, cnt, o, kAggLanes);
+        if (k == 0) moff[v] = cnt;
+    }
 }
 
 __global__ void __launch_bounds__(kAggBS) fk_maggl(int ncp, GcParams p, const SysInfo* __restrict__ sys,
@@ -1214,13 +1222,13 @@ __global__ void __launch_bounds__(kAggBS) fk_maggl(int ncp, GcParams p, const Sy
     // whole groups: kAggLanes divides the block.  Lists that did not fit
     // (raised as kMorseFull; the host runs the steps again with room) are
     // not read.
-    const bool live = v < ncp && moff[(size_t)ncp * kAggLanes] <= mcap;
+    const bool live = v < ncp && moff[ncp] <= mcap;
     float3 f = f3(0.f, 0.f, 0.f);
     if (live) {
         const GcGrid& g = sys[msys ? msys[v] : 0].mg;
         const float3 xi = xyz(mpos[v]);
         const float ai = parea[v];
-        const unsigned b = moff[(size_t)v * kAggLanes], e = moff[(size_t)(v + 1) * kAggLanes];
+        const unsigned b = moff[v], e = moff[v + 1];
         for (unsigned u = b + k; u < e; u += kAggLanes) {
             const int j = mlist[u];
             morse_pair<true>(p, g, xi, ai, mpos[j], parea + j, f);
@@ -1481,9 +1489,10 @@ int ensure_agg_sort_bufs(GcFused* f) {
 int build_morse_lists(GcFused* f, cudaStream_t st, const float4* mp, bool host) {
     if (!f->have_agg || f->ncp <= 0 || f->ncell <= 0) return GC_OK;
     const int ncp = f->ncp;
-    const size_t nl = (size_t)ncp * kAggLanes + 1;
+    const size_t nl = (size_t)ncp + 1;   // per vertex, scanned into offsets
     if (host && !f->moff) {
         GC_CUDA(cudaMalloc(&f->moff, nl * sizeof(unsigned)), "fused: Morse lists");
+        GC_CUDA(cudaMalloc(&f->mcnt, (size_t)ncp * kAggLanes * sizeof(unsigned)), "fused: Morse lists");
         GC_CUDA(cudaMalloc(&f->mscan, gc_scan_blocks((int)nl) * sizeof(unsigned)), "fused: Morse lists");
         drop_graphs(f);
     }
@@ -1500,12 +1509,12 @@ int build_morse_lists(GcFused* f, cudaStream_t st, const float4* mp, bool host) 
         constexpr bool F = decltype(fill)::value;
         if (f->agg_runs)
             fk_mlist<true, F><<<nba, kAggBS, 0, st>>>(ncp, f->p, cutl, f->dsys, f->msys, f->mvals, f->sb_agg.cnt,
-                                                      f->mspos, f->celltab, f->cell_verts, f->moff, f->mlist,
-                                                      (unsigned)f->mcap, f->oflag);
+                                                      f->mspos, f->celltab, f->cell_verts, f->moff, f->mcnt,
+                                                      f->mlist, (unsigned)f->mcap, f->oflag);
         else
             fk_mlist<false, F><<<nba, kAggBS, 0, st>>>(ncp, f->p, cutl, f->dsys, f->msys, f->mvals, f->sb_agg.cnt,
-                                                       f->mspos, f->celltab, f->cell_verts, f->moff, f->mlist,
-                                                       (unsigned)f->mcap, f->oflag);
+                                                       f->mspos, f->celltab, f->cell_verts, f->moff, f->mcnt,
+                                                       f->mlist, (unsigned)f->mcap, f->oflag);
         GC_CHECK_LAUNCH("fused: Morse lists");
         return GC_OK;
     };
@@ -2148,7 +2157,7 @@ int graph_segment(GcFused* f, int nsteps, int drive) {
         if (f->h->oflag & kMorseFull) {
             // the Morse lists: room for what the failed rebuild wanted
             unsigned need = 0;
-            GC_CUDA(cudaMemcpy(&need, f->moff + (size_t)f->ncp * kAggLanes, sizeof(unsigned), cudaMemcpyDeviceToHost),
+            GC_CUDA(cudaMemcpy(&need, f->moff + f->ncp, sizeof(unsigned), cudaMemcpyDeviceToHost),
                     "fused: Morse lists");
             const size_t want = (size_t)(1.5 * (need > f->mcap ? need : f->mcap)) + 4096;
             if (f->mlist) cudaFree(f->mlist);
@@ -3120,7 +3129,7 @@ int gc_fused_destroy(GcFused* f) {
     for (int c = 0; c < 4; ++c)
         if (f->xev[c]) cudaEventDestroy(f->xev[c]);
     if (f->sortmem_agg) cudaFree(f->sortmem_agg);
-    for (void* q : {(void*)f->moff, (void*)f->mscan, (void*)f->mlist, (void*)f->mref})
+    for (void* q : {(void*)f->moff, (void*)f->mcnt, (void*)f->mscan, (void*)f->mlist, (void*)f->mref})
         if (q) cudaFree(q);
     if (f->xst) cudaStreamSynchronize(f->xst);
     for (int k = 0; k < 4; ++k)

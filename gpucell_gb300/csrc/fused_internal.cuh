@@ -264,10 +264,12 @@ struct GcFused {
     GcSortBufs sb{};
     void* sortmem_agg = nullptr;   // the aggregation sort's own temporaries (the Morse list build)
     int sort_agg_n = 0, sort_agg_K = 0;
-    // Morse Verlet lists: per vertex and lane the offset of its entries
-    // (ncp x 8 + 1, scanned), the scan's block sums, the entries (membrane
-    // indices) and their capacity, and the membrane positions of a restore
+    // Morse Verlet lists: per vertex the offset of its entries (ncp + 1,
+    // scanned from the counts), per vertex and lane of the build the count,
+    // the scan's block sums, the entries (membrane indices) and their
+    // capacity, and the membrane positions of a restore
     unsigned* moff = nullptr;
+    unsigned* mcnt = nullptr;
     unsigned* mscan = nullptr;
     int* mlist = nullptr;
     size_t mcap = 0;
